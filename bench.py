@@ -1,0 +1,293 @@
+#!/usr/bin/env python
+"""Benchmark: cell-updates/s of the explicit first-order FV step on one GB300.
+
+Workload (default): single-phase Rusanov step on 2^24 cells, 64 seeded
+piecewise-constant segments (rho/rho0 log-uniform in [0.9, 1.1], |u| <= 0.5 b0
+in a uniform direction, A = R (I + 0.05 G)), CFL 0.5, frozen end cells, default
+Barton2009. One "step" = one time step over all cells. Inputs are larger than
+L2 (state 1.88 GB in FP64), so no L2 flush is needed between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the CPU restatement of the reference's step (the
+oracle, the same per-cell algorithm main.jl runs) on all host cores, each step
+a bounded window of the same workload. Prints one JSON line (rank 0).
+"""
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+LOCAL_RANK = int(os.environ.get("LOCAL_RANK", "0"))
+RANK = int(os.environ.get("RANK", "0"))
+WORLD = int(os.environ.get("WORLD_SIZE", "1"))
+if WORLD > 1:  # one process per GPU: each rank sees only its own device
+    os.environ["CUDA_VISIBLE_DEVICES"] = str(LOCAL_RANK)
+
+import numpy as np  # noqa: E402
+
+METRIC = "cell-updates/s"
+BYTES_PER_CELL_UPDATE = {"single": 224, "multi": 480}  # state read + write per cell-update (14 or 30 values x 8 B x 2)
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """dram bytes per cell for `kernel` from the committed ncu summary (profiles/ncu_traffic.txt)."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.txt")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        for line in fh:
+            parts = line.split()
+            if len(parts) >= 2 and not line.startswith("#") and parts[0] == kernel:
+                return float(parts[1])
+    return None
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle-reason samples every 200 ms during the timed region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self):
+        self.proc, self.path = None, None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(prefix="clocks_", suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200", "-i", os.environ.get("CUDA_VISIBLE_DEVICES", "0").split(",")[0]],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        time.sleep(0.25)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        time.sleep(0.25)
+        self.proc.terminate()
+        self.proc.wait()
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                for n, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(n)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def dist_setup():
+    if WORLD == 1:
+        return None
+    import torch.distributed as dist
+    dist.init_process_group("gloo")  # only timing scalars cross ranks; the problems are independent
+    return dist
+
+
+def dist_max(dist, x):
+    if dist is None:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def workload(n_cells, seed=None):
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300 import Hyperelasticity as H
+    from hyperelasticsolver_gb300._cases import segment_states, segment_fill
+    eos = h.Barton2009()
+    seg_p = segment_states(eos, 64) if seed is None else segment_states(eos, 64, seed)
+    seg_q = H.prim2cons(eos, seg_p)  # conservative segment states on the GPU
+    return eos, seg_q, segment_fill
+
+
+def config_block(args, precision):
+    return {"workload": f"single-phase Rusanov FV step, {args.n_cells} cells, 64 seeded segments, CFL 0.5",
+            "n_cells": args.n_cells, "model": "single-phase (Barton2009 default)", "flux": "rusanov",
+            "bc": "frozen", "cfl": 0.5, "precision": precision,
+            "l2": "inputs larger than L2 (state %.2f GB)" % (args.n_cells * 14 * 8 / 1e9)}
+
+
+def cpu_sample(Q0, target_s, nthreads):
+    """Time the oracle (the reference's per-cell algorithm, literal face evaluation)
+    on a window of the workload; returns (cell-updates/s, description)."""
+    import oracle
+    pb = oracle.problem(cfl=0.5)
+    nx = Q0.shape[1]
+    start = (nx * 37) // 64 - 2048
+    W = np.ascontiguousarray(Q0[:, start:start + 4096])
+    t0 = time.perf_counter()
+    oracle.run(pb, W, max_steps=1, nthreads=nthreads, literal=True)
+    per = (time.perf_counter() - t0) / W.shape[1]
+    cells = int(min(nx, max(4096, 2 ** round(math.log2(max(4096, 0.5 / per))))))
+    steps = max(1, int(target_s / (per * cells)))
+    start = max(0, (nx * 37) // 64 - cells // 2)
+    W = np.ascontiguousarray(Q0[:, start:start + cells])
+    t0 = time.perf_counter()
+    oracle.run(pb, W, max_steps=steps, nthreads=nthreads, literal=True)
+    el = time.perf_counter() - t0
+    return W.shape[1] * steps / el, f"{steps} steps of a {W.shape[1]}-cell window of the workload ({el:.1f} s)"
+
+
+def run_reference(args):
+    if RANK != 0:
+        return 0
+    import oracle
+    oracle.build()
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300._cases import segment_states, segment_fill
+    eos = h.Barton2009()
+    pb = oracle.problem(cfl=0.5)
+    seg_q = oracle.prim2cons(pb, segment_states(eos, 64))
+    nthreads = os.cpu_count()
+    # window size so that one step of the window takes about 0.25 s on all host cores
+    probe = segment_fill(seg_q, 4096)
+    t0 = time.perf_counter()
+    oracle.run(pb, probe, max_steps=1, nthreads=nthreads, literal=True)
+    per = (time.perf_counter() - t0) / 4096
+    cells = int(2 ** round(math.log2(max(4096, 0.25 / per))))
+    full = args.n_cells
+    start = (full * 37) // 64 - cells // 2
+    idx = np.arange(start, start + cells)
+    Q0 = np.ascontiguousarray(seg_q[(idx * 64) // full].T)
+    Q, _, _, _ = oracle.run(pb, Q0, max_steps=args.warmup, nthreads=nthreads, literal=True)
+    t0 = time.perf_counter()
+    oracle.run(pb, Q, max_steps=args.steps, nthreads=nthreads, literal=True)
+    el = time.perf_counter() - t0
+    v = cells * args.steps / el
+    sample = f"each step: a {cells}-cell window (around a segment boundary) of the {full}-cell workload"
+    line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": config_block(args, "fp64"),
+            "cpu_baseline": {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_ours(args):
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300._lib import PinnedArray
+    dist = dist_setup()
+    h.build_library()
+    eos, seg_q, segment_fill = workload(args.n_cells)
+    n, K, W = args.n_cells, args.steps, args.warmup
+    Q0 = segment_fill(seg_q, n)
+    state_bytes = Q0.nbytes
+    prec = args.precision
+    # ---- device-resident throughput --------------------------------------
+    s = h.Solver(eos, n, precision=prec, cfl=0.5)
+    s.upload(Q0)
+    s.step(max_steps=W)
+    s.set_profiling(True)
+    if dist:
+        dist.barrier()
+    clk = ClockSampler()
+    clk.start()
+    s.step(max_steps=K)
+    clocks = clk.stop()
+    tm = s.timing()
+    s.set_profiling(False)
+    ms_total = dist_max(dist, tm["ms_total"])
+    value = WORLD * n * K / (ms_total / 1e3)
+    # ---- end to end through the C ABI from pinned host memory -------------
+    pin_in, pin_out = PinnedArray(Q0.shape), PinnedArray(Q0.shape)
+    pin_in.array[...] = Q0
+    s.upload(pin_in.array)
+    s.step(max_steps=W)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    s.upload(pin_in.array)
+    for _ in range(K):
+        s.step(max_steps=1)  # per step the host reads back t (the reference logs Step/t/dt every step)
+    s.download(pin_out.array)
+    e2e_s = dist_max(dist, time.perf_counter() - t0)
+    e2e = WORLD * n * K / e2e_s
+    s.close()
+    pin_in.close()
+    pin_out.close()
+    # ---- roofline of the dominant kernel ----------------------------------
+    peak, peak_kind = measured_peaks()
+    kern = "cell" if tm["ms_cell"] >= tm["ms_update"] else "update"
+    ms_k = tm["ms_" + kern] / max(1, tm["n_" + kern])
+    alg = BYTES_PER_CELL_UPDATE["single"] * n
+    achieved = alg / (ms_k / 1e3) / 1e9
+    tr = ncu_traffic({"cell": "cell1_f64_kernel", "update": "update1_f64_kernel"}[kern])
+    if RANK != 0:
+        return 0
+    line = {
+        "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": WORLD, "steps": K, "warmup": W,
+        "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64" if prec == "fp64" else "f32+f32x2", "data": "synthetic",
+        "config": config_block(args, prec),
+        "clocks": clocks,
+        "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": state_bytes / K,
+                "d2h_bytes_per_step": state_bytes / K + 64},
+        "gpu_launches": tm["n_cell"] + tm["n_update"],
+        "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "peak_source": peak_kind,
+                     "traffic": (tr * n if tr is not None else None),
+                     "algorithmic_bytes_per_launch": alg,
+                     "ms_per_launch": ms_k,
+                     "step_hbm_frac": (BYTES_PER_CELL_UPDATE["single"] * n / (ms_total / K / 1e3) / 1e9) / peak},
+    }
+    if not args.no_cpu:
+        v, sample = cpu_sample(Q0, args.cpu_seconds, os.cpu_count())
+        line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": os.cpu_count(), "kind": "port", "sample": sample}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--n-cells", type=int, default=1 << 24)
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--cpu-seconds", type=float, default=12.0)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 1:
+        ap.error("--warmup must be >= 1")
+    return run_reference(args) if args.impl == "reference" else run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,66 @@
+"""EquationsOfState mirror (reference: EquationsOfState.jl) over the GPU C ABI.
+
+Functions accept one item (shape (9,)) or a batch (shape (n, 9)) and evaluate it
+with the same device code as the solver step.
+"""
+import numpy as np
+
+from . import _lib as L
+
+
+class Barton2009:
+    """Barton2009 EOS parameters (EquationsOfState.jl:71-116), same keyword names and defaults."""
+
+    def __init__(self, _rho0=8.93, _c0=4.6, _cv=3.9e-4, _t0=300, _b0=2.1, _alpha=1, _beta=3, _gamma=2):
+        self.rho0, self.c0, self.cv, self.t0 = float(_rho0), float(_c0), float(_cv), float(_t0)
+        self.b0, self.alpha, self.beta, self.gamma = float(_b0), float(_alpha), float(_beta), float(_gamma)
+        self.b0sq = self.b0 ** 2                               # :111
+        self.k0 = self.c0 ** 2 - (4 / 3) * self.b0 ** 2        # :112
+
+    def c(self):
+        return L.Barton2009C(self.rho0, self.c0, self.cv, self.t0, self.b0, self.alpha, self.beta, self.gamma)
+
+    def __repr__(self):
+        return (f"Barton2009(rho0={self.rho0}, c0={self.c0}, cv={self.cv}, t0={self.t0}, b0={self.b0}, "
+                f"alpha={self.alpha}, beta={self.beta}, gamma={self.gamma})")
+
+
+EoS = Barton2009
+
+
+def _scalar_vec(x, n):
+    return np.ascontiguousarray(np.broadcast_to(np.asarray(x, dtype=np.float64), (n,)))
+
+
+def _eval(fname, eos, s, M, k_out):
+    m, n, single = L.soa(M, 9)
+    s = _scalar_vec(s, n)
+    out = np.empty((k_out, n))
+    e = eos.c()
+    L.check(getattr(L.load(), fname)(e, L.ptr(s), L.ptr(m), L.ptr(out), n), what=fname)
+    if k_out == 1:
+        return out[0, 0] if single else out[0]
+    return L.unsoa(out, single)
+
+
+def energy(eos, S, G):
+    """Internal energy e(S, G) (EquationsOfState.jl:118-137)."""
+    return _eval("hyp_eval_energy", eos, S, G, 1)
+
+
+def entropy(eos, e_int, G):
+    """Entropy from internal energy, argument clamped at 1e-6 (EquationsOfState.jl:139-156)."""
+    return _eval("hyp_eval_entropy", eos, e_int, G, 1)
+
+
+def stress(eos, ent, F):
+    """Cauchy stress -2 rho G dE/dG, rho = rho0/det F (EquationsOfState.jl:179-190); column-major 9-vector."""
+    return _eval("hyp_eval_stress", eos, ent, F, 9)
+
+
+def acoustic(eos, ent, F, n=(1, 0, 0)):
+    """Acoustic tensor along n = e1 (EquationsOfState.jl:223-246) as a 3x3 matrix (or (n,3,3))."""
+    if tuple(np.asarray(n).tolist()) != (1, 0, 0):
+        raise NotImplementedError("the x-split solver evaluates the acoustic tensor along n = [1, 0, 0] only")
+    r = _eval("hyp_eval_acoustic", eos, ent, F, 9)
+    return r.reshape(3, 3, order="F") if r.ndim == 1 else r.reshape(-1, 3, 3).transpose(0, 2, 1)

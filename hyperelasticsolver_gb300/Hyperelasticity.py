@@ -1,0 +1,37 @@
+"""Single-phase model over the GPU C ABI: 14 values per cell (rho, rho u(3), rho E, rho A(9)).
+
+The reference's single-phase module (Hyperelasticity.jl) does not run against its
+current EOS API; its solver restates single-phase hyperelasticity as the per-phase
+functions of HyperelasticityMPh.jl with volume fraction alpha == 1, which is what
+these functions evaluate. Primitive layout: (rho, u(3), S, A(9)).
+"""
+import numpy as np
+
+from . import _lib as L
+from . import _model as M
+
+
+def _cfg(eos):
+    return M.config(eos, L.HYP_MODEL_SINGLE)
+
+
+def prim2cons(eos, P):
+    """(rho, u, S, A) -> (rho, rho u, rho E, rho A) (HyperelasticityMPh.jl:66-87 at alpha = 1)."""
+    return M.call("hyp_eval_prim2cons", _cfg(eos), P, 14, 14)
+
+
+def cons2prim(eos, Q):
+    """(HyperelasticityMPh.jl:106-133 at alpha = 1); rho = sqrt(det(rho A)/rho0)."""
+    return M.call("hyp_eval_cons2prim", _cfg(eos), Q, 14, 14)
+
+
+def flux(eos, Q):
+    """Physical x-flux (HyperelasticityMPh.jl:146-175 at alpha = 1)."""
+    return M.call("hyp_eval_flux", _cfg(eos), Q, 14, 14)
+
+
+def get_eigvals(eos, Q, n=(1, 0, 0)):
+    """u1 +- sqrt|eig(acoustic)| (HyperelasticityMPh.jl:258-266), 6 speeds."""
+    if tuple(np.asarray(n).tolist()) != (1, 0, 0):
+        raise NotImplementedError("the x-split solver evaluates wave speeds along n = [1, 0, 0] only")
+    return M.call("hyp_eval_eigvals", _cfg(eos), Q, 14, 6)

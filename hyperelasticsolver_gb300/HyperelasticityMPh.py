@@ -1,0 +1,41 @@
+"""HyperelasticityMPh mirror (reference: HyperelasticityMPh.jl): two-phase model, 30 values per cell.
+
+`eos` is a pair of Barton2009 (main.jl:134). Inputs are one cell (shape (30,)) or a batch (n, 30).
+"""
+import numpy as np
+
+from . import _lib as L
+from . import _model as M
+
+
+def _cfg(eos):
+    return M.config(eos, L.HYP_MODEL_MULTI)
+
+
+def prim2cons_mph(eos, P):
+    """Primitive [alpha, rho, u(3), S, A(9)] x 2 -> conservative (HyperelasticityMPh.jl:63-90)."""
+    return M.call("hyp_eval_prim2cons", _cfg(eos), P, 30, 30)
+
+
+def cons2prim_mph(eos, Q):
+    """Conservative -> primitive; density from det(alpha rho A) (HyperelasticityMPh.jl:99-133)."""
+    return M.call("hyp_eval_cons2prim", _cfg(eos), Q, 30, 30)
+
+
+def flux_mph(eos, Q):
+    """Physical x-flux of both phases (HyperelasticityMPh.jl:140-175)."""
+    return M.call("hyp_eval_flux", _cfg(eos), Q, 30, 30)
+
+
+def get_eigvals(eos, Q, n=(1, 0, 0)):
+    """Wave speeds u1 +- sqrt|eig(acoustic)| of both phases, n = e1 (HyperelasticityMPh.jl:252-266)."""
+    if tuple(np.asarray(n).tolist()) != (1, 0, 0):
+        raise NotImplementedError("the x-split solver evaluates wave speeds along n = [1, 0, 0] only")
+    return M.call("hyp_eval_eigvals", _cfg(eos), Q, 30, 12)
+
+
+def initial_states(eos, testcase):
+    """Left/right conservative states of the Riemann test cases (HyperelasticityMPh.jl:275-426)."""
+    from ._cases import mph_case
+    Pl, Pr = mph_case(testcase)
+    return prim2cons_mph(eos, Pl), prim2cons_mph(eos, Pr)

@@ -1,0 +1,23 @@
+"""NumFluxes mirror (reference: NumFluxes.jl) over the GPU C ABI."""
+import numpy as np
+
+from . import _lib as L
+from . import _model as M
+
+
+def lxf(eos, Q_l, Q_r, lam):
+    """Lax-Friedrichs / Rusanov face flux (NumFluxes.jl:25-60).
+
+    Returns (cons, D-, D+): cons = 0.5 (f(Q_l) + f(Q_r)) - 0.5 lam (Q_r - Q_l); the
+    path-conservative parts are zero for one phase. `eos` a Barton2009 selects the
+    single-phase model (14 values)."""
+    if isinstance(eos, (tuple, list)):
+        raise NotImplementedError("two-phase lxf is evaluated inside the solver step")
+    cfg = M.config(eos, L.HYP_MODEL_SINGLE)
+    l, n, single = L.soa(Q_l, 14)
+    r, _, _ = L.soa(Q_r, 14)
+    lam = np.ascontiguousarray(np.broadcast_to(np.asarray(lam, dtype=np.float64), (n,)))
+    cons, dm, dp = (np.empty((14, n)) for _ in range(3))
+    L.check(L.load().hyp_eval_lxf(cfg, L.ptr(l), L.ptr(r), L.ptr(lam), L.ptr(cons), L.ptr(dm), L.ptr(dp), n),
+            what="lxf")
+    return L.unsoa(cons, single), L.unsoa(dm, single), L.unsoa(dp, single)

@@ -1,0 +1,111 @@
+"""Initial data: the reference's Riemann test cases and the seeded synthetic workloads.
+
+`mph_case` restates the primitive left/right states of
+HyperelasticityMPh.initial_states (HyperelasticityMPh.jl:275-426); the values are
+the reference's test-case table. The other builders generate the synthetic
+single-phase workloads (primitive layout rho, u(3), S, A(9), column-major A).
+"""
+import numpy as np
+
+
+def _col(F):
+    return list(np.asarray(F, dtype=np.float64).reshape(-1, order="F"))
+
+
+def mph_case(testcase):
+    """Primitive 30-vectors (Pl, Pr) of HyperelasticityMPh.jl:275-426."""
+    I = np.eye(3)
+    F3 = np.array([[1.0, 0.0, 0.0], [-0.01, 0.95, 0.02], [-0.015, 0.0, 0.9]])
+    F5r = np.array([[1.0, 0.0, 0.0], [0.015, 0.95, 0.0], [-0.01, 0.0, 0.9]])
+    F4l = np.array([[0.98, 0.0, 0.0], [0.02, 1.0, 0.1], [0.0, 0.0, 1.0]])
+    F4r = np.array([[1.0, 0.0, 0.0], [0.0, 1.0, 0.1], [0.0, 0.0, 1.0]])
+    if testcase == 1:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.5, 0.5, 0.5, 0.5), 5.0, [0, 0, 0], [0, 0, 0], 0.0, 0.0, I, I
+    elif testcase == 2:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.5, 0.5, 0.5, 0.5), 5.0, [1.0, 0, 0], [1.0, 0, 0], 0.0, 0.0, I, I
+    elif testcase == 3:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.5, 0.5, 0.5, 0.5), 8.9, [2.0, 0.0, 0.1], [2.0, 0.0, 0.1], 0.0, 0.0, F3, F3
+    elif testcase == 4:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.5, 0.5, 0.5, 0.5), 8.9, [0.0, 0.5, 1.0], [0, 0, 0], 1e-3, 0.0, F4l, F4r
+    elif testcase == 5:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.5, 0.5, 0.5, 0.5), 8.9, [2.0, 0.0, 0.1], [0.0, -0.03, -0.01], 0.0, 0.0, F3, F5r
+    elif testcase == 6:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.1, 0.9, 0.9, 0.1), 8.9, [0.0, 0.5, 1.0], [0, 0, 0], 1e-3, 0.0, F4l, F4r
+    elif testcase == 7:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.1, 0.9, 0.9, 0.1), 8.9, [2.0, 0.0, 0.1], [0.0, -0.03, -0.01], 0.0, 0.0, F3, F5r
+    elif testcase == 10:
+        a, den, ul, ur, Sl, Sr, Fl, Fr = (0.4, 0.6, 0.6, 0.4), 8.9, [2.0, 0.0, 0.1], [2.0, 0.0, 0.1], 0.0, 0.0, F3, F3
+    else:
+        raise ValueError(f"unknown test case {testcase}")
+    al1, al2, ar1, ar2 = a
+    dl, dr = den / np.linalg.det(Fl), den / np.linalg.det(Fr)
+    Pl = [al1, dl, *ul, Sl, *_col(Fl), al2, dl, *ul, Sl, *_col(Fl)]
+    Pr = [ar1, dr, *ur, Sr, *_col(Fr), ar2, dr, *ur, Sr, *_col(Fr)]
+    return np.array(Pl, dtype=np.float64), np.array(Pr, dtype=np.float64)
+
+
+def riemann_1ph(eos, u_l=(0.0, 0.5, 1.0), u_r=(0.0, -0.5, -1.0), A_l=(1 / 0.98, 1.0, 1.0), A_r=(1.0, 1.0, 1.0), S=0.0):
+    """Single-phase Riemann primitive states (rho, u, S, A): velocities in units of b0,
+    diagonal distortions, density rho0/det(A) (consistent with cons2prim's density)."""
+    def prim(u, Ad):
+        A = np.diag(Ad)
+        return np.array([eos.rho0 / np.linalg.det(A), *(np.asarray(u) * eos.b0), S, *_col(A)])
+    return prim(u_l, A_l), prim(u_r, A_r)
+
+
+def initial_condition(Ql, Qr, nx):
+    """Two-state Riemann fill, (i-1) < nx/2 on the left (main.jl:99-106). Returns SoA (nvar, nx)."""
+    Ql, Qr = np.asarray(Ql, dtype=np.float64), np.asarray(Qr, dtype=np.float64)
+    left = (np.arange(nx) < nx / 2)[None, :]
+    return np.ascontiguousarray(np.where(left, Ql[:, None], Qr[:, None]))
+
+
+def random_rotation(rng):
+    """Haar-random rotation (QR of a Gaussian matrix with sign fix, det +1)."""
+    q, r = np.linalg.qr(rng.standard_normal((3, 3)))
+    q = q * np.sign(np.diag(r))
+    if np.linalg.det(q) < 0:
+        q[:, 0] = -q[:, 0]
+    return q
+
+
+SEGMENT_SEED = 20261204  # first seed from 20261203 whose 63 boundaries all survive 320 steps
+
+
+def segment_states(eos, n_seg=64, seed=SEGMENT_SEED, shared_rotation=True):
+    """Primitive states of the seeded piecewise-constant workload: per segment
+    rho/rho0 log-uniform in [0.9, 1.1], |u| uniform in [0, 0.5 b0] along a uniform
+    direction, A = R (I + 0.05 G) (G standard Gaussian, resampled until det > 0)
+    rescaled so that rho0/det(A) equals the drawn rho, S = 0. R is one random
+    rotation shared by all segments (shared_rotation=True) or drawn per segment.
+    Returns an (n_seg, 14) array.
+
+    With a rotation per segment the Rusanov dissipation averages distortions of
+    different orientation across a segment boundary and det(rho A) reaches 0
+    within a few hundred steps at about a third of the boundaries (the reference
+    raises DomainError there), so the workload shares one rotation."""
+    rng = np.random.default_rng(seed)
+    R_shared = random_rotation(np.random.default_rng(seed + 1))
+    out = np.empty((n_seg, 14))
+    for s in range(n_seg):
+        rho = eos.rho0 * np.exp(rng.uniform(np.log(0.9), np.log(1.1)))
+        v = rng.standard_normal(3)
+        v /= np.linalg.norm(v)
+        u = v * rng.uniform(0.0, 0.5 * eos.b0)
+        while True:
+            A = np.eye(3) + 0.05 * rng.standard_normal((3, 3))
+            if np.linalg.det(A) > 0:
+                break
+        R = random_rotation(rng)
+        A = (R_shared if shared_rotation else R) @ A
+        A *= (eos.rho0 / (rho * np.linalg.det(A))) ** (1.0 / 3.0)
+        out[s] = [rho, *u, 0.0, *_col(A)]
+    return out
+
+
+def segment_fill(states, nx):
+    """Broadcast per-segment conservative (or primitive) states to nx cells: SoA (k, nx)."""
+    states = np.asarray(states)
+    n_seg = states.shape[0]
+    seg = (np.arange(nx, dtype=np.int64) * n_seg) // nx
+    return np.ascontiguousarray(states[seg].T)

@@ -1,0 +1,335 @@
+// hyp_capi.cu -- context lifecycle, transfers and the step driver of the C ABI.
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include "hyp_internal.cuh"
+
+using namespace hyp;
+
+#define CK(call)                                                                           \
+  do {                                                                                     \
+    cudaError_t _e = (call);                                                               \
+    if (_e != cudaSuccess) return set_err(c, HYP_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(_e)); \
+  } while (0)
+
+static int set_err(hyp_ctx* c, int code, const std::string& msg) {
+  if (c) c->err = msg;
+  return code;
+}
+
+static const char* kNoCtx = "no context";
+
+extern "C" const char* hyp_last_error(const hyp_ctx* c) { return c ? c->err.c_str() : kNoCtx; }
+extern "C" int64_t hyp_error_cell(const hyp_ctx* c) { return c ? c->err_cell : -1; }
+
+static EosC to_eos(const hyp_barton2009& b) {
+  return make_eos(b.rho0, b.c0, b.cv, b.t0, b.b0, b.alpha, b.beta, b.gamma);
+}
+
+static bool valid_eos(const hyp_barton2009& b) {
+  return b.rho0 > 0 && b.cv > 0 && b.t0 > 0 && b.alpha != 0 && std::isfinite(b.c0) && std::isfinite(b.b0) &&
+         std::isfinite(b.beta) && std::isfinite(b.gamma);
+}
+
+static int free_ctx(hyp_ctx* c) {
+  if (!c) return HYP_OK;
+  cudaSetDevice(c->device);
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int p = 0; p < 2; ++p) {
+    if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
+    cudaFree(c->Q[p]);
+  }
+  cudaFree(c->F);
+  cudaFree(c->lam);
+  cudaFree(c->st);
+  if (c->st_host) cudaFreeHost(c->st_host);
+  for (auto& e : c->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto& e : c->prof_ev) cudaEventDestroy(e);
+  if (c->stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return HYP_OK;
+}
+
+extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
+  if (!cfg || !out) return HYP_ERR_INVALID;
+  *out = nullptr;
+  if (cfg->n_cells < 3 || cfg->x_length <= 0 || !(cfg->cfl > 0)) return HYP_ERR_INVALID;
+  if (cfg->model != HYP_MODEL_SINGLE && cfg->model != HYP_MODEL_MULTI) return HYP_ERR_INVALID;
+  if (cfg->flux < HYP_FLUX_RUSANOV || cfg->flux > HYP_FLUX_HLL) return HYP_ERR_INVALID;
+  if (cfg->bc != HYP_BC_FROZEN && cfg->bc != HYP_BC_TRANSMISSIVE) return HYP_ERR_INVALID;
+  if (cfg->precision != HYP_PREC_FP64 && cfg->precision != HYP_PREC_MIXED) return HYP_ERR_INVALID;
+  if (!valid_eos(cfg->eos[0]) || (cfg->model == HYP_MODEL_MULTI && !valid_eos(cfg->eos[1]))) return HYP_ERR_INVALID;
+  if (cfg->model != HYP_MODEL_SINGLE || cfg->flux == HYP_FLUX_HLL || cfg->precision != HYP_PREC_FP64)
+    return HYP_ERR_UNSUPPORTED;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
+  hyp_ctx* c = new (std::nothrow) hyp_ctx();
+  if (!c) return HYP_ERR_INVALID;
+  for (auto& e : c->ev) e = nullptr;
+  c->cfg = *cfg;
+  c->eos[0] = to_eos(cfg->eos[0]);
+  c->eos[1] = to_eos(cfg->model == HYP_MODEL_MULTI ? cfg->eos[1] : cfg->eos[0]);
+  c->n = cfg->n_cells;
+  c->nvar = cfg->model == HYP_MODEL_SINGLE ? 14 : 30;
+  int rc = HYP_OK;
+  auto fail = [&](cudaError_t e, const char* what) {
+    rc = HYP_ERR_CUDA;
+    fprintf(stderr, "hyp_create: %s: %s\n", what, cudaGetErrorString(e));
+  };
+  cudaError_t e;
+  if ((e = cudaGetDevice(&c->device)) != cudaSuccess) fail(e, "cudaGetDevice");
+  if (rc == HYP_OK && (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
+    fail(e, "cudaStreamCreate");
+  const size_t nq = (size_t)c->nvar * c->n * sizeof(double);
+  for (int p = 0; p < 2 && rc == HYP_OK; ++p)
+    if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");
+  if (rc == HYP_OK && (e = cudaMalloc(&c->F, (size_t)kNFlux1 * c->n * sizeof(double))) != cudaSuccess)
+    fail(e, "cudaMalloc(F)");
+  if (rc == HYP_OK && (e = cudaMalloc(&c->lam, (size_t)c->n * sizeof(double))) != cudaSuccess)
+    fail(e, "cudaMalloc(lam)");
+  if (rc == HYP_OK && (e = cudaMalloc(&c->st, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMalloc(state)");
+  if (rc == HYP_OK && (e = cudaMallocHost(&c->st_host, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMallocHost");
+  for (auto& ev : c->ev)
+    if (rc == HYP_OK && (e = cudaEventCreate(&ev)) != cudaSuccess) fail(e, "cudaEventCreate");
+  if (rc == HYP_OK) {
+    std::memset(c->st_host, 0, sizeof(DevState));
+    if ((e = cudaMemcpy(c->st, c->st_host, sizeof(DevState), cudaMemcpyHostToDevice)) != cudaSuccess)
+      fail(e, "cudaMemcpy(state)");
+  }
+  if (rc != HYP_OK) {
+    free_ctx(c);
+    return rc;
+  }
+  *out = c;
+  return HYP_OK;
+}
+
+extern "C" int hyp_destroy(hyp_ctx* c) { return free_ctx(c); }
+
+static int sync_state(hyp_ctx* c) {
+  CK(cudaMemcpyAsync(c->st_host, c->st, sizeof(DevState), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return HYP_OK;
+}
+
+static int check_cell_error(hyp_ctx* c) {
+  int code = c->st_host->err_code;
+  if (!code) return HYP_OK;
+  c->err_cell = c->st_host->err_cell;
+  char buf[160];
+  if (code & HYP_CELL_NEG_DET) {
+    snprintf(buf, sizeof buf, "det(rho A) <= 0 in cell %lld (reference: DomainError in sqrt)", (long long)c->err_cell);
+    return set_err(c, HYP_ERR_NEG_DET, buf);
+  }
+  snprintf(buf, sizeof buf, "non-finite state or wave speed in cell %lld", (long long)c->err_cell);
+  return set_err(c, HYP_ERR_NONFINITE, buf);
+}
+
+extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_vars, double t0) {
+  if (!c || !Q) return HYP_ERR_INVALID;
+  if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_upload: size mismatch");
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(c->Q[0], Q, (size_t)n_vars * n_cells * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  std::memset(c->st_host, 0, sizeof(DevState));
+  c->st_host->t[0] = c->st_host->t[1] = t0;
+  CK(cudaMemcpyAsync(c->st, c->st_host, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  c->cur = 0;
+  c->t_host = t0;
+  c->steps_host = 0;
+  c->err_cell = -1;
+  return HYP_OK;
+}
+
+extern "C" int hyp_download(hyp_ctx* c, double* Q, int64_t n_cells, int n_vars) {
+  if (!c || !Q) return HYP_ERR_INVALID;
+  if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_download: size mismatch");
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemcpyAsync(Q, c->Q[c->cur], (size_t)n_vars * n_cells * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  CK(cudaStreamSynchronize(c->stream));
+  return HYP_OK;
+}
+
+// Enqueue one step of parity p (no host synchronisation). With profiling on,
+// each kernel is bracketed by events taken from the context's pool; the
+// durations are summed when hyp_step finishes.
+static int prof_event(hyp_ctx* c, cudaEvent_t* out) {
+  if (c->prof_used == c->prof_ev.size()) {
+    cudaEvent_t e;
+    CK(cudaEventCreate(&e));
+    c->prof_ev.push_back(e);
+  }
+  *out = c->prof_ev[c->prof_used++];
+  return HYP_OK;
+}
+
+static int enqueue_step(hyp_ctx* c, int p, double t_end, bool prof) {
+  cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
+  int rc;
+  if (prof) {
+    if ((rc = prof_event(c, &e0)) || (rc = prof_event(c, &e1)) || (rc = prof_event(c, &e2))) return rc;
+    CK(cudaEventRecord(e0, c->stream));
+  }
+  CK(launch_cell1_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
+  if (prof) CK(cudaEventRecord(e1, c->stream));
+  CK(launch_update1_f64(c, p, t_end));
+  if (prof) CK(cudaEventRecord(e2, c->stream));
+  return HYP_OK;
+}
+
+static int collect_profile(hyp_ctx* c) {
+  for (size_t k = 0; k + 3 <= c->prof_used; k += 3) {
+    float a = 0.f, b = 0.f;
+    CK(cudaEventElapsedTime(&a, c->prof_ev[k], c->prof_ev[k + 1]));
+    CK(cudaEventElapsedTime(&b, c->prof_ev[k + 1], c->prof_ev[k + 2]));
+    c->timing.ms_cell += a;
+    c->timing.ms_update += b;
+    c->timing.n_cell += 1;
+    c->timing.n_update += 1;
+  }
+  c->prof_used = 0;
+  return HYP_OK;
+}
+
+static constexpr int kGraphSteps = 16;  // steps per captured graph (even)
+
+static int ensure_graph(hyp_ctx* c, int p, double t_end) {
+  if (c->graph[p] && c->graph_t_end == t_end && c->graph_steps == kGraphSteps) return HYP_OK;
+  if (c->graph_t_end != t_end || c->graph_steps != kGraphSteps) {
+    for (int q = 0; q < 2; ++q)
+      if (c->graph[q]) {
+        cudaGraphExecDestroy(c->graph[q]);
+        c->graph[q] = nullptr;
+      }
+  }
+  cudaGraph_t g;
+  CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = HYP_OK;
+  for (int s = 0; s < kGraphSteps && rc == HYP_OK; ++s) rc = enqueue_step(c, (p + s) & 1, t_end, false);
+  cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+  if (rc != HYP_OK) return rc;
+  if (e != cudaSuccess) return set_err(c, HYP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+  e = cudaGraphInstantiate(&c->graph[p], g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return set_err(c, HYP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+  c->graph_t_end = t_end;
+  c->graph_steps = kGraphSteps;
+  return HYP_OK;
+}
+
+extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done, double* t_out) {
+  if (!c) return HYP_ERR_INVALID;
+  if (std::isnan(t_end)) return set_err(c, HYP_ERR_INVALID, "t_end is NaN");
+  CK(cudaSetDevice(c->device));
+  const bool unlimited = max_steps <= 0;
+  if (unlimited && std::isinf(t_end)) return set_err(c, HYP_ERR_INVALID, "hyp_step: neither max_steps nor t_end bounds the run");
+  c->timing = StepTiming();
+  c->prof_used = 0;
+  const long long steps0 = c->steps_host;
+  CK(cudaEventRecord(c->ev[0], c->stream));
+  int launched = 0;
+  const bool prof = c->profiling != 0;
+  // With a finite t_end, steps past t_end are no-ops on the device; launch in
+  // chunks and stop once the device reports t >= t_end.
+  const int chunk = std::isinf(t_end) ? (unlimited ? 0 : max_steps) : 256;
+  int rc = HYP_OK;
+  while (rc == HYP_OK) {
+    int todo = unlimited ? chunk : (max_steps - launched);
+    if (!std::isinf(t_end) && todo > chunk) todo = chunk;
+    if (todo <= 0) break;
+    // every launched step flips the parity (an inactive step copies t across and
+    // leaves Q alone; only active steps move the current buffer)
+    int p = (int)((c->cur + launched) & 1);
+    int s = 0;
+    if (!prof) {
+      while (rc == HYP_OK && todo - s >= kGraphSteps) {
+        rc = ensure_graph(c, p, t_end);
+        if (rc == HYP_OK) {
+          cudaError_t e = cudaGraphLaunch(c->graph[p], c->stream);
+          if (e != cudaSuccess) rc = set_err(c, HYP_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+        }
+        s += kGraphSteps;  // even: parity unchanged
+      }
+    }
+    for (; rc == HYP_OK && s < todo; ++s) {
+      rc = enqueue_step(c, p, t_end, prof);
+      p ^= 1;
+    }
+    launched += todo;
+    if (rc != HYP_OK) break;
+    if (!std::isinf(t_end)) {
+      rc = sync_state(c);
+      if (rc != HYP_OK) break;
+      if (c->st_host->err_code) break;
+      double tl = c->st_host->t[(c->cur + launched) & 1];
+      if (!(tl < t_end)) break;
+    }
+    if (std::isinf(t_end)) break;
+  }
+  CK(cudaEventRecord(c->ev[1], c->stream));
+  if (rc == HYP_OK) rc = sync_state(c);
+  if (rc != HYP_OK) return rc;
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, c->ev[0], c->ev[1]));
+  c->timing.ms_total = ms;
+  if (prof && (rc = collect_profile(c)) != HYP_OK) return rc;
+  const long long active = c->st_host->steps - steps0;
+  c->cur = (int)((c->cur + active) & 1);
+  c->steps_host = c->st_host->steps;
+  c->t_host = c->st_host->t[c->cur];
+  if (steps_done) *steps_done = (int)active;
+  if (t_out) *t_out = c->t_host;
+  return check_cell_error(c);
+}
+
+extern "C" int hyp_max_wavespeed(hyp_ctx* c, double* out) {
+  if (!c || !out) return HYP_ERR_INVALID;
+  CK(cudaSetDevice(c->device));
+  CK(cudaMemsetAsync(&c->st->lam_query, 0, sizeof(unsigned long long), c->stream));
+  CK(launch_cell1_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
+  int rc = sync_state(c);
+  if (rc != HYP_OK) return rc;
+  unsigned long long b = c->st_host->lam_query;
+  double v;
+  std::memcpy(&v, &b, sizeof v);
+  *out = v;
+  return check_cell_error(c);
+}
+
+extern "C" int hyp_get_time(const hyp_ctx* c, double* t, int64_t* steps) {
+  if (!c) return HYP_ERR_INVALID;
+  if (t) *t = c->t_host;
+  if (steps) *steps = c->steps_host;
+  return HYP_OK;
+}
+
+extern "C" int hyp_set_profiling(hyp_ctx* c, int on) {
+  if (!c) return HYP_ERR_INVALID;
+  c->profiling = on;
+  return HYP_OK;
+}
+
+extern "C" int hyp_last_timing(const hyp_ctx* c, double* ms_total, double* ms_cell, int* n_cell, double* ms_update,
+                               int* n_update) {
+  if (!c) return HYP_ERR_INVALID;
+  if (ms_total) *ms_total = c->timing.ms_total;
+  if (ms_cell) *ms_cell = c->timing.ms_cell;
+  if (n_cell) *n_cell = c->timing.n_cell;
+  if (ms_update) *ms_update = c->timing.ms_update;
+  if (n_update) *n_update = c->timing.n_update;
+  return HYP_OK;
+}
+
+extern "C" int hyp_host_alloc(int64_t bytes, void** out) {
+  if (!out || bytes <= 0) return HYP_ERR_INVALID;
+  *out = nullptr;
+  cudaError_t e = cudaMallocHost(out, (size_t)bytes);
+  return e == cudaSuccess ? HYP_OK : HYP_ERR_CUDA;
+}
+
+extern "C" int hyp_host_free(void* p) {
+  if (!p) return HYP_OK;
+  return cudaFreeHost(p) == cudaSuccess ? HYP_OK : HYP_ERR_CUDA;
+}

@@ -1,0 +1,81 @@
+// hyp_internal.cuh -- context, device-side step state and kernel launchers
+// shared by the translation units of libhyperelastic_cuda.so.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include <string>
+#include <vector>
+#include "../../include/hyperelastic.h"
+#include "hyp_physics.cuh"
+
+namespace hyp {
+
+constexpr int kBlock = 256;
+
+// Device-resident loop control of one context. The step kernels read the
+// input slot of t / lam_max and write the other slot, so a sequence of steps
+// needs no host round trip (and can be captured in a CUDA graph).
+struct DevState {
+  double t[2];                        // time before the step of parity p is t[p]
+  unsigned long long lam_bits[2];     // max wave speed of the state of parity p (bits of a double >= 0)
+  unsigned long long lam_query;       // hyp_max_wavespeed slot
+  long long steps;                    // steps taken
+  int err_code;                       // first HYP_CELL_* status raised (0 = none)
+  int pad_;
+  long long err_cell;                 // cell that raised it
+};
+
+// Per-cell flux components that are not identically zero for one phase:
+// mass, momentum(3), energy and rows 2-3 of rho*A (row 1 of the rho*A flux is
+// den*(u1 A[0,b] - u1 A[0,b]) = 0 exactly, HyperelasticityMPh.jl:172).
+constexpr int kNFlux1 = 11;
+__host__ __device__ __forceinline__ int flux_slot1(int v) {
+  // v: index in the 14-vector [rho, rho u(3), rho E, rho A(9)]; -1 = zero flux
+  if (v < 5) return v;
+  int a = (v - 5) % 3;  // row of rho*A
+  if (a == 0) return -1;
+  int b = (v - 5) / 3;
+  return 5 + 2 * b + (a - 1);
+}
+
+struct StepTiming {
+  float ms_total = 0.f, ms_cell = 0.f, ms_update = 0.f;
+  int n_cell = 0, n_update = 0;
+};
+
+}  // namespace hyp
+
+struct hyp_ctx {
+  hyp_config cfg;
+  hyp::EosC eos[2];
+  int device = 0;
+  int nvar = 14;
+  int64_t n = 0;
+  cudaStream_t stream = nullptr;
+  // FP64 state, double-buffered: Q[p] is the state before a step of parity p.
+  double* Q[2] = {nullptr, nullptr};
+  double* F = nullptr;     // per-cell fluxes (scratch)
+  double* lam = nullptr;   // per-cell max wave speed (scratch)
+  hyp::DevState* st = nullptr;
+  hyp::DevState* st_host = nullptr;  // pinned mirror
+  int cur = 0;             // parity of the buffer that holds the current state
+  long long steps_host = 0;
+  double t_host = 0.0;
+  int profiling = 0;
+  cudaEvent_t ev[8];
+  std::vector<cudaEvent_t> prof_ev;  // profiling: 3 events per step
+  size_t prof_used = 0;
+  hyp::StepTiming timing;
+  // CUDA graph of an even number of steps, per starting parity
+  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  int graph_steps = 0;
+  double graph_t_end = 0.0;
+  std::string err;
+  int64_t err_cell = -1;
+};
+
+namespace hyp {
+// single-phase FP64 kernels (hyp_step1.cu)
+cudaError_t launch_cell1_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
+cudaError_t launch_update1_f64(hyp_ctx* c, int p, double t_end);
+}  // namespace hyp

@@ -1,0 +1,429 @@
+// hyp_physics.cuh -- per-cell hyperelastic physics in closed form (FP64).
+//
+// Restates, for one phase of one cell, the chain the reference evaluates with
+// ForwardDiff and LAPACK:
+//   cons2prim            HyperelasticityMPh.jl:106-133
+//   finger, invariants   Strains.jl:26-32, 46-52
+//   energy, entropy      EquationsOfState.jl:118-137, 139-156   (Barton2009)
+//   stress               EquationsOfState.jl:179-190  sigma = -2 rho G dE/dG
+//   acoustic (n = e1)    EquationsOfState.jl:223-246
+//   get_eigvals          HyperelasticityMPh.jl:258-266  u1 +- sqrt|eig(acoustic)|
+//   flux                 HyperelasticityMPh.jl:146-175
+// The reference differentiates the energy numerically-exactly with dual
+// numbers; here the same derivatives are written in closed form:
+//   dE/dG = E1 I + E2 (i1 I - G) + E3 p M,   M = A A^T = G^-1, p = det G,
+//   G dE/dG = cG G + cGG G^2 + cI I,  cG = E1 + E2 i1, cGG = -E2, cI = E3 p,
+// and the acoustic tensor needs only the three directional derivatives of
+// row 1 of sigma along dA = e_j A[0,:]:  dG = -(G e_j e_0^T + e_0 e_j^T G),
+// d i1 = -2 G0j, d i2 = -2 i1 G0j + 2 (G^2)0j, d p = -2 p [j==0],
+// d rho_s = -rho_s [j==0].  Only the spectral radius of that tensor is used
+// (max |u1 +- c| = |u1| + c_max, and the HLL bounds u1 -+ c_max), so the
+// eigen-solve returns max |mu| of the 3x3 matrix.
+//
+// Written as __host__ __device__ code with no CUDA intrinsics so that the
+// same source can be compiled on the host by the unit tests.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#ifndef HYP_HD
+#ifdef __CUDACC__
+#define HYP_HD __host__ __device__ __forceinline__
+#else
+#define HYP_HD inline
+#endif
+#endif
+
+namespace hyp {
+
+// Barton2009 parameters with the derived constants the closed forms use.
+struct EosC {
+  double rho0, inv_rho0, cv, t0, cvt0, inv_cvt0;
+  double alpha, beta, gamma;
+  double b0sq, k0;
+  double kU;       // 0.5 k0 / alpha^2          (cold energy prefactor)
+  double kE3a;     // k0 / (2 alpha)            (dUcold/dp prefactor)
+  double kE3b;     // b0sq * beta / 4           (dW/dp prefactor)
+  double kE3g;     // cv t0 gamma / 2           (d thermal / dp prefactor)
+  int default_exp; // alpha == 1, beta == 3, gamma == 2 (integer-power fast path)
+};
+
+HYP_HD EosC make_eos(double rho0, double c0, double cv, double t0, double b0, double alpha, double beta,
+                     double gamma) {
+  EosC e;
+  e.rho0 = rho0;
+  e.inv_rho0 = 1.0 / rho0;
+  e.cv = cv;
+  e.t0 = t0;
+  e.cvt0 = cv * t0;
+  e.inv_cvt0 = 1.0 / e.cvt0;
+  e.alpha = alpha;
+  e.beta = beta;
+  e.gamma = gamma;
+  e.b0sq = b0 * b0;                          // EquationsOfState.jl:111
+  e.k0 = c0 * c0 - (4.0 / 3.0) * (b0 * b0);  // EquationsOfState.jl:112
+  e.kU = 0.5 * e.k0 / (alpha * alpha);
+  e.kE3a = e.k0 / (2.0 * alpha);
+  e.kE3b = e.b0sq * beta / 4.0;
+  e.kE3g = e.cvt0 * gamma / 2.0;
+  e.default_exp = (alpha == 1.0 && beta == 3.0 && gamma == 2.0) ? 1 : 0;
+  return e;
+}
+
+// Symmetric 3x3 stored as (00, 11, 22, 01, 02, 12).
+struct Sym {
+  double a00, a11, a22, a01, a02, a12;
+};
+HYP_HD double sym_at(const Sym& s, int i, int j) {
+  if (i == j) return i == 0 ? s.a00 : (i == 1 ? s.a11 : s.a22);
+  int k = i + j;  // 1: (0,1), 2: (0,2), 3: (1,2)
+  return k == 1 ? s.a01 : (k == 2 ? s.a02 : s.a12);
+}
+
+// Powers of p = i3 = det G needed by the energy and its first two p-derivatives.
+struct Pows {
+  double Pa, Pa1, Pa2;  // p^(a/2), p^(a/2-1), p^(a/2-2)   a = alpha
+  double Pb, Pb1, Pb2;  // beta
+  double Pg, Pg1, Pg2;  // gamma
+  double inv_Pg;
+};
+
+// Kinematic quantities of the distortion A (column-major 9-vector).
+struct Kin {
+  Sym G;     // Finger tensor G = (A A^T)^-1   (Strains.jl:26-32)
+  Sym H;     // G^2
+  double i1, i2, p;  // invariants (Strains.jl:46-52); p = i3 = det G
+  double s, inv_s;   // sqrt(p) = 1/det A and det A
+  double psi;        // i1^2/3 - i2
+};
+
+// A -> G, G^2, invariants. `detA` is det(A) (> 0 for admissible states).
+HYP_HD Kin kinematics(const double* A, double detA) {
+  Kin k;
+  // M = A A^T (symmetric)
+  double m00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+  double m11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+  double m22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+  double m01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+  double m02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+  double m12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+  k.inv_s = detA;
+  k.s = 1.0 / detA;
+  k.p = k.s * k.s;  // det G = 1/det(M) = 1/det(A)^2
+  // G = adj(M) / det(M) = adj(M) * p
+  k.G.a00 = (m11 * m22 - m12 * m12) * k.p;
+  k.G.a11 = (m00 * m22 - m02 * m02) * k.p;
+  k.G.a22 = (m00 * m11 - m01 * m01) * k.p;
+  k.G.a01 = (m02 * m12 - m01 * m22) * k.p;
+  k.G.a02 = (m01 * m12 - m02 * m11) * k.p;
+  k.G.a12 = (m01 * m02 - m00 * m12) * k.p;
+  const Sym& g = k.G;
+  k.H.a00 = g.a00 * g.a00 + g.a01 * g.a01 + g.a02 * g.a02;
+  k.H.a11 = g.a01 * g.a01 + g.a11 * g.a11 + g.a12 * g.a12;
+  k.H.a22 = g.a02 * g.a02 + g.a12 * g.a12 + g.a22 * g.a22;
+  k.H.a01 = g.a00 * g.a01 + g.a01 * g.a11 + g.a02 * g.a12;
+  k.H.a02 = g.a00 * g.a02 + g.a01 * g.a12 + g.a02 * g.a22;
+  k.H.a12 = g.a01 * g.a02 + g.a11 * g.a12 + g.a12 * g.a22;
+  k.i1 = g.a00 + g.a11 + g.a22;
+  double trH = k.H.a00 + k.H.a11 + k.H.a22;
+  k.i2 = 0.5 * (k.i1 * k.i1 - trH);
+  k.psi = k.i1 * k.i1 / 3.0 - k.i2;
+  return k;
+}
+
+HYP_HD double det3(const double* m) {  // column-major, cofactor expansion (SimpleLA.jl:84-89)
+  return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
+         m[6] * (m[1] * m[5] - m[4] * m[2]);
+}
+
+HYP_HD Pows powers(const EosC& e, const Kin& k) {
+  Pows w;
+  if (e.default_exp) {  // alpha = 1, beta = 3, gamma = 2: p^(n/2) = s^n
+    double s = k.s, is = k.inv_s, ip = is * is;
+    w.Pa = s;         w.Pa1 = is;  w.Pa2 = is * ip;
+    w.Pb = s * k.p;   w.Pb1 = s;   w.Pb2 = is;
+    w.Pg = k.p;       w.Pg1 = 1.0; w.Pg2 = ip;
+    w.inv_Pg = ip;
+  } else {
+    double lp = log(k.p), ip = 1.0 / k.p;
+    w.Pa = exp(0.5 * e.alpha * lp); w.Pa1 = w.Pa * ip; w.Pa2 = w.Pa1 * ip;
+    w.Pb = exp(0.5 * e.beta * lp);  w.Pb1 = w.Pb * ip; w.Pb2 = w.Pb1 * ip;
+    w.Pg = exp(0.5 * e.gamma * lp); w.Pg1 = w.Pg * ip; w.Pg2 = w.Pg1 * ip;
+    w.inv_Pg = 1.0 / w.Pg;
+  }
+  return w;
+}
+
+// Cold (Ucold) and shear (W) parts of the Barton2009 energy (EquationsOfState.jl:129-134).
+HYP_HD double e_cold(const EosC& e, const Pows& w) { return e.kU * (w.Pa - 1.0) * (w.Pa - 1.0); }
+HYP_HD double e_shear(const EosC& e, const Kin& k, const Pows& w) { return 0.5 * e.b0sq * w.Pb * k.psi; }
+
+// x - 1 with x the entropy argument of EquationsOfState.jl:150-154 (clamped at
+// 1e-6); exp(S/cv) - 1 of the energy equals it because S = cv log x.
+HYP_HD double entropy_xm1(const EosC& e, double e_int, const Kin& k, const Pows& w) {
+  double xm1 = (e_int - e_shear(e, k, w) - e_cold(e, w)) * e.inv_cvt0 * w.inv_Pg;
+  if (xm1 + 1.0 < 1e-6) xm1 = 1e-6 - 1.0;
+  return xm1;
+}
+
+// Stress coefficients: G dE/dG = cG G + cGG G^2 + cI I (with S fixed).
+struct StressC {
+  double cG, cGG, cI, E3;
+};
+HYP_HD StressC stress_coeffs(const EosC& e, const Kin& k, const Pows& w, double xm1) {
+  StressC c;
+  double E1 = (e.b0sq / 3.0) * w.Pb * k.i1;
+  double E2 = -0.5 * e.b0sq * w.Pb;
+  c.E3 = e.kE3a * (w.Pa - 1.0) * w.Pa1 + e.kE3g * w.Pg1 * xm1 + e.kE3b * w.Pb1 * k.psi;
+  c.cG = E1 + E2 * k.i1;
+  c.cGG = -E2;
+  c.cI = c.E3 * k.p;
+  return c;
+}
+
+// Row 1 of sigma = -2 rho_s (cG G + cGG G^2 + cI I).
+HYP_HD void stress_row0(double rho_s, const Kin& k, const StressC& c, double* s0) {
+  double m = -2.0 * rho_s;
+  s0[0] = m * (c.cG * k.G.a00 + c.cGG * k.H.a00 + c.cI);
+  s0[1] = m * (c.cG * k.G.a01 + c.cGG * k.H.a01);
+  s0[2] = m * (c.cG * k.G.a02 + c.cGG * k.H.a02);
+}
+HYP_HD void stress_full(double rho_s, const Kin& k, const StressC& c, double* sig) {
+  double m = -2.0 * rho_s;
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i)
+      sig[i + 3 * j] = m * (c.cG * sym_at(k.G, i, j) + c.cGG * sym_at(k.H, i, j) + (i == j ? c.cI : 0.0));
+}
+
+// Acoustic tensor Omega[i][j] = (1/rho_s) d_j sigma[0,i] (EquationsOfState.jl:223-246, n = e1),
+// written column-major: om[i + 3 j].
+HYP_HD void acoustic_omega(const EosC& e, const Kin& k, const Pows& w, const StressC& c, double xm1,
+                           const double* s0_over_rho, double* om) {
+  const double bs6 = e.b0sq / 6.0;
+  for (int j = 0; j < 3; ++j) {
+    double G0j = sym_at(k.G, 0, j), H0j = sym_at(k.H, 0, j);
+    double di1 = -2.0 * G0j;
+    double dpsi = (2.0 / 3.0) * k.i1 * G0j - 2.0 * H0j;
+    double dcG, dcGG, dE3, dcI;
+    if (j == 0) {
+      double dp = -2.0 * k.p;
+      double dPb = 0.5 * e.beta * w.Pb1 * dp;
+      double dPa = 0.5 * e.alpha * w.Pa1 * dp;
+      double dPa1 = (0.5 * e.alpha - 1.0) * w.Pa2 * dp;
+      double dPg1 = (0.5 * e.gamma - 1.0) * w.Pg2 * dp;
+      double dPb1 = (0.5 * e.beta - 1.0) * w.Pb2 * dp;
+      dcG = -bs6 * (dPb * k.i1 + w.Pb * di1);
+      dcGG = 0.5 * e.b0sq * dPb;
+      dE3 = e.kE3a * (dPa * w.Pa1 + (w.Pa - 1.0) * dPa1) + e.kE3g * dPg1 * xm1 +
+            e.kE3b * (dPb1 * k.psi + w.Pb1 * dpsi);
+      dcI = dE3 * k.p + c.E3 * dp;
+    } else {
+      dcG = -bs6 * w.Pb * di1;
+      dcGG = 0.0;
+      dE3 = e.kE3b * w.Pb1 * dpsi;
+      dcI = dE3 * k.p;
+    }
+    for (int i = 0; i < 3; ++i) {
+      double G0i = sym_at(k.G, 0, i), H0i = sym_at(k.H, 0, i);
+      double Gij = sym_at(k.G, i, j), Hij = sym_at(k.H, i, j);
+      double Gi0 = G0i;
+      double dG0i = -(G0j * (i == 0 ? 1.0 : 0.0) + Gij);
+      double dH0i = -(G0j * Gi0 + Hij + H0j * (i == 0 ? 1.0 : 0.0) + k.G.a00 * Gij);
+      double v = dcG * G0i + c.cG * dG0i + dcGG * H0i + c.cGG * dH0i + (i == 0 ? dcI : 0.0);
+      om[i + 3 * j] = -2.0 * v - (j == 0 ? s0_over_rho[i] : 0.0);
+    }
+  }
+}
+
+// Eigenvalue moduli of a real 3x3 (column-major). Characteristic polynomial
+// mu^3 - c2 mu^2 + c1 mu - c0; single-precision closed-form seeds
+// (trigonometric for three real roots, Cardano otherwise), three FP64 Newton
+// steps on the seed of largest modulus (a real root r), and deflation to the
+// quadratic mu^2 - (c2 - r) mu + c0/r for the other two (a complex pair has
+// modulus sqrt(c0/r)). Returns |r| and the two other moduli.
+HYP_HD void eig_core(const double* a, double* mods) {
+  double c2 = a[0] + a[4] + a[8];
+  double c1 = (a[0] * a[4] - a[3] * a[1]) + (a[0] * a[8] - a[6] * a[2]) + (a[4] * a[8] - a[7] * a[5]);
+  double c0 = det3(a);
+  float C2 = (float)c2, C1 = (float)c1, C0 = (float)c0;
+  float p = C1 - C2 * C2 * (1.0f / 3.0f);
+  float q = -2.0f / 27.0f * C2 * C2 * C2 + C2 * C1 * (1.0f / 3.0f) - C0;
+  float disc = 0.25f * q * q + p * p * p * (1.0f / 27.0f);
+  float seed;
+  if (disc < 0.0f && p < 0.0f) {
+    float m = 2.0f * sqrtf(-p * (1.0f / 3.0f));
+    float cc = fminf(1.0f, fmaxf(-1.0f, 3.0f * q / (p * m)));
+    float th = acosf(cc) * (1.0f / 3.0f);
+    float y0 = m * cosf(th) + C2 * (1.0f / 3.0f);
+    float y1 = m * cosf(th - 2.0943951f) + C2 * (1.0f / 3.0f);
+    float y2 = m * cosf(th - 4.1887902f) + C2 * (1.0f / 3.0f);
+    seed = y0;
+    if (fabsf(y1) > fabsf(seed)) seed = y1;
+    if (fabsf(y2) > fabsf(seed)) seed = y2;
+  } else {
+    float sd = sqrtf(fmaxf(disc, 0.0f));
+    seed = cbrtf(-0.5f * q + sd) + cbrtf(-0.5f * q - sd) + C2 * (1.0f / 3.0f);
+  }
+  double r = (double)seed;
+  for (int it = 0; it < 3; ++it) {
+    double f = ((r - c2) * r + c1) * r - c0;
+    double fp = (3.0 * r - 2.0 * c2) * r + c1;
+    r = (fp != 0.0) ? r - f / fp : r;
+  }
+  double s, qq;
+  if (r != 0.0) {
+    s = c2 - r;
+    qq = c0 / r;
+  } else {  // singular: the other roots solve mu^2 - c2 mu + c1
+    s = c2;
+    qq = c1;
+  }
+  double dsc = s * s - 4.0 * qq;
+  mods[0] = fabs(r);
+  if (dsc < 0.0) {
+    mods[1] = mods[2] = sqrt(fabs(qq));
+  } else {
+    double sq = sqrt(dsc);
+    double ra = s >= 0.0 ? 0.5 * (s + sq) : 0.5 * (s - sq);
+    mods[1] = fabs(ra);
+    mods[2] = ra != 0.0 ? fabs(qq / ra) : fabs(s - ra);
+  }
+}
+// Largest eigenvalue modulus (what the step consumes).
+HYP_HD double spectral_radius(const double* a) {
+  double m[3];
+  eig_core(a, m);
+  return fmax(m[0], fmax(m[1], m[2]));
+}
+// All three moduli, descending (the function-level get_eigvals).
+HYP_HD void eig_moduli3(const double* a, double* mods) {
+  double v[3];
+  eig_core(a, v);
+  for (int i = 0; i < 3; ++i)
+    for (int j = i + 1; j < 3; ++j)
+      if (v[j] > v[i]) { double t = v[i]; v[i] = v[j]; v[j] = t; }
+  mods[0] = v[0]; mods[1] = v[1]; mods[2] = v[2];
+}
+
+// ---- per-cell, per-phase evaluation ---------------------------------------
+
+// Status bits a cell can raise (reported through the context's error word).
+enum { HYP_CELL_OK = 0, HYP_CELL_NEG_DET = 1, HYP_CELL_NONFINITE = 2 };
+
+// Primitive quantities of one phase: alpha, stored alpha*rho (unused, as in the
+// reference), alpha*rho*u, alpha*rho*E, alpha*rho*A.
+struct Prim {
+  double den, true_den, inv_den;  // alpha*rho_true, rho_true, 1/(alpha*rho_true)
+  double u[3], E, e_int;
+  double A[9];
+  double xm1;                     // exp(S/cv) - 1 (clamped entropy argument minus one)
+  Kin k;
+  Pows w;
+};
+
+// HyperelasticityMPh.jl:106-133. Returns HYP_CELL_* status.
+HYP_HD int cons_to_prim(const EosC& e, double alpha, const double* m, double rhoE, const double* rA, Prim& P) {
+  double FQ[9];
+  double ia = 1.0 / alpha;
+  for (int c = 0; c < 9; ++c) FQ[c] = rA[c] * ia;
+  double d = det3(FQ);
+  int st = d > 0.0 ? HYP_CELL_OK : HYP_CELL_NEG_DET;
+  P.true_den = sqrt(d * e.inv_rho0);
+  P.den = alpha * P.true_den;
+  P.inv_den = 1.0 / P.den;
+  for (int c = 0; c < 3; ++c) P.u[c] = m[c] * P.inv_den;
+  P.E = rhoE * P.inv_den;
+  P.e_int = P.E - 0.5 * (P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2]);
+  for (int c = 0; c < 9; ++c) P.A[c] = rA[c] * P.inv_den;
+  // det A = det(rA/den) = d alpha^3 / den^3 = rho0 / true_den  ->  1/det A = true_den / rho0
+  double detA = e.rho0 / P.true_den;
+  P.k = kinematics(P.A, detA);
+  P.w = powers(e, P.k);
+  P.xm1 = entropy_xm1(e, P.e_int, P.k, P.w);
+  if (!(P.e_int == P.e_int) || !(P.xm1 == P.xm1) || !isfinite(P.k.p)) st |= HYP_CELL_NONFINITE;
+  return st;
+}
+
+// Physical x-flux of one phase, the 14 entries after alpha (HyperelasticityMPh.jl:146-175):
+// [alpha*rho u1, momentum(3), energy, alpha*rho*A(9)], plus row 1 of sigma.
+HYP_HD void phase_flux(const EosC& e, double alpha, const Prim& P, const StressC& c, double* f, double* s0) {
+  double rho_s = e.rho0 * P.k.s;  // rho0 / det A (EquationsOfState.jl:180)
+  stress_row0(rho_s, P.k, c, s0);
+  s0[0] *= alpha; s0[1] *= alpha; s0[2] *= alpha;
+  double du = P.den * P.u[0];
+  f[0] = du;
+  f[1] = du * P.u[0] - s0[0];
+  f[2] = du * P.u[1] - s0[1];
+  f[3] = du * P.u[2] - s0[2];
+  f[4] = du * P.E - (P.u[0] * s0[0] + P.u[1] * s0[1] + P.u[2] * s0[2]);
+  for (int b = 0; b < 3; ++b)
+    for (int a = 0; a < 3; ++a) f[5 + a + 3 * b] = P.den * (P.u[0] * P.A[a + 3 * b] - P.u[a] * P.A[3 * b]);
+}
+
+// Largest acoustic wave speed sqrt(max |eig(acoustic)|) of one phase.
+HYP_HD double phase_cmax(const EosC& e, const Prim& P, const StressC& c) {
+  double rho_s = e.rho0 * P.k.s;
+  double s0[3], s0r[3], om[9];
+  stress_row0(rho_s, P.k, c, s0);
+  for (int i = 0; i < 3; ++i) s0r[i] = s0[i] / rho_s;
+  acoustic_omega(e, P.k, P.w, c, P.xm1, s0r, om);
+  return sqrt(spectral_radius(om));
+}
+
+// ---- function-level forms with the reference's signatures -----------------
+
+// stress(eos, ent, F) (EquationsOfState.jl:179-190): full 3x3, column-major.
+HYP_HD void stress_SF(const EosC& e, double S, const double* F, double* sig) {
+  Kin k = kinematics(F, det3(F));
+  Pows w = powers(e, k);
+  StressC c = stress_coeffs(e, k, w, exp(S / e.cv) - 1.0);
+  stress_full(e.rho0 * k.s, k, c, sig);
+}
+// acoustic(eos, ent, F, [1,0,0]) (EquationsOfState.jl:223-246), column-major.
+HYP_HD void acoustic_SF(const EosC& e, double S, const double* F, double* om) {
+  Kin k = kinematics(F, det3(F));
+  Pows w = powers(e, k);
+  double xm1 = exp(S / e.cv) - 1.0;
+  StressC c = stress_coeffs(e, k, w, xm1);
+  double rho_s = e.rho0 * k.s, s0[3], s0r[3];
+  stress_row0(rho_s, k, c, s0);
+  for (int i = 0; i < 3; ++i) s0r[i] = s0[i] / rho_s;
+  acoustic_omega(e, k, w, c, xm1, s0r, om);
+}
+// Invariants of a general (not necessarily symmetric) G (Strains.jl:46-52).
+HYP_HD void invariants_general(const double* g, double* out) {
+  double i1 = g[0] + g[4] + g[8];
+  double trg2 = 0.0;
+  for (int i = 0; i < 3; ++i)
+    for (int k = 0; k < 3; ++k) trg2 += g[i + 3 * k] * g[k + 3 * i];
+  out[0] = i1;
+  out[1] = 0.5 * (i1 * i1 - trg2);
+  out[2] = det3(g);
+}
+HYP_HD double pow_half(const EosC& e, double p, double a) { return e.default_exp ? pow(p, 0.5 * a) : exp(0.5 * a * log(p)); }
+// energy(eos, S, G) (EquationsOfState.jl:118-137)
+HYP_HD double energy_SG(const EosC& e, double S, const double* G) {
+  double i[3];
+  invariants_general(G, i);
+  double pa = pow_half(e, i[2], e.alpha) - 1.0;
+  return e.kU * pa * pa + e.cvt0 * pow_half(e, i[2], e.gamma) * (exp(S / e.cv) - 1.0) +
+         0.5 * e.b0sq * pow_half(e, i[2], e.beta) * (i[0] * i[0] / 3.0 - i[1]);
+}
+// entropy(eos, e, G) (EquationsOfState.jl:139-156)
+HYP_HD double entropy_eG(const EosC& e, double eint, const double* G) {
+  double i[3];
+  invariants_general(G, i);
+  double pa = pow_half(e, i[2], e.alpha) - 1.0;
+  double x = eint - 0.5 * e.b0sq * pow_half(e, i[2], e.beta) * (i[0] * i[0] / 3.0 - i[1]) - e.kU * pa * pa;
+  x = x / (e.cvt0 * pow_half(e, i[2], e.gamma)) + 1.0;
+  if (x < 1e-6) x = 1e-6;
+  return log(x) * e.cv;
+}
+// finger(A) = (A A^T)^-1, column-major 9-vector (Strains.jl:26-32)
+HYP_HD void finger_A(const double* A, double* g) {
+  Kin k = kinematics(A, det3(A));
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) g[i + 3 * j] = sym_at(k.G, i, j);
+}
+
+}  // namespace hyp

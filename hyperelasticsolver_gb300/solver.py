@@ -1,0 +1,89 @@
+"""The explicit time loop of main.jl:202-241 on the GPU (one context = one problem)."""
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib as L
+from . import _model as M
+
+_MODELS = {"single": L.HYP_MODEL_SINGLE, "multi": L.HYP_MODEL_MULTI}
+_FLUXES = {"rusanov": L.HYP_FLUX_RUSANOV, "lxf": L.HYP_FLUX_LXF, "hll": L.HYP_FLUX_HLL}
+_BCS = {"frozen": L.HYP_BC_FROZEN, "transmissive": L.HYP_BC_TRANSMISSIVE}
+_PRECS = {"fp64": L.HYP_PREC_FP64, "mixed": L.HYP_PREC_MIXED}
+
+
+class Solver:
+    """Device-resident solver state for one 1D problem.
+
+    Parameters mirror the reference driver's globals (main.jl:133-152):
+    eos (one Barton2009, or a pair for the two-phase model), nx, X, cfl, and
+    the flux choice of main.jl:223-225. State arrays are SoA (nvar, nx)."""
+
+    def __init__(self, eos, nx, model="single", flux="rusanov", bc="frozen", precision="fp64", X=1.0, cfl=0.5):
+        self.model = _MODELS[model]
+        self.nvar = M.nvar(self.model)
+        self.nx = int(nx)
+        self.cfg = M.config(eos, self.model, nx, _FLUXES[flux], _BCS[bc], _PRECS[precision], X, cfl)
+        lib = L.load()
+        h = ctypes.c_void_p()
+        L.check(lib.hyp_create(self.cfg, ctypes.byref(h)), what="hyp_create")
+        self._h = h
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().hyp_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, Q, t0=0.0):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        if Q.shape != (self.nvar, self.nx):
+            raise ValueError(f"state must be SoA {(self.nvar, self.nx)}, got {Q.shape}")
+        L.check(L.load().hyp_upload(self._h, L.ptr(Q), self.nx, self.nvar, float(t0)), self._h, "hyp_upload")
+
+    def download(self, out=None):
+        out = np.empty((self.nvar, self.nx)) if out is None else out
+        L.check(L.load().hyp_download(self._h, L.ptr(out), self.nx, self.nvar), self._h, "hyp_download")
+        return out
+
+    def step(self, max_steps=0, t_end=math.inf):
+        """Advance like `while t < T` (main.jl:202); returns (steps taken, t)."""
+        s = ctypes.c_int(0)
+        t = ctypes.c_double(0.0)
+        L.check(L.load().hyp_step(self._h, int(max_steps), float(t_end), ctypes.byref(s), ctypes.byref(t)),
+                self._h, "hyp_step")
+        return s.value, t.value
+
+    def max_wavespeed(self):
+        v = ctypes.c_double(0.0)
+        L.check(L.load().hyp_max_wavespeed(self._h, ctypes.byref(v)), self._h, "hyp_max_wavespeed")
+        return v.value
+
+    def time(self):
+        t = ctypes.c_double(0.0)
+        s = ctypes.c_int64(0)
+        L.check(L.load().hyp_get_time(self._h, ctypes.byref(t), ctypes.byref(s)), self._h, "hyp_get_time")
+        return t.value, s.value
+
+    def set_profiling(self, on):
+        L.check(L.load().hyp_set_profiling(self._h, int(bool(on))), self._h, "hyp_set_profiling")
+
+    def timing(self):
+        a, b, d = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        nc, nu = ctypes.c_int(), ctypes.c_int()
+        L.check(L.load().hyp_last_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(nc), ctypes.byref(d),
+                                         ctypes.byref(nu)), self._h, "hyp_last_timing")
+        return {"ms_total": a.value, "ms_cell": b.value, "n_cell": nc.value, "ms_update": d.value,
+                "n_update": nu.value}

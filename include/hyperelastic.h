@@ -1,0 +1,150 @@
+/*
+ * hyperelastic.h -- C ABI of libhyperelastic_cuda.so, the GB300 (sm_103a)
+ * explicit first-order finite-volume step of BlackSiberian/HyperelasticSolver.
+ *
+ * The reference is a set of pure Julia functions called per cell from a
+ * threaded driver loop. This library replaces that hot path with whole-array,
+ * device-resident calls. Every entry point below names the reference interface
+ * it stands in for (file:line in the reference project).
+ *
+ * Conventions
+ *  - Status: every function returns int, HYP_OK (0) on success; no exception
+ *    or longjmp crosses the ABI. hyp_last_error() gives a message for a context.
+ *  - Arrays are structure-of-arrays, double precision, in HOST memory unless a
+ *    name says otherwise: x[k * n + i] is component k of cell/item i (a Julia
+ *    Matrix{Float64}(n, k) has exactly this layout).
+ *  - 3x3 tensors are column-major 9-vectors, as the reference's reshape(x,(3,3)).
+ *  - Single-phase state (14 per cell): rho, rho*u(3), rho*E, rho*A(9) -- the
+ *    reference's per-phase 15-vector (HyperelasticityMPh.jl:80-84) with the
+ *    volume fraction alpha == 1 dropped. Two-phase state (30 per cell): the
+ *    reference's [alpha, alpha*rho, alpha*rho*u(3), alpha*rho*E, alpha*rho*A(9)]
+ *    for phase 1 then phase 2.
+ *  - A context owns one CUDA stream and its device buffers; it is not
+ *    thread-safe, the library is (one context per host thread).
+ */
+#ifndef HYPERELASTIC_H
+#define HYPERELASTIC_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* status codes */
+#define HYP_OK 0
+#define HYP_ERR_INVALID 1     /* null pointer, bad size, bad enum                          */
+#define HYP_ERR_CUDA 2        /* CUDA runtime error (message in hyp_last_error)            */
+#define HYP_ERR_NEG_DET 3     /* det(rho A) <= 0 in a cell: the reference's sqrt DomainError
+                                 (HyperelasticityMPh.jl:114)                                 */
+#define HYP_ERR_NONFINITE 4   /* non-finite state, wave speed or time step                 */
+#define HYP_ERR_TIMEOUT 5     /* a bounded device-side wait gave up                         */
+#define HYP_ERR_UNSUPPORTED 6 /* option combination not implemented                         */
+#define HYP_ERR_NO_DEVICE 7   /* no CUDA device                                             */
+
+enum { HYP_MODEL_SINGLE = 1, HYP_MODEL_MULTI = 2 };
+/* numerical flux: Rusanov (local max speed per face, main.jl:45-48 with NumFluxes.lxf),
+   Lax-Friedrichs (lambda = dx/dt, main.jl:223, 30-41), path-conservative HLL
+   (NumFluxes.jl:70-132, main.jl:225) */
+enum { HYP_FLUX_RUSANOV = 0, HYP_FLUX_LXF = 1, HYP_FLUX_HLL = 2 };
+/* boundary: end cells frozen as main.jl:219-220, or zero-gradient (transmissive) ghosts */
+enum { HYP_BC_FROZEN = 0, HYP_BC_TRANSMISSIVE = 1 };
+/* arithmetic: plain FP64, or FP32 fluxes with a compensated hi/lo FP32 state */
+enum { HYP_PREC_FP64 = 0, HYP_PREC_MIXED = 1 };
+
+/* Barton2009 primary parameters (EquationsOfState.jl:71-116); b0sq and k0 are derived.
+   Defaults of the reference constructor: 8.93, 4.6, 3.9e-4, 300, 2.1, 1, 3, 2. */
+typedef struct {
+  double rho0, c0, cv, t0, b0, alpha, beta, gamma;
+} hyp_barton2009;
+
+typedef struct {
+  int64_t n_cells;     /* nx (main.jl:143)                                      */
+  int model;           /* HYP_MODEL_*                                           */
+  int flux;            /* HYP_FLUX_*                                            */
+  int bc;              /* HYP_BC_*                                              */
+  int precision;       /* HYP_PREC_*                                            */
+  double x_length;     /* X, domain [0, X] (main.jl:140); dx = X / nx           */
+  double cfl;          /* main.jl:144                                           */
+  hyp_barton2009 eos[2]; /* eos[1] is used by the two-phase model only (main.jl:134) */
+} hyp_config;
+
+typedef struct hyp_ctx hyp_ctx;
+
+/* ---- solver context: the time loop of main.jl:202-241 -------------------- */
+
+/* Create a context on the current CUDA device; allocates the state buffers. */
+int hyp_create(const hyp_config* cfg, hyp_ctx** out);
+int hyp_destroy(hyp_ctx* ctx);
+/* Message of the last failure on this context (never NULL). */
+const char* hyp_last_error(const hyp_ctx* ctx);
+/* Cell index recorded with the last HYP_ERR_NEG_DET / HYP_ERR_NONFINITE, or -1. */
+int64_t hyp_error_cell(const hyp_ctx* ctx);
+
+/* Copy a conservative state in (host SoA [n_vars][n_cells]); resets t to t0.
+   Replaces the driver's Q0 = initial_condition(...) (main.jl:99-106, 178-179). */
+int hyp_upload(hyp_ctx* ctx, const double* Q, int64_t n_cells, int n_vars, double t0);
+/* Copy the current conservative state out (host SoA). */
+int hyp_download(hyp_ctx* ctx, double* Q, int64_t n_cells, int n_vars);
+
+/* Advance while steps < max_steps (max_steps <= 0: no limit) and t < t_end
+   (t_end = +inf: no limit), exactly as `while t < T` of main.jl:202-241:
+   per step, wave speeds of every cell (:204-211), dt = cfl*dx/max lambda
+   (:212), t += dt (:214), update of the interior cells with frozen ends
+   (:218-226). Reports the steps taken and the new time. */
+int hyp_step(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double* t_out);
+
+/* max_i lambda_i of the current state, lambda_i = max |get_eigvals(Q_i)|
+   (main.jl:204-211; HyperelasticityMPh.jl:252-266). */
+int hyp_max_wavespeed(hyp_ctx* ctx, double* out);
+
+/* Current time and step count of the context. */
+int hyp_get_time(const hyp_ctx* ctx, double* t, int64_t* steps);
+
+/* Device timing of the last hyp_step: total elapsed ms, and when profiling is
+   on, the summed ms and launch count of the per-cell flux/wave-speed kernel. */
+int hyp_set_profiling(hyp_ctx* ctx, int on);
+int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel, int* cell_launches,
+                    double* ms_update_kernel, int* update_launches);
+
+/* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
+int hyp_host_alloc(int64_t bytes, void** out);
+int hyp_host_free(void* p);
+
+/* ---- function-level evaluators (host arrays, n items, SoA) --------------- */
+/* Each runs the same device code as the step on n independent inputs.       */
+
+/* Strains.finger (Strains.jl:26-32): G = inv(A A^T).  A, G: [9][n] */
+int hyp_eval_finger(const double* A, double* G, int64_t n);
+/* Strains.invariants (Strains.jl:46-52): (tr G, (tr^2 G - tr G^2)/2, det G).  out: [3][n] */
+int hyp_eval_invariants(const double* G, double* out, int64_t n);
+/* EquationsOfState.energy(eos, S, G) (EquationsOfState.jl:118-137).  S, e: [n]; G: [9][n] */
+int hyp_eval_energy(const hyp_barton2009* eos, const double* S, const double* G, double* e, int64_t n);
+/* EquationsOfState.entropy(eos, e, G) (EquationsOfState.jl:139-156). */
+int hyp_eval_entropy(const hyp_barton2009* eos, const double* e, const double* G, double* S, int64_t n);
+/* EquationsOfState.stress(eos, ent, F) (EquationsOfState.jl:179-190).  sigma: [9][n] */
+int hyp_eval_stress(const hyp_barton2009* eos, const double* S, const double* F, double* sigma, int64_t n);
+/* EquationsOfState.acoustic(eos, ent, F, [1,0,0]) (EquationsOfState.jl:223-246).  [9][n] */
+int hyp_eval_acoustic(const hyp_barton2009* eos, const double* S, const double* F, double* ac, int64_t n);
+
+/* Model-level functions; cfg selects model and EOS (n_cells etc. ignored).
+   cons2prim / prim2cons (HyperelasticityMPh.jl:99-133, 63-90): per phase
+   [alpha, rho_true, u(3), S, A(9)] (single phase: alpha dropped). [nvar][n] */
+int hyp_eval_cons2prim(const hyp_config* cfg, const double* Q, double* P, int64_t n);
+int hyp_eval_prim2cons(const hyp_config* cfg, const double* P, double* Q, int64_t n);
+/* flux_mph / flux (HyperelasticityMPh.jl:140-175).  [nvar][n] */
+int hyp_eval_flux(const hyp_config* cfg, const double* Q, double* F, int64_t n);
+/* get_eigvals (HyperelasticityMPh.jl:252-266) with n = e1: per phase
+   u1 + c_k (k = 1..3) then u1 - c_k, c_k = sqrt|eig_k|, moduli in descending
+   order.  out: [6*phases][n] */
+int hyp_eval_eigvals(const hyp_config* cfg, const double* Q, double* out, int64_t n);
+/* NumFluxes.lxf(eos, Q_l, Q_r, lambda) (NumFluxes.jl:25-60): conservative part
+   and the path-conservative D-, D+.  Ql, Qr, cons, dm, dp: [nvar][n]; lambda: [n] */
+int hyp_eval_lxf(const hyp_config* cfg, const double* Ql, const double* Qr, const double* lambda, double* cons,
+                 double* dm, double* dp, int64_t n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* HYPERELASTIC_H */

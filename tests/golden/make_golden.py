@@ -1,0 +1,102 @@
+"""Writes tests/golden/golden_literal.json: 40-digit values of the reference's
+functions from the independent transliteration oracle/literal.py, for seeded
+inputs. Run from the repository root:  python tests/golden/make_golden.py
+"""
+import json
+import os
+import sys
+
+import numpy as np
+import mpmath as mp
+
+sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))))
+from oracle import literal as L  # noqa: E402
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden_literal.json")
+
+
+def f(x):
+    return float(L.val(x))
+
+
+def main():
+    rng = np.random.default_rng(20261203)
+    e = L.Barton()
+    e2 = L.Barton(b0=2.1 * np.sqrt(0.1))
+    g = {"eos": [8.93, 4.6, 3.9e-4, 300, 2.1, 1, 3, 2], "eos2_b0": 2.1 * float(np.sqrt(0.1)), "tensors": [],
+         "cells": [], "noncons": [], "hll": [], "rusanov": {}}
+    # tensor-level functions
+    for k in range(6):
+        F = np.eye(3) + 0.08 * rng.standard_normal((3, 3))
+        if np.linalg.det(F) <= 0:
+            F = np.eye(3)
+        Fv = [float(x) for x in F.reshape(-1, order="F")]
+        S = float(rng.uniform(0, 1.5e-3)) if k else 0.0
+        Fm = [mp.mpf(x) for x in Fv]
+        G = L.finger(Fm)
+        ac = L.acoustic(e, mp.mpf(S), Fm)
+        g["tensors"].append({
+            "F": Fv, "S": S,
+            "finger": [f(x) for x in G],
+            "invariants": [f(x) for x in L.invariants(G)],
+            "energy": f(L.energy(e, mp.mpf(S), G)),
+            "stress": [f(x) for x in L.stress(e, mp.mpf(S), Fm)],
+            "acoustic": [f(x) for x in ac],
+            "moduli": [float(x) for x in L.eig_moduli(ac)],
+        })
+    # single-phase cells (alpha = 1)
+    for k in range(4):
+        F = np.eye(3) + 0.05 * rng.standard_normal((3, 3))
+        u = rng.uniform(-1, 1, 3)
+        S = float(rng.uniform(0, 1e-3))
+        rho = 8.93 / np.linalg.det(F)
+        P = [1.0, rho, *u, S, *F.reshape(-1, order="F")]
+        Pm = [mp.mpf(float(x)) for x in P]
+        Q = L.prim2cons(e, Pm)
+        g["cells"].append({
+            "P": [float(x) for x in P],
+            "Q": [f(x) for x in Q],
+            "prim": [f(x) for x in L.cons2prim(e, Q)],
+            "flux": [f(x) for x in L.flux(e, Q)],
+            "speeds": [float(x) for x in L.speeds(e, Q)],
+        })
+    # two-phase non-conservative columns and an HLL face (test case 6 states, mixed)
+    from hyperelasticsolver_gb300._cases import mph_case
+    Pl, Pr = mph_case(6)
+    eos = (e, e2)
+    Ql = L.prim2cons(eos[0], [mp.mpf(float(x)) for x in Pl[:15]]) + L.prim2cons(eos[1], [mp.mpf(float(x)) for x in Pl[15:]])
+    Qr = L.prim2cons(eos[0], [mp.mpf(float(x)) for x in Pr[:15]]) + L.prim2cons(eos[1], [mp.mpf(float(x)) for x in Pr[15:]])
+    Ql = [mp.mpf(float(x)) for x in Ql]
+    Qr = [mp.mpf(float(x)) for x in Qr]
+    Qmix = [(a * 3 + b) / 4 for a, b in zip(Ql, Qr)]
+    Qmix = [mp.mpf(float(x)) for x in Qmix]
+    g["noncons"].append({"Q": [float(x) for x in Qmix], "bcol": [f(x) for x in L.noncons_cols(eos, Qmix)]})
+    spdL = L.speeds(eos[0], Ql[:15]) + L.speeds(eos[1], Ql[15:])
+    spdR = L.speeds(eos[0], Qr[:15]) + L.speeds(eos[1], Qr[15:])
+    dm, dp = L.hll(eos, Ql, Qr, spdL, spdR)
+    g["hll"].append({"Ql": [float(x) for x in Ql], "Qr": [float(x) for x in Qr],
+                     "spdL": [float(x) for x in spdL], "spdR": [float(x) for x in spdR],
+                     "dm": [f(x) for x in dm], "dp": [f(x) for x in dp]})
+    # two Rusanov steps on 6 cells (single phase, frozen ends)
+    cells = []
+    for k in range(6):
+        F = np.eye(3) + 0.03 * rng.standard_normal((3, 3))
+        u = rng.uniform(-0.5, 0.5, 3)
+        P = [1.0, 8.93 / np.linalg.det(F), *u, 0.0, *F.reshape(-1, order="F")]
+        Q = L.prim2cons(e, [mp.mpf(float(x)) for x in P])
+        cells.append([mp.mpf(float(x)) for x in Q[1:]])
+    g["rusanov"]["Q0"] = [[float(x) for x in c] for c in cells]
+    Q = cells
+    dts = []
+    for _ in range(2):
+        Q, dt = L.rusanov_step(e, Q, mp.mpf("0.5"))
+        dts.append(float(dt))
+    g["rusanov"]["Q2"] = [[float(x) for x in c] for c in Q]
+    g["rusanov"]["dt"] = dts
+    with open(OUT, "w") as fh:
+        json.dump(g, fh, indent=1)
+    print("wrote", OUT)
+
+
+if __name__ == "__main__":
+    main()

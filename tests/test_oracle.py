@@ -1,0 +1,175 @@
+"""The oracle pinned: known-answer tests from the physics, the committed 40-digit
+golden vectors of the independent transliteration, LAPACK eigenvalues, and
+internal consistency of its modes. CPU only."""
+import json
+import os
+
+import numpy as np
+import pytest
+
+from helpers import rel_err
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "golden_literal.json")
+
+
+@pytest.fixture(scope="module")
+def golden():
+    with open(GOLDEN) as fh:
+        return json.load(fh)
+
+
+I9 = np.eye(3).reshape(-1, order="F")
+
+
+def test_stress_vanishes_at_rest(orc):
+    # A = I, S = 0: e = 0 and sigma = 0 (EquationsOfState.jl:118-137, 179-190)
+    e = orc.barton2009()
+    assert np.max(np.abs(orc.stress(e, 0.0, I9))) < 1e-14
+    assert abs(orc.energy(e, 0.0, I9)) < 1e-15
+
+
+def test_speeds_at_rest_are_c0_b0_b0(orc):
+    # k0 = c0^2 - 4/3 b0^2 makes the rest-state acoustic tensor diag(c0^2, b0^2, b0^2)
+    e = orc.barton2009()
+    ac = orc.acoustic(e, 0.0, I9).reshape(3, 3, order="F")
+    np.testing.assert_allclose(np.diag(ac), [4.6 ** 2, 2.1 ** 2, 2.1 ** 2], rtol=1e-14)
+    assert np.max(np.abs(ac - np.diag(np.diag(ac)))) < 1e-13
+    mods = np.sort(np.sqrt(orc.eig3_moduli(ac.reshape(-1, order="F"))))[::-1]
+    np.testing.assert_allclose(mods, [4.6, 2.1, 2.1], rtol=1e-7)
+
+
+def test_testcase6_left_speeds(orc):
+    # HyperelasticityMPh.jl:355-360 left distortion with S = 1e-3
+    e = orc.barton2009()
+    F = np.array([[0.98, 0, 0], [0.02, 1, 0.1], [0, 0, 1.0]]).reshape(-1, order="F")
+    mods = np.sort(np.sqrt(orc.eig3_moduli(orc.acoustic(e, 1e-3, F))))[::-1]
+    np.testing.assert_allclose(mods, [5.78791431, 2.41681731, 1.9840291], rtol=2e-8)
+
+
+def test_eigen_moduli_match_lapack(orc):
+    rng = np.random.default_rng(7)
+    e = orc.barton2009()
+    for _ in range(50):
+        F = np.eye(3) + 0.15 * rng.standard_normal((3, 3))
+        if np.linalg.det(F) <= 0:
+            continue
+        ac = orc.acoustic(e, rng.uniform(0, 2e-3), F.reshape(-1, order="F"))
+        ref = np.sort(np.abs(np.linalg.eigvals(ac.reshape(3, 3, order="F"))))[::-1]
+        got = np.sort(orc.eig3_moduli(ac))[::-1]
+        assert abs(got[0] - ref[0]) <= 1e-13 * ref[0]  # the spectral radius (what the solver uses)
+        np.testing.assert_allclose(got, ref, rtol=1e-6)  # all moduli (degenerate pairs lose digits)
+
+
+def test_quadrature_nodes(orc):
+    x, w = orc.quadrature(0)
+    xr, wr = np.polynomial.legendre.leggauss(6)
+    np.testing.assert_allclose(x, (xr + 1) / 2, rtol=0, atol=2e-16)
+    np.testing.assert_allclose(w, wr / 2, rtol=0, atol=2e-16)
+    xl, wl = orc.quadrature(1)
+    assert xl[0] == 0.0 and xl[-1] == 1.0 and abs(np.sum(wl) - 1) < 1e-15
+    # 6-point Lobatto integrates polynomials of degree <= 9 exactly
+    assert abs(np.sum(wl * xl ** 9) - 0.1) < 1e-15
+
+
+def test_golden_tensor_functions(orc, golden):
+    e = orc.barton2009()
+    for t in golden["tensors"]:
+        F = np.array(t["F"])
+        assert rel_err(orc.finger(F), t["finger"]) < 1e-14
+        assert rel_err(orc.invariants(np.array(t["finger"])), t["invariants"]) < 1e-14
+        if abs(t["energy"]) > 1e-12:
+            assert rel_err(orc.energy(e, t["S"], np.array(t["finger"])), t["energy"]) < 1e-12
+        st = np.array(t["stress"])
+        if np.max(np.abs(st)) > 1e-12:
+            assert rel_err(orc.stress(e, t["S"], F), st) < 1e-13
+        assert rel_err(orc.acoustic(e, t["S"], F), t["acoustic"]) < 1e-13
+        got = np.sort(orc.eig3_moduli(np.array(t["acoustic"])))[::-1]
+        assert abs(got[0] - t["moduli"][0]) <= 1e-14 * t["moduli"][0]
+
+
+def test_golden_cells(orc, golden):
+    pb = orc.problem()
+    for c in golden["cells"]:
+        P = np.array(c["P"])[1:]  # alpha == 1 dropped
+        Q = orc.prim2cons(pb, P)
+        assert rel_err(Q, c["Q"][1:]) < 1e-14
+        Qg = np.array(c["Q"][1:])
+        assert rel_err(orc.cons2prim(pb, Qg), c["prim"][1:]) < 1e-12
+        assert rel_err(orc.flux(pb, Qg), c["flux"][1:]) < 1e-13
+        s = orc.speeds(pb, Qg)
+        assert abs(np.max(np.abs(s)) - np.max(np.abs(c["speeds"]))) < 1e-14 * np.max(np.abs(c["speeds"]))
+
+
+def test_golden_twophase_noncons_and_hll(orc, golden):
+    eos = (orc.barton2009(), orc.barton2009(b0=golden["eos2_b0"]))
+    pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, eos=eos)
+    for c in golden["noncons"]:
+        assert rel_err(orc.noncons(pb, np.array(c["Q"])), c["bcol"]) < 1e-13
+    for h in golden["hll"]:
+        dm, dp = orc.hll(pb, np.array(h["Ql"]), np.array(h["Qr"]), np.array(h["spdL"]), np.array(h["spdR"]))
+        assert rel_err(dm, h["dm"]) < 1e-12
+        assert rel_err(dp, h["dp"]) < 1e-12
+
+
+def test_golden_rusanov_steps(orc, golden):
+    g = golden["rusanov"]
+    Q0 = np.array(g["Q0"]).T.copy()
+    pb = orc.problem(nx=Q0.shape[1], cfl=0.5)
+    Q, steps, t, dt = orc.run(pb, Q0, max_steps=2, nthreads=1)
+    assert steps == 2
+    assert abs(t - sum(g["dt"])) < 1e-15
+    err = rel_err(Q, np.array(g["Q2"]).T, axis=1)
+    assert np.all(err < 1e-13), err
+
+
+def test_uniform_state_is_preserved_exactly(orc):
+    pb = orc.problem(nx=16)
+    e = orc.barton2009()
+    F = np.array([[1.01, 0.02, 0], [0, 0.99, 0.01], [0.005, 0, 1.0]]).reshape(-1, order="F")
+    P = np.array([8.93 / np.linalg.det(F.reshape(3, 3, order="F")), 0.3, -0.2, 0.1, 1e-4, *F])
+    Q0 = np.repeat(orc.prim2cons(pb, P)[:, None], 16, axis=1)
+    for bc in (orc.BC_FROZEN, orc.BC_TRANSMISSIVE):
+        pb.bc = bc
+        Q, _, _, _ = orc.run(pb, Q0, max_steps=5, nthreads=2)
+        assert np.array_equal(Q, Q0)
+
+
+def test_constant_alpha_gives_zero_noncons(orc):
+    # alpha constant across a face: B(Q) dQ only involves d alpha, so D+- = 0 (NumFluxes.jl:35-60)
+    from hyperelasticsolver_gb300._cases import mph_case
+    eos = (orc.barton2009(), orc.barton2009())
+    pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_LXF, eos=eos)
+    Pl, Pr = mph_case(5)
+    Ql, Qr = orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr)
+    cons, dm, dp = orc.lxf(pb, Ql, Qr, 5.0)
+    assert np.max(np.abs(dm)) == 0 and np.max(np.abs(dp)) == 0
+
+
+def test_prim_cons_round_trip(orc):
+    pb = orc.problem()
+    rng = np.random.default_rng(3)
+    for _ in range(20):
+        F = np.eye(3) + 0.05 * rng.standard_normal((3, 3))
+        P = np.array([8.93 / np.linalg.det(F), *rng.uniform(-1, 1, 3), rng.uniform(0, 1e-3), *F.reshape(-1, order="F")])
+        P2 = orc.cons2prim(pb, orc.prim2cons(pb, P))
+        assert rel_err(np.delete(P2, 4), np.delete(P, 4)) < 1e-13
+        assert abs(P2[4] - P[4]) < 1e-11 * max(P[4], 1e-3)
+
+
+@pytest.mark.parametrize("model,flux", [(1, 0), (1, 1), (2, 2), (2, 1)])
+def test_literal_and_face_modes_agree_bitwise(orc, model, flux):
+    """The literal mode (each face evaluated twice, as update_cell) and the
+    once-per-face mode give identical results: the functions are pure."""
+    from hyperelasticsolver_gb300._cases import mph_case, riemann_1ph, initial_condition
+    import hyperelasticsolver_gb300 as h
+    nx = 12
+    if model == 1:
+        pb = orc.problem(nx=nx, flux=flux)
+        Pl, Pr = riemann_1ph(h.Barton2009())
+    else:
+        pb = orc.problem(model=2, flux=flux, nx=nx, eos=(orc.barton2009(), orc.barton2009(b0=0.66)))
+        Pl, Pr = mph_case(6)
+    Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
+    a = orc.run(pb, Q0, max_steps=3, literal=True, nthreads=2)[0]
+    b = orc.run(pb, Q0, max_steps=3, literal=False, nthreads=2)[0]
+    assert np.array_equal(a, b)
