@@ -1,0 +1,127 @@
+#
+# HyperelasticCUDA.jl -- Julia binding of libhyperelastic_cuda.so.
+#
+# Keeps the reference's module and function names (Strains, EquationsOfState,
+# HyperelasticityMPh, NumFluxes) and forwards array-of-cells calls to the C ABI in
+# include/hyperelastic.h. Arrays are Matrix{Float64}(n, k): one row per cell, which
+# is exactly the ABI's structure-of-arrays layout. A driver replaces the per-cell
+# loops of main.jl:202-241 by a Solver (hyp_create / hyp_upload / hyp_step).
+#
+module HyperelasticCUDA
+
+const libhyp = get(ENV, "HYP_LIB", joinpath(@__DIR__, "..", "_build", "libhyperelastic_cuda.so"))
+
+struct Barton2009C
+  rho0::Float64; c0::Float64; cv::Float64; t0::Float64
+  b0::Float64; alpha::Float64; beta::Float64; gamma::Float64
+end
+Barton2009C(; _rho0=8.93, _c0=4.6, _cv=3.9e-4, _t0=300, _b0=2.1, _alpha=1, _beta=3, _gamma=2) =
+  Barton2009C(_rho0, _c0, _cv, _t0, _b0, _alpha, _beta, _gamma)
+
+struct ConfigC
+  n_cells::Int64; model::Cint; flux::Cint; bc::Cint; precision::Cint
+  x_length::Float64; cfl::Float64; eos1::Barton2009C; eos2::Barton2009C
+end
+
+const HYP_MODEL_SINGLE, HYP_MODEL_MULTI = Cint(1), Cint(2)
+const HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = Cint(0), Cint(1), Cint(2)
+const HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = Cint(0), Cint(1)
+const HYP_PREC_FP64, HYP_PREC_MIXED = Cint(0), Cint(1)
+
+struct HypError <: Exception
+  code::Cint
+  msg::String
+end
+check(rc, what, ctx=C_NULL) = rc == 0 ? nothing :
+  throw(HypError(rc, what * ": " * unsafe_string(ccall((:hyp_last_error, libhyp), Cstring, (Ptr{Cvoid},), ctx))))
+
+config(eos, model; n=3, flux=HYP_FLUX_RUSANOV, bc=HYP_BC_FROZEN, prec=HYP_PREC_FP64, X=1.0, cfl=0.5) =
+  ConfigC(n, model, flux, bc, prec, X, cfl, eos isa Tuple ? eos[1] : eos, eos isa Tuple ? eos[2] : eos)
+
+module Strains
+  import ..libhyp, ..check
+  "finger(A::Matrix{Float64}(n, 9)) -> G (Strains.jl:26-32)"
+  function finger(A::Matrix{Float64})
+    G = similar(A)
+    check(ccall((:hyp_eval_finger, libhyp), Cint, (Ptr{Float64}, Ptr{Float64}, Int64), A, G, size(A, 1)), "finger")
+    G
+  end
+  function invariants(G::Matrix{Float64})
+    out = Matrix{Float64}(undef, size(G, 1), 3)
+    check(ccall((:hyp_eval_invariants, libhyp), Cint, (Ptr{Float64}, Ptr{Float64}, Int64), G, out, size(G, 1)), "invariants")
+    out
+  end
+end
+
+module EquationsOfState
+  import ..libhyp, ..check, ..Barton2009C
+  for (jl, c, k) in ((:energy, :hyp_eval_energy, 1), (:entropy, :hyp_eval_entropy, 1),
+                     (:stress, :hyp_eval_stress, 9), (:acoustic, :hyp_eval_acoustic, 9))
+    @eval function $jl(eos::Barton2009C, s::Vector{Float64}, M::Matrix{Float64})
+      out = Matrix{Float64}(undef, size(M, 1), $k)
+      e = Ref(eos)
+      check(ccall(($(QuoteNode(c)), libhyp), Cint, (Ref{Barton2009C}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                  e, s, M, out, size(M, 1)), $(string(jl)))
+      $k == 1 ? vec(out) : out
+    end
+  end
+end
+
+module HyperelasticityMPh
+  import ..libhyp, ..check, ..config, ..ConfigC, ..HYP_MODEL_MULTI
+  for (jl, c, k) in ((:cons2prim_mph, :hyp_eval_cons2prim, 30), (:prim2cons_mph, :hyp_eval_prim2cons, 30),
+                     (:flux_mph, :hyp_eval_flux, 30), (:get_eigvals, :hyp_eval_eigvals, 12))
+    @eval function $jl(eos, Q::Matrix{Float64})
+      out = Matrix{Float64}(undef, size(Q, 1), $k)
+      cfg = Ref(config(eos, HYP_MODEL_MULTI))
+      check(ccall(($(QuoteNode(c)), libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64),
+                  cfg, Q, out, size(Q, 1)), $(string(jl)))
+      out
+    end
+  end
+end
+
+module NumFluxes
+  import ..libhyp, ..check, ..config, ..ConfigC, ..HYP_MODEL_SINGLE
+  "lxf(eos, Q_l, Q_r, lambda) for single-phase cells (NumFluxes.jl:25-60): (cons, D-, D+)"
+  function lxf(eos, Ql::Matrix{Float64}, Qr::Matrix{Float64}, lam::Vector{Float64})
+    n = size(Ql, 1)
+    cons, dm, dp = similar(Ql), similar(Ql), similar(Ql)
+    cfg = Ref(config(eos, HYP_MODEL_SINGLE))
+    check(ccall((:hyp_eval_lxf, libhyp), Cint,
+                (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                cfg, Ql, Qr, lam, cons, dm, dp, n), "lxf")
+    cons, dm, dp
+  end
+end
+
+"Device-resident solver for one 1D problem: the time loop of main.jl:202-241."
+mutable struct Solver
+  h::Ptr{Cvoid}
+  n::Int64
+  nvar::Int
+  function Solver(cfg::ConfigC)
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    check(ccall((:hyp_create, libhyp), Cint, (Ref{ConfigC}, Ref{Ptr{Cvoid}}), Ref(cfg), r), "hyp_create")
+    s = new(r[], cfg.n_cells, cfg.model == HYP_MODEL_SINGLE ? 14 : 30)
+    finalizer(x -> ccall((:hyp_destroy, libhyp), Cint, (Ptr{Cvoid},), x.h), s)
+  end
+end
+upload!(s::Solver, Q::Matrix{Float64}, t0=0.0) =
+  check(ccall((:hyp_upload, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64, Cint, Float64), s.h, Q, s.n, s.nvar, t0),
+        "hyp_upload", s.h)
+function download(s::Solver)
+  Q = Matrix{Float64}(undef, s.n, s.nvar)
+  check(ccall((:hyp_download, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64, Cint), s.h, Q, s.n, s.nvar),
+        "hyp_download", s.h)
+  Q
+end
+"step!(s; max_steps, T): advance while t < T (main.jl:202); returns (steps, t)"
+function step!(s::Solver; max_steps::Integer=0, T::Float64=Inf)
+  n, t = Ref{Cint}(0), Ref{Float64}(0.0)
+  check(ccall((:hyp_step, libhyp), Cint, (Ptr{Cvoid}, Cint, Float64, Ref{Cint}, Ref{Float64}), s.h, max_steps, T, n, t),
+        "hyp_step", s.h)
+  (n[], t[])
+end
+
+end # module HyperelasticCUDA
