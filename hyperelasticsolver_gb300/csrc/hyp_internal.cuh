@@ -75,7 +75,19 @@ struct hyp_ctx {
 };
 
 namespace hyp {
-// single-phase FP64 kernels (hyp_step1.cu)
+// single-phase FP64 step kernels (defined in hyp_step1.cu)
+__global__ void __launch_bounds__(kBlock) cell1_f64_kernel(const double* __restrict__ Q, int64_t n, EosC e,
+                                                           double* __restrict__ F, double* __restrict__ lam,
+                                                           unsigned long long* lam_slot, const double* t_now,
+                                                           double t_end, DevState* S);
+__global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __restrict__ Q, double* __restrict__ Qn,
+                                                             int64_t n, const double* __restrict__ F,
+                                                             const double* __restrict__ lam,
+                                                             const unsigned long long* lam_in,
+                                                             unsigned long long* lam_next, const double* t_in,
+                                                             double* t_out, long long* steps, double t_end,
+                                                             double cfl, double dx, int flux, int bc);
+// single-phase FP64 launchers on a context (hyp_step1.cu)
 cudaError_t launch_cell1_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
 cudaError_t launch_update1_f64(hyp_ctx* c, int p, double t_end);
 }  // namespace hyp

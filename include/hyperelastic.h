@@ -107,6 +107,23 @@ int hyp_set_profiling(hyp_ctx* ctx, int on);
 int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel, int* cell_launches,
                     double* ms_update_kernel, int* update_launches);
 
+/* Single-phase FP64 steps on caller-owned device buffers, allocating nothing.
+   No counterpart in the reference: it serves callers that cannot allocate device
+   memory where they step the solver (device memory owned by another allocator,
+   or a latency-critical loop that must not call cudaMalloc). d_Q_in / d_Q_out are
+   device SoA states [14][n_cells] (may be the same buffer); cfg must be
+   single-phase, FP64, Rusanov or LxF, with cfg->n_cells == n_cells. The step's
+   scratch is one fixed static device array sized for at most 65,536 cells
+   (13.6 MiB per GPU that loads the library, held until exit); larger n_cells is
+   rejected with HYP_ERR_INVALID. The first call on a device looks up that array
+   (cudaGetSymbolAddress) and should come before any stream capture. Calls share
+   the array, so calls that overlap on the GPU race. Runs n_steps CFL steps from
+   time t0 on `stream` (a cudaStream_t, NULL = default stream), synchronises it,
+   and reports the new time; on HYP_ERR_NEG_DET / HYP_ERR_NONFINITE the first
+   failing cell is stored in *err_cell. */
+int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_Q_out, int64_t n_cells, int n_steps,
+                         double t0, void* stream, double* t_out, int64_t* err_cell);
+
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);
 int hyp_host_free(void* p);
