@@ -134,10 +134,14 @@ def workload(n_cells, seed=None):
     return eos, seg_q, segment_fill
 
 
-def config_block(args, precision):
+PRECISION_NOTE = {"fp64": "FP64 throughout",
+                  "mixed": "FP32 fluxes and wave speeds, compensated hi/lo FP32 state, float-float cons2prim islands"}
+
+
+def config_block(args):
     return {"workload": f"single-phase Rusanov FV step, {args.n_cells} cells, 64 seeded segments, CFL 0.5",
             "n_cells": args.n_cells, "model": "single-phase (Barton2009 default)", "flux": "rusanov",
-            "bc": "frozen", "cfl": 0.5, "precision": precision,
+            "bc": "frozen", "cfl": 0.5,
             "l2": "inputs larger than L2 (state %.2f GB)" % (args.n_cells * 14 * 8 / 1e9)}
 
 
@@ -192,11 +196,55 @@ def run_reference(args):
     line = {"impl": "reference", "metric": METRIC, "value": v, "unit": METRIC, "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-            "config": config_block(args, "fp64"),
+            "config": config_block(args), "precision": "FP64 (CPU restatement of the reference's step)",
             "cpu_baseline": {"value": v, "unit": METRIC, "cores": nthreads, "kind": "port", "sample": sample},
             "e2e": {"value": v, "unit": METRIC, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
+
+
+KERNEL_NAMES = {("fp64", "cell"): "cell1_f64_kernel", ("fp64", "update"): "update1_f64_kernel",
+                ("mixed", "cell"): "step1_mixed_kernel"}
+
+
+def density(Q, rho0=8.93):
+    """rho_true = sqrt(det(rho A)/rho0) of SoA single-phase states (cons2prim's density)."""
+    m = Q[5:14]
+    det = (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[3] * (m[1] * m[8] - m[7] * m[2])
+           + m[6] * (m[1] * m[5] - m[4] * m[2]))
+    return np.sqrt(det / rho0)
+
+
+def device_run(h, eos, Q0, prec, K, W, dist, clocks=True):
+    """W untimed steps, then K steps timed with CUDA events (per-kernel events on)."""
+    s = h.Solver(eos, Q0.shape[1], precision=prec, cfl=0.5)
+    s.upload(Q0)
+    s.step(max_steps=W)
+    s.set_profiling(True)
+    if dist:
+        dist.barrier()
+    clk = ClockSampler() if clocks else None
+    if clk:
+        clk.start()
+    s.step(max_steps=K)
+    ck = clk.stop() if clk else None
+    tm = s.timing()
+    s.set_profiling(False)
+    Q = s.download()
+    s.close()
+    return tm, ck, Q
+
+
+def roofline(tm, prec, n, peak, peak_kind):
+    kern = "cell" if tm["ms_cell"] >= tm["ms_update"] else "update"
+    ms_k = tm["ms_" + kern] / max(1, tm["n_" + kern])
+    alg = BYTES_PER_CELL_UPDATE["single"] * n
+    achieved = alg / (ms_k / 1e3) / 1e9
+    name = KERNEL_NAMES[(prec, kern)]
+    tr = ncu_traffic(name)
+    return {"bound": "hbm", "kernel": name, "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind, "traffic": (tr * n if tr is not None else None),
+            "algorithmic_bytes_per_launch": alg, "ms_per_launch": ms_k}
 
 
 def run_ours(args):
@@ -209,22 +257,13 @@ def run_ours(args):
     Q0 = segment_fill(seg_q, n)
     state_bytes = Q0.nbytes
     prec = args.precision
-    # ---- device-resident throughput --------------------------------------
-    s = h.Solver(eos, n, precision=prec, cfl=0.5)
-    s.upload(Q0)
-    s.step(max_steps=W)
-    s.set_profiling(True)
-    if dist:
-        dist.barrier()
-    clk = ClockSampler()
-    clk.start()
-    s.step(max_steps=K)
-    clocks = clk.stop()
-    tm = s.timing()
-    s.set_profiling(False)
+    peak, peak_kind = measured_peaks()
+    # ---- device-resident throughput of the headline precision -------------
+    tm, clocks, Qh = device_run(h, eos, Q0, prec, K, W, dist)
     ms_total = dist_max(dist, tm["ms_total"])
     value = WORLD * n * K / (ms_total / 1e3)
     # ---- end to end through the C ABI from pinned host memory -------------
+    s = h.Solver(eos, n, precision=prec, cfl=0.5)
     pin_in, pin_out = PinnedArray(Q0.shape), PinnedArray(Q0.shape)
     pin_in.array[...] = Q0
     s.upload(pin_in.array)
@@ -241,31 +280,35 @@ def run_ours(args):
     s.close()
     pin_in.close()
     pin_out.close()
-    # ---- roofline of the dominant kernel ----------------------------------
-    peak, peak_kind = measured_peaks()
-    kern = "cell" if tm["ms_cell"] >= tm["ms_update"] else "update"
-    ms_k = tm["ms_" + kern] / max(1, tm["n_" + kern])
-    alg = BYTES_PER_CELL_UPDATE["single"] * n
-    achieved = alg / (ms_k / 1e3) / 1e9
-    tr = ncu_traffic({"cell": "cell1_f64_kernel", "update": "update1_f64_kernel"}[kern])
+    # ---- the plain FP64 step on the same workload, and the accuracy -------
+    fp64 = None
+    if prec == "mixed" and not args.no_fp64:
+        tm64, _, Q64 = device_run(h, eos, Q0, "fp64", K, W, dist, clocks=False)
+        ms64 = dist_max(dist, tm64["ms_total"])
+        a, b = density(Qh), density(Q64)
+        fp64 = {"value": WORLD * n * K / (ms64 / 1e3), "ms_per_step": ms64 / K,
+                "mixed_over_fp64": (WORLD * n * K / (ms_total / 1e3)) / (WORLD * n * K / (ms64 / 1e3)),
+                "roofline": roofline(tm64, "fp64", n, peak, peak_kind),
+                "density_error_vs_fp64": {"l1": float(np.sum(np.abs(a - b)) / np.sum(np.abs(b))),
+                                          "linf": float(np.max(np.abs(a - b)) / np.max(np.abs(b))),
+                                          "after_steps": W + K}}
     if RANK != 0:
         return 0
+    rf = roofline(tm, prec, n, peak, peak_kind)
+    rf["step_hbm_frac"] = (BYTES_PER_CELL_UPDATE["single"] * n / (ms_total / K / 1e3) / 1e9) / peak
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": WORLD, "steps": K, "warmup": W,
         "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-        "dtype": "f64" if prec == "fp64" else "f32+f32x2", "data": "synthetic",
-        "config": config_block(args, prec),
+        "dtype": "f64" if prec == "fp64" else "f32", "data": "synthetic",
+        "config": config_block(args), "precision": PRECISION_NOTE[prec],
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": state_bytes / K,
                 "d2h_bytes_per_step": state_bytes / K + 64},
         "gpu_launches": tm["n_cell"] + tm["n_update"],
-        "roofline": {"bound": "hbm", "kernel": kern, "achieved": achieved, "peak": peak, "unit": "GB/s",
-                     "frac": achieved / peak, "peak_source": peak_kind,
-                     "traffic": (tr * n if tr is not None else None),
-                     "algorithmic_bytes_per_launch": alg,
-                     "ms_per_launch": ms_k,
-                     "step_hbm_frac": (BYTES_PER_CELL_UPDATE["single"] * n / (ms_total / K / 1e3) / 1e9) / peak},
+        "roofline": rf,
     }
+    if fp64:
+        line["fp64"] = fp64
     if not args.no_cpu:
         v, sample = cpu_sample(Q0, args.cpu_seconds, os.cpu_count())
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": os.cpu_count(), "kind": "port", "sample": sample}
@@ -280,7 +323,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--n-cells", type=int, default=1 << 24)
-    ap.add_argument("--precision", choices=["fp64", "mixed"], default="fp64")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
     args = ap.parse_args()

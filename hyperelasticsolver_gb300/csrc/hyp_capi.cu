@@ -32,13 +32,19 @@ static bool valid_eos(const hyp_barton2009& b) {
          std::isfinite(b.beta) && std::isfinite(b.gamma);
 }
 
+static bool mixed(const hyp_ctx* c) { return c->cfg.precision == HYP_PREC_MIXED; }
+
 static int free_ctx(hyp_ctx* c) {
   if (!c) return HYP_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  for (auto& g : c->graph)
+    if (g) cudaGraphExecDestroy(g);
   for (int p = 0; p < 2; ++p) {
-    if (c->graph[p]) cudaGraphExecDestroy(c->graph[p]);
     cudaFree(c->Q[p]);
+    cudaFree(c->Qh[p]);  // the (hi, lo) block
+    cudaFree(c->lamf[p]);
+    cudaFree(c->isl[p]);
   }
   cudaFree(c->F);
   cudaFree(c->lam);
@@ -61,8 +67,7 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if (cfg->bc != HYP_BC_FROZEN && cfg->bc != HYP_BC_TRANSMISSIVE) return HYP_ERR_INVALID;
   if (cfg->precision != HYP_PREC_FP64 && cfg->precision != HYP_PREC_MIXED) return HYP_ERR_INVALID;
   if (!valid_eos(cfg->eos[0]) || (cfg->model == HYP_MODEL_MULTI && !valid_eos(cfg->eos[1]))) return HYP_ERR_INVALID;
-  if (cfg->model != HYP_MODEL_SINGLE || cfg->flux == HYP_FLUX_HLL || cfg->precision != HYP_PREC_FP64)
-    return HYP_ERR_UNSUPPORTED;
+  if (cfg->model != HYP_MODEL_SINGLE || cfg->flux == HYP_FLUX_HLL) return HYP_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
   hyp_ctx* c = new (std::nothrow) hyp_ctx();
@@ -71,6 +76,7 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   c->cfg = *cfg;
   c->eos[0] = to_eos(cfg->eos[0]);
   c->eos[1] = to_eos(cfg->model == HYP_MODEL_MULTI ? cfg->eos[1] : cfg->eos[0]);
+  c->eos_mixed = make_eos_mixed(c->eos[0]);
   c->n = cfg->n_cells;
   c->nvar = cfg->model == HYP_MODEL_SINGLE ? 14 : 30;
   int rc = HYP_OK;
@@ -83,12 +89,25 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if (rc == HYP_OK && (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
     fail(e, "cudaStreamCreate");
   const size_t nq = (size_t)c->nvar * c->n * sizeof(double);
-  for (int p = 0; p < 2 && rc == HYP_OK; ++p)
-    if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");
-  if (rc == HYP_OK && (e = cudaMalloc(&c->F, (size_t)kNFlux1 * c->n * sizeof(double))) != cudaSuccess)
-    fail(e, "cudaMalloc(F)");
-  if (rc == HYP_OK && (e = cudaMalloc(&c->lam, (size_t)c->n * sizeof(double))) != cudaSuccess)
-    fail(e, "cudaMalloc(lam)");
+  if (!mixed(c)) {
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p)
+      if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->F, (size_t)kNFlux1 * c->n * sizeof(double))) != cudaSuccess)
+      fail(e, "cudaMalloc(F)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->lam, (size_t)c->n * sizeof(double))) != cudaSuccess)
+      fail(e, "cudaMalloc(lam)");
+  } else {
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
+      if ((e = cudaMalloc(&c->Qh[p], nq)) != cudaSuccess) {  // 2 x 14 x n floats = 14 x n doubles
+        fail(e, "cudaMalloc(Q hi/lo)");
+        break;
+      }
+      c->Ql[p] = c->Qh[p] + (size_t)c->nvar * c->n;
+      if ((e = cudaMalloc(&c->lamf[p], (size_t)c->n * sizeof(float))) != cudaSuccess) fail(e, "cudaMalloc(lambda)");
+      if (rc == HYP_OK && (e = cudaMalloc(&c->isl[p], (size_t)3 * c->n * sizeof(float))) != cudaSuccess)
+        fail(e, "cudaMalloc(islands)");
+    }
+  }
   if (rc == HYP_OK && (e = cudaMalloc(&c->st, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMalloc(state)");
   if (rc == HYP_OK && (e = cudaMallocHost(&c->st_host, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMallocHost");
   for (auto& ev : c->ev)
@@ -131,29 +150,44 @@ extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_va
   if (!c || !Q) return HYP_ERR_INVALID;
   if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_upload: size mismatch");
   CK(cudaSetDevice(c->device));
-  CK(cudaMemcpyAsync(c->Q[0], Q, (size_t)n_vars * n_cells * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+  const size_t bytes = (size_t)n_vars * n_cells * sizeof(double);
   std::memset(c->st_host, 0, sizeof(DevState));
   c->st_host->t[0] = c->st_host->t[1] = t0;
   CK(cudaMemcpyAsync(c->st, c->st_host, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
-  CK(cudaStreamSynchronize(c->stream));
+  if (!mixed(c)) {
+    CK(cudaMemcpyAsync(c->Q[0], Q, bytes, cudaMemcpyHostToDevice, c->stream));
+  } else {
+    double* stage = (double*)c->Qh[1];
+    CK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, c->stream));
+    CK(launch_split(c, stage, c->Qh[0], c->Ql[0]));
+    CK(launch_lam1_mixed(c, 0, &c->st->lam_slots[0]));
+  }
+  int rc = sync_state(c);
+  if (rc != HYP_OK) return rc;
   c->cur = 0;
   c->t_host = t0;
   c->steps_host = 0;
   c->err_cell = -1;
-  return HYP_OK;
+  return check_cell_error(c);
 }
 
 extern "C" int hyp_download(hyp_ctx* c, double* Q, int64_t n_cells, int n_vars) {
   if (!c || !Q) return HYP_ERR_INVALID;
   if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_download: size mismatch");
   CK(cudaSetDevice(c->device));
-  CK(cudaMemcpyAsync(Q, c->Q[c->cur], (size_t)n_vars * n_cells * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+  const size_t bytes = (size_t)n_vars * n_cells * sizeof(double);
+  if (!mixed(c)) {
+    CK(cudaMemcpyAsync(Q, c->Q[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    double* stage = (double*)c->Qh[1 - c->cur];  // the other parity's block is free between steps
+    CK(launch_join(c, c->Qh[c->cur], c->Ql[c->cur], stage));
+    CK(cudaMemcpyAsync(Q, stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+  }
   CK(cudaStreamSynchronize(c->stream));
   return HYP_OK;
 }
 
-// Enqueue one step of parity p (no host synchronisation). With profiling on,
-// each kernel is bracketed by events taken from the context's pool; the
+// Profiling: each kernel is bracketed by events from the context's pool; the
 // durations are summed when hyp_step finishes.
 static int prof_event(hyp_ctx* c, cudaEvent_t* out) {
   if (c->prof_used == c->prof_ev.size()) {
@@ -165,16 +199,24 @@ static int prof_event(hyp_ctx* c, cudaEvent_t* out) {
   return HYP_OK;
 }
 
-static int enqueue_step(hyp_ctx* c, int p, double t_end, bool prof) {
+// Enqueue step number k (k = steps taken since the upload + steps already
+// enqueued); no host synchronisation.
+static int enqueue_step(hyp_ctx* c, long long k, double t_end, bool prof) {
   cudaEvent_t e0 = nullptr, e1 = nullptr, e2 = nullptr;
   int rc;
   if (prof) {
     if ((rc = prof_event(c, &e0)) || (rc = prof_event(c, &e1)) || (rc = prof_event(c, &e2))) return rc;
     CK(cudaEventRecord(e0, c->stream));
   }
-  CK(launch_cell1_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
-  if (prof) CK(cudaEventRecord(e1, c->stream));
-  CK(launch_update1_f64(c, p, t_end));
+  if (!mixed(c)) {
+    const int p = (int)(k & 1);
+    CK(launch_cell1_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
+    if (prof) CK(cudaEventRecord(e1, c->stream));
+    CK(launch_update1_f64(c, p, t_end));
+  } else {
+    CK(launch_step1_mixed(c, k, t_end));
+    if (prof) CK(cudaEventRecord(e1, c->stream));
+  }
   if (prof) CK(cudaEventRecord(e2, c->stream));
   return HYP_OK;
 }
@@ -185,37 +227,42 @@ static int collect_profile(hyp_ctx* c) {
     CK(cudaEventElapsedTime(&a, c->prof_ev[k], c->prof_ev[k + 1]));
     CK(cudaEventElapsedTime(&b, c->prof_ev[k + 1], c->prof_ev[k + 2]));
     c->timing.ms_cell += a;
-    c->timing.ms_update += b;
     c->timing.n_cell += 1;
-    c->timing.n_update += 1;
+    if (!mixed(c)) {
+      c->timing.ms_update += b;
+      c->timing.n_update += 1;
+    }
   }
   c->prof_used = 0;
   return HYP_OK;
 }
 
-static constexpr int kGraphSteps = 16;  // steps per captured graph (even)
+// steps per captured graph: a multiple of the launch pattern's period
+static int graph_period(const hyp_ctx* c) { return mixed(c) ? 6 : 2; }
+static int graph_steps(const hyp_ctx* c) { return mixed(c) ? 12 : 16; }
 
-static int ensure_graph(hyp_ctx* c, int p, double t_end) {
-  if (c->graph[p] && c->graph_t_end == t_end && c->graph_steps == kGraphSteps) return HYP_OK;
-  if (c->graph_t_end != t_end || c->graph_steps != kGraphSteps) {
-    for (int q = 0; q < 2; ++q)
-      if (c->graph[q]) {
-        cudaGraphExecDestroy(c->graph[q]);
-        c->graph[q] = nullptr;
+static int ensure_graph(hyp_ctx* c, long long k0, double t_end) {
+  const int key = (int)(k0 % graph_period(c));
+  if (c->graph_t_end != t_end || c->graph_steps != graph_steps(c)) {
+    for (auto& g : c->graph)
+      if (g) {
+        cudaGraphExecDestroy(g);
+        g = nullptr;
       }
+    c->graph_t_end = t_end;
+    c->graph_steps = graph_steps(c);
   }
+  if (c->graph[key]) return HYP_OK;
   cudaGraph_t g;
   CK(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
   int rc = HYP_OK;
-  for (int s = 0; s < kGraphSteps && rc == HYP_OK; ++s) rc = enqueue_step(c, (p + s) & 1, t_end, false);
+  for (int s = 0; s < c->graph_steps && rc == HYP_OK; ++s) rc = enqueue_step(c, k0 + s, t_end, false);
   cudaError_t e = cudaStreamEndCapture(c->stream, &g);
   if (rc != HYP_OK) return rc;
   if (e != cudaSuccess) return set_err(c, HYP_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
-  e = cudaGraphInstantiate(&c->graph[p], g, 0);
+  e = cudaGraphInstantiate(&c->graph[key], g, 0);
   cudaGraphDestroy(g);
   if (e != cudaSuccess) return set_err(c, HYP_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
-  c->graph_t_end = t_end;
-  c->graph_steps = kGraphSteps;
   return HYP_OK;
 }
 
@@ -229,41 +276,41 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
   c->prof_used = 0;
   const long long steps0 = c->steps_host;
   CK(cudaEventRecord(c->ev[0], c->stream));
-  int launched = 0;
+  long long launched = 0;
   const bool prof = c->profiling != 0;
   // With a finite t_end, steps past t_end are no-ops on the device; launch in
   // chunks and stop once the device reports t >= t_end.
-  const int chunk = std::isinf(t_end) ? (unlimited ? 0 : max_steps) : 256;
+  const long long chunk = std::isinf(t_end) ? (unlimited ? 0 : max_steps) : 256;
+  const int gs = graph_steps(c);
   int rc = HYP_OK;
   while (rc == HYP_OK) {
-    int todo = unlimited ? chunk : (max_steps - launched);
+    long long todo = unlimited ? chunk : (max_steps - launched);
     if (!std::isinf(t_end) && todo > chunk) todo = chunk;
     if (todo <= 0) break;
-    // every launched step flips the parity (an inactive step copies t across and
-    // leaves Q alone; only active steps move the current buffer)
-    int p = (int)((c->cur + launched) & 1);
-    int s = 0;
+    // Every launched step advances the pattern index. An inactive step (t >= t_end)
+    // copies t across and leaves the state and its max-lambda slot alone; active
+    // steps always precede inactive ones, so the state index is steps0 + active.
+    long long k = steps0 + launched;
+    long long s = 0;
     if (!prof) {
-      while (rc == HYP_OK && todo - s >= kGraphSteps) {
-        rc = ensure_graph(c, p, t_end);
+      while (rc == HYP_OK && todo - s >= gs) {
+        rc = ensure_graph(c, k, t_end);
         if (rc == HYP_OK) {
-          cudaError_t e = cudaGraphLaunch(c->graph[p], c->stream);
+          cudaError_t e = cudaGraphLaunch(c->graph[k % graph_period(c)], c->stream);
           if (e != cudaSuccess) rc = set_err(c, HYP_ERR_CUDA, std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
         }
-        s += kGraphSteps;  // even: parity unchanged
+        s += gs;
+        k += gs;
       }
     }
-    for (; rc == HYP_OK && s < todo; ++s) {
-      rc = enqueue_step(c, p, t_end, prof);
-      p ^= 1;
-    }
+    for (; rc == HYP_OK && s < todo; ++s, ++k) rc = enqueue_step(c, k, t_end, prof);
     launched += todo;
     if (rc != HYP_OK) break;
     if (!std::isinf(t_end)) {
       rc = sync_state(c);
       if (rc != HYP_OK) break;
       if (c->st_host->err_code) break;
-      double tl = c->st_host->t[(c->cur + launched) & 1];
+      double tl = c->st_host->t[(steps0 + launched) & 1];
       if (!(tl < t_end)) break;
     }
     if (std::isinf(t_end)) break;
@@ -287,6 +334,15 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
 extern "C" int hyp_max_wavespeed(hyp_ctx* c, double* out) {
   if (!c || !out) return HYP_ERR_INVALID;
   CK(cudaSetDevice(c->device));
+  if (mixed(c)) {  // kept by the last step (or the upload) for the current state
+    int rc = sync_state(c);
+    if (rc != HYP_OK) return rc;
+    unsigned bits = (unsigned)c->st_host->lam_slots[c->steps_host % 3];
+    float v;
+    std::memcpy(&v, &bits, sizeof v);
+    *out = v;
+    return check_cell_error(c);
+  }
   CK(cudaMemsetAsync(&c->st->lam_query, 0, sizeof(unsigned long long), c->stream));
   CK(launch_cell1_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
   int rc = sync_state(c);

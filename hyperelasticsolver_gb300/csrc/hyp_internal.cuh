@@ -7,6 +7,7 @@
 #include <vector>
 #include "../../include/hyperelastic.h"
 #include "hyp_physics.cuh"
+#include "hyp_physics_mixed.cuh"
 
 namespace hyp {
 
@@ -19,6 +20,7 @@ struct DevState {
   double t[2];                        // time before the step of parity p is t[p]
   unsigned long long lam_bits[2];     // max wave speed of the state of parity p (bits of a double >= 0)
   unsigned long long lam_query;       // hyp_max_wavespeed slot
+  unsigned long long lam_slots[3];    // mixed precision: FP32 max lambda (bits) of states k, k+1 (slot k%3)
   long long steps;                    // steps taken
   int err_code;                       // first HYP_CELL_* status raised (0 = none)
   int pad_;
@@ -56,6 +58,13 @@ struct hyp_ctx {
   double* Q[2] = {nullptr, nullptr};
   double* F = nullptr;     // per-cell fluxes (scratch)
   double* lam = nullptr;   // per-cell max wave speed (scratch)
+  // mixed precision: per parity one block of 2 x 14 x n floats (hi then lo), which
+  // also serves as the FP64 staging buffer of uploads and downloads; per-cell FP32 lambda
+  float* Qh[2] = {nullptr, nullptr};
+  float* Ql[2] = {nullptr, nullptr};
+  float* lamf[2] = {nullptr, nullptr};
+  float* isl[2] = {nullptr, nullptr};  // cached float-float island outputs [3][n] (1/rho, e_int, rho/rho0 - 1)
+  hyp::EosMixed eos_mixed;
   hyp::DevState* st = nullptr;
   hyp::DevState* st_host = nullptr;  // pinned mirror
   int cur = 0;             // parity of the buffer that holds the current state
@@ -67,7 +76,9 @@ struct hyp_ctx {
   size_t prof_used = 0;
   hyp::StepTiming timing;
   // CUDA graph of an even number of steps, per starting parity
-  cudaGraphExec_t graph[2] = {nullptr, nullptr};
+  // graphs keyed by the starting step index modulo the pattern period (2 for
+  // FP64: buffer parity; 6 for mixed: parity x three max-lambda slots)
+  cudaGraphExec_t graph[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int graph_steps = 0;
   double graph_t_end = 0.0;
   std::string err;
@@ -90,4 +101,9 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
 // single-phase FP64 launchers on a context (hyp_step1.cu)
 cudaError_t launch_cell1_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
 cudaError_t launch_update1_f64(hyp_ctx* c, int p, double t_end);
+// single-phase mixed-precision launchers (hyp_step1_mixed.cu)
+cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo);
+cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q);
+cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot);
+cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end);
 }  // namespace hyp

@@ -36,17 +36,22 @@
 
 namespace hyp {
 
-// Barton2009 parameters with the derived constants the closed forms use.
-struct EosC {
-  double rho0, inv_rho0, cv, t0, cvt0, inv_cvt0;
-  double alpha, beta, gamma;
-  double b0sq, k0;
-  double kU;       // 0.5 k0 / alpha^2          (cold energy prefactor)
-  double kE3a;     // k0 / (2 alpha)            (dUcold/dp prefactor)
-  double kE3b;     // b0sq * beta / 4           (dW/dp prefactor)
-  double kE3g;     // cv t0 gamma / 2           (d thermal / dp prefactor)
+// Barton2009 parameters with the derived constants the closed forms use. The
+// templates below take the arithmetic type R: double for the FP64 step, float
+// for the mixed-precision step (every constant goes through R(...) so that no
+// FP32 expression is promoted to the slow FP64 pipe).
+template <class R> struct EosT {
+  R rho0, inv_rho0, cv, t0, cvt0, inv_cvt0;
+  R alpha, beta, gamma;
+  R b0sq, k0;
+  R kU;            // 0.5 k0 / alpha^2          (cold energy prefactor)
+  R kE3a;          // k0 / (2 alpha)            (dUcold/dp prefactor)
+  R kE3b;          // b0sq * beta / 4           (dW/dp prefactor)
+  R kE3g;          // cv t0 gamma / 2           (d thermal / dp prefactor)
+  R b0sq_3, b0sq_6;  // b0sq / 3, b0sq / 6
   int default_exp; // alpha == 1, beta == 3, gamma == 2 (integer-power fast path)
 };
+using EosC = EosT<double>;
 
 HYP_HD EosC make_eos(double rho0, double c0, double cv, double t0, double b0, double alpha, double beta,
                      double gamma) {
@@ -66,49 +71,66 @@ HYP_HD EosC make_eos(double rho0, double c0, double cv, double t0, double b0, do
   e.kE3a = e.k0 / (2.0 * alpha);
   e.kE3b = e.b0sq * beta / 4.0;
   e.kE3g = e.cvt0 * gamma / 2.0;
+  e.b0sq_3 = e.b0sq / 3.0;
+  e.b0sq_6 = e.b0sq / 6.0;
   e.default_exp = (alpha == 1.0 && beta == 3.0 && gamma == 2.0) ? 1 : 0;
   return e;
 }
+template <class R> HYP_HD EosT<R> eos_as(const EosC& e) {
+  EosT<R> r;
+  r.rho0 = (R)e.rho0; r.inv_rho0 = (R)e.inv_rho0; r.cv = (R)e.cv; r.t0 = (R)e.t0;
+  r.cvt0 = (R)e.cvt0; r.inv_cvt0 = (R)e.inv_cvt0;
+  r.alpha = (R)e.alpha; r.beta = (R)e.beta; r.gamma = (R)e.gamma;
+  r.b0sq = (R)e.b0sq; r.k0 = (R)e.k0;
+  r.kU = (R)e.kU; r.kE3a = (R)e.kE3a; r.kE3b = (R)e.kE3b; r.kE3g = (R)e.kE3g;
+  r.b0sq_3 = (R)e.b0sq_3; r.b0sq_6 = (R)e.b0sq_6;
+  r.default_exp = e.default_exp;
+  return r;
+}
 
 // Symmetric 3x3 stored as (00, 11, 22, 01, 02, 12).
-struct Sym {
-  double a00, a11, a22, a01, a02, a12;
+template <class R> struct SymT {
+  R a00, a11, a22, a01, a02, a12;
 };
-HYP_HD double sym_at(const Sym& s, int i, int j) {
+using Sym = SymT<double>;
+template <class R> HYP_HD R sym_at(const SymT<R>& s, int i, int j) {
   if (i == j) return i == 0 ? s.a00 : (i == 1 ? s.a11 : s.a22);
   int k = i + j;  // 1: (0,1), 2: (0,2), 3: (1,2)
   return k == 1 ? s.a01 : (k == 2 ? s.a02 : s.a12);
 }
 
 // Powers of p = i3 = det G needed by the energy and its first two p-derivatives.
-struct Pows {
-  double Pa, Pa1, Pa2;  // p^(a/2), p^(a/2-1), p^(a/2-2)   a = alpha
-  double Pb, Pb1, Pb2;  // beta
-  double Pg, Pg1, Pg2;  // gamma
-  double inv_Pg;
+template <class R> struct PowsT {
+  R Pa, Pa1, Pa2;  // p^(a/2), p^(a/2-1), p^(a/2-2)   a = alpha
+  R Pb, Pb1, Pb2;  // beta
+  R Pg, Pg1, Pg2;  // gamma
+  R inv_Pg;
+  R Pam1;          // p^(a/2) - 1 (the cold-energy strain; set accurately by the mixed path)
 };
+using Pows = PowsT<double>;
 
 // Kinematic quantities of the distortion A (column-major 9-vector).
-struct Kin {
-  Sym G;     // Finger tensor G = (A A^T)^-1   (Strains.jl:26-32)
-  Sym H;     // G^2
-  double i1, i2, p;  // invariants (Strains.jl:46-52); p = i3 = det G
-  double s, inv_s;   // sqrt(p) = 1/det A and det A
-  double psi;        // i1^2/3 - i2
+template <class R> struct KinT {
+  SymT<R> G;         // Finger tensor G = (A A^T)^-1   (Strains.jl:26-32)
+  SymT<R> H;         // G^2
+  R i1, i2, p;       // invariants (Strains.jl:46-52); p = i3 = det G
+  R s, inv_s;        // sqrt(p) = 1/det A and det A
+  R psi;             // i1^2/3 - i2
 };
+using Kin = KinT<double>;
 
-// A -> G, G^2, invariants. `detA` is det(A) (> 0 for admissible states).
-HYP_HD Kin kinematics(const double* A, double detA) {
-  Kin k;
+// A -> G, G^2, invariants, given s = 1/det A (> 0 for admissible states).
+template <class R> HYP_HD KinT<R> kinematics_s(const R* A, R s, R inv_s) {
+  KinT<R> k;
   // M = A A^T (symmetric)
-  double m00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
-  double m11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
-  double m22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
-  double m01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
-  double m02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
-  double m12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
-  k.inv_s = detA;
-  k.s = 1.0 / detA;
+  R m00 = A[0] * A[0] + A[3] * A[3] + A[6] * A[6];
+  R m11 = A[1] * A[1] + A[4] * A[4] + A[7] * A[7];
+  R m22 = A[2] * A[2] + A[5] * A[5] + A[8] * A[8];
+  R m01 = A[0] * A[1] + A[3] * A[4] + A[6] * A[7];
+  R m02 = A[0] * A[2] + A[3] * A[5] + A[6] * A[8];
+  R m12 = A[1] * A[2] + A[4] * A[5] + A[7] * A[8];
+  k.inv_s = inv_s;
+  k.s = s;
   k.p = k.s * k.s;  // det G = 1/det(M) = 1/det(A)^2
   // G = adj(M) / det(M) = adj(M) * p
   k.G.a00 = (m11 * m22 - m12 * m12) * k.p;
@@ -117,7 +139,7 @@ HYP_HD Kin kinematics(const double* A, double detA) {
   k.G.a01 = (m02 * m12 - m01 * m22) * k.p;
   k.G.a02 = (m01 * m12 - m02 * m11) * k.p;
   k.G.a12 = (m01 * m02 - m00 * m12) * k.p;
-  const Sym& g = k.G;
+  const SymT<R>& g = k.G;
   k.H.a00 = g.a00 * g.a00 + g.a01 * g.a01 + g.a02 * g.a02;
   k.H.a11 = g.a01 * g.a01 + g.a11 * g.a11 + g.a12 * g.a12;
   k.H.a22 = g.a02 * g.a02 + g.a12 * g.a12 + g.a22 * g.a22;
@@ -125,56 +147,68 @@ HYP_HD Kin kinematics(const double* A, double detA) {
   k.H.a02 = g.a00 * g.a02 + g.a01 * g.a12 + g.a02 * g.a22;
   k.H.a12 = g.a01 * g.a02 + g.a11 * g.a12 + g.a12 * g.a22;
   k.i1 = g.a00 + g.a11 + g.a22;
-  double trH = k.H.a00 + k.H.a11 + k.H.a22;
-  k.i2 = 0.5 * (k.i1 * k.i1 - trH);
-  k.psi = k.i1 * k.i1 / 3.0 - k.i2;
+  R trH = k.H.a00 + k.H.a11 + k.H.a22;
+  k.i2 = R(0.5) * (k.i1 * k.i1 - trH);
+  if (sizeof(R) == sizeof(double)) {
+    k.psi = k.i1 * k.i1 / R(3) - k.i2;
+  } else {
+    // i1^2/3 - i2 = |dev G|^2 / 2 without the cancellation near G = I (FP32)
+    R d01 = g.a00 - g.a11, d12 = g.a11 - g.a22, d20 = g.a22 - g.a00;
+    k.psi = (d01 * d01 + d12 * d12 + d20 * d20) * R(1.0 / 6.0) + (g.a01 * g.a01 + g.a02 * g.a02 + g.a12 * g.a12);
+  }
   return k;
 }
+template <class R> HYP_HD KinT<R> kinematics(const R* A, R detA) { return kinematics_s(A, R(1) / detA, detA); }
 
-HYP_HD double det3(const double* m) {  // column-major, cofactor expansion (SimpleLA.jl:84-89)
+template <class R> HYP_HD R det3(const R* m) {  // column-major, cofactor expansion (SimpleLA.jl:84-89)
   return m[0] * (m[4] * m[8] - m[5] * m[7]) - m[3] * (m[1] * m[8] - m[7] * m[2]) +
          m[6] * (m[1] * m[5] - m[4] * m[2]);
 }
 
-HYP_HD Pows powers(const EosC& e, const Kin& k) {
-  Pows w;
+template <class R> HYP_HD PowsT<R> powers(const EosT<R>& e, const KinT<R>& k) {
+  PowsT<R> w;
   if (e.default_exp) {  // alpha = 1, beta = 3, gamma = 2: p^(n/2) = s^n
-    double s = k.s, is = k.inv_s, ip = is * is;
+    R s = k.s, is = k.inv_s, ip = is * is;
     w.Pa = s;         w.Pa1 = is;  w.Pa2 = is * ip;
     w.Pb = s * k.p;   w.Pb1 = s;   w.Pb2 = is;
-    w.Pg = k.p;       w.Pg1 = 1.0; w.Pg2 = ip;
+    w.Pg = k.p;       w.Pg1 = R(1); w.Pg2 = ip;
     w.inv_Pg = ip;
   } else {
-    double lp = log(k.p), ip = 1.0 / k.p;
-    w.Pa = exp(0.5 * e.alpha * lp); w.Pa1 = w.Pa * ip; w.Pa2 = w.Pa1 * ip;
-    w.Pb = exp(0.5 * e.beta * lp);  w.Pb1 = w.Pb * ip; w.Pb2 = w.Pb1 * ip;
-    w.Pg = exp(0.5 * e.gamma * lp); w.Pg1 = w.Pg * ip; w.Pg2 = w.Pg1 * ip;
-    w.inv_Pg = 1.0 / w.Pg;
+    R lp = log(k.p), ip = R(1) / k.p;
+    w.Pa = exp(R(0.5) * e.alpha * lp); w.Pa1 = w.Pa * ip; w.Pa2 = w.Pa1 * ip;
+    w.Pb = exp(R(0.5) * e.beta * lp);  w.Pb1 = w.Pb * ip; w.Pb2 = w.Pb1 * ip;
+    w.Pg = exp(R(0.5) * e.gamma * lp); w.Pg1 = w.Pg * ip; w.Pg2 = w.Pg1 * ip;
+    w.inv_Pg = R(1) / w.Pg;
   }
+  w.Pam1 = w.Pa - R(1);
   return w;
 }
 
 // Cold (Ucold) and shear (W) parts of the Barton2009 energy (EquationsOfState.jl:129-134).
-HYP_HD double e_cold(const EosC& e, const Pows& w) { return e.kU * (w.Pa - 1.0) * (w.Pa - 1.0); }
-HYP_HD double e_shear(const EosC& e, const Kin& k, const Pows& w) { return 0.5 * e.b0sq * w.Pb * k.psi; }
+template <class R> HYP_HD R e_cold(const EosT<R>& e, const PowsT<R>& w) { return e.kU * w.Pam1 * w.Pam1; }
+template <class R> HYP_HD R e_shear(const EosT<R>& e, const KinT<R>& k, const PowsT<R>& w) {
+  return R(0.5) * e.b0sq * w.Pb * k.psi;
+}
 
 // x - 1 with x the entropy argument of EquationsOfState.jl:150-154 (clamped at
 // 1e-6); exp(S/cv) - 1 of the energy equals it because S = cv log x.
-HYP_HD double entropy_xm1(const EosC& e, double e_int, const Kin& k, const Pows& w) {
-  double xm1 = (e_int - e_shear(e, k, w) - e_cold(e, w)) * e.inv_cvt0 * w.inv_Pg;
-  if (xm1 + 1.0 < 1e-6) xm1 = 1e-6 - 1.0;
+template <class R> HYP_HD R entropy_xm1(const EosT<R>& e, R e_int, const KinT<R>& k, const PowsT<R>& w) {
+  R xm1 = (e_int - e_shear(e, k, w) - e_cold(e, w)) * e.inv_cvt0 * w.inv_Pg;
+  if (xm1 + R(1) < R(1e-6)) xm1 = R(1e-6) - R(1);
   return xm1;
 }
 
 // Stress coefficients: G dE/dG = cG G + cGG G^2 + cI I (with S fixed).
-struct StressC {
-  double cG, cGG, cI, E3;
+template <class R> struct StressCT {
+  R cG, cGG, cI, E3;
 };
-HYP_HD StressC stress_coeffs(const EosC& e, const Kin& k, const Pows& w, double xm1) {
-  StressC c;
-  double E1 = (e.b0sq / 3.0) * w.Pb * k.i1;
-  double E2 = -0.5 * e.b0sq * w.Pb;
-  c.E3 = e.kE3a * (w.Pa - 1.0) * w.Pa1 + e.kE3g * w.Pg1 * xm1 + e.kE3b * w.Pb1 * k.psi;
+using StressC = StressCT<double>;
+template <class R>
+HYP_HD StressCT<R> stress_coeffs(const EosT<R>& e, const KinT<R>& k, const PowsT<R>& w, R xm1) {
+  StressCT<R> c;
+  R E1 = e.b0sq_3 * w.Pb * k.i1;
+  R E2 = R(-0.5) * e.b0sq * w.Pb;
+  c.E3 = e.kE3a * w.Pam1 * w.Pa1 + e.kE3g * w.Pg1 * xm1 + e.kE3b * w.Pb1 * k.psi;
   c.cG = E1 + E2 * k.i1;
   c.cGG = -E2;
   c.cI = c.E3 * k.p;
@@ -182,69 +216,70 @@ HYP_HD StressC stress_coeffs(const EosC& e, const Kin& k, const Pows& w, double 
 }
 
 // Row 1 of sigma = -2 rho_s (cG G + cGG G^2 + cI I).
-HYP_HD void stress_row0(double rho_s, const Kin& k, const StressC& c, double* s0) {
-  double m = -2.0 * rho_s;
+template <class R> HYP_HD void stress_row0(R rho_s, const KinT<R>& k, const StressCT<R>& c, R* s0) {
+  R m = R(-2) * rho_s;
   s0[0] = m * (c.cG * k.G.a00 + c.cGG * k.H.a00 + c.cI);
   s0[1] = m * (c.cG * k.G.a01 + c.cGG * k.H.a01);
   s0[2] = m * (c.cG * k.G.a02 + c.cGG * k.H.a02);
 }
-HYP_HD void stress_full(double rho_s, const Kin& k, const StressC& c, double* sig) {
-  double m = -2.0 * rho_s;
+template <class R> HYP_HD void stress_full(R rho_s, const KinT<R>& k, const StressCT<R>& c, R* sig) {
+  R m = R(-2) * rho_s;
   for (int j = 0; j < 3; ++j)
     for (int i = 0; i < 3; ++i)
-      sig[i + 3 * j] = m * (c.cG * sym_at(k.G, i, j) + c.cGG * sym_at(k.H, i, j) + (i == j ? c.cI : 0.0));
+      sig[i + 3 * j] = m * (c.cG * sym_at(k.G, i, j) + c.cGG * sym_at(k.H, i, j) + (i == j ? c.cI : R(0)));
 }
 
 // Acoustic tensor Omega[i][j] = (1/rho_s) d_j sigma[0,i] (EquationsOfState.jl:223-246, n = e1),
 // written column-major: om[i + 3 j].
-HYP_HD void acoustic_omega(const EosC& e, const Kin& k, const Pows& w, const StressC& c, double xm1,
-                           const double* s0_over_rho, double* om) {
-  const double bs6 = e.b0sq / 6.0;
+template <class R>
+HYP_HD void acoustic_omega(const EosT<R>& e, const KinT<R>& k, const PowsT<R>& w, const StressCT<R>& c, R xm1,
+                           const R* s0_over_rho, R* om) {
+  const R bs6 = e.b0sq_6;
   for (int j = 0; j < 3; ++j) {
-    double G0j = sym_at(k.G, 0, j), H0j = sym_at(k.H, 0, j);
-    double di1 = -2.0 * G0j;
-    double dpsi = (2.0 / 3.0) * k.i1 * G0j - 2.0 * H0j;
-    double dcG, dcGG, dE3, dcI;
+    R G0j = sym_at(k.G, 0, j), H0j = sym_at(k.H, 0, j);
+    R di1 = R(-2) * G0j;
+    R dpsi = (R(2) / R(3)) * k.i1 * G0j - R(2) * H0j;
+    R dcG, dcGG, dE3, dcI;
     if (j == 0) {
-      double dp = -2.0 * k.p;
-      double dPb = 0.5 * e.beta * w.Pb1 * dp;
-      double dPa = 0.5 * e.alpha * w.Pa1 * dp;
-      double dPa1 = (0.5 * e.alpha - 1.0) * w.Pa2 * dp;
-      double dPg1 = (0.5 * e.gamma - 1.0) * w.Pg2 * dp;
-      double dPb1 = (0.5 * e.beta - 1.0) * w.Pb2 * dp;
+      R dp = R(-2) * k.p;
+      R dPb = R(0.5) * e.beta * w.Pb1 * dp;
+      R dPa = R(0.5) * e.alpha * w.Pa1 * dp;
+      R dPa1 = (R(0.5) * e.alpha - R(1)) * w.Pa2 * dp;
+      R dPg1 = (R(0.5) * e.gamma - R(1)) * w.Pg2 * dp;
+      R dPb1 = (R(0.5) * e.beta - R(1)) * w.Pb2 * dp;
       dcG = -bs6 * (dPb * k.i1 + w.Pb * di1);
-      dcGG = 0.5 * e.b0sq * dPb;
-      dE3 = e.kE3a * (dPa * w.Pa1 + (w.Pa - 1.0) * dPa1) + e.kE3g * dPg1 * xm1 +
+      dcGG = R(0.5) * e.b0sq * dPb;
+      dE3 = e.kE3a * (dPa * w.Pa1 + w.Pam1 * dPa1) + e.kE3g * dPg1 * xm1 +
             e.kE3b * (dPb1 * k.psi + w.Pb1 * dpsi);
       dcI = dE3 * k.p + c.E3 * dp;
     } else {
       dcG = -bs6 * w.Pb * di1;
-      dcGG = 0.0;
+      dcGG = R(0);
       dE3 = e.kE3b * w.Pb1 * dpsi;
       dcI = dE3 * k.p;
     }
     for (int i = 0; i < 3; ++i) {
-      double G0i = sym_at(k.G, 0, i), H0i = sym_at(k.H, 0, i);
-      double Gij = sym_at(k.G, i, j), Hij = sym_at(k.H, i, j);
-      double Gi0 = G0i;
-      double dG0i = -(G0j * (i == 0 ? 1.0 : 0.0) + Gij);
-      double dH0i = -(G0j * Gi0 + Hij + H0j * (i == 0 ? 1.0 : 0.0) + k.G.a00 * Gij);
-      double v = dcG * G0i + c.cG * dG0i + dcGG * H0i + c.cGG * dH0i + (i == 0 ? dcI : 0.0);
-      om[i + 3 * j] = -2.0 * v - (j == 0 ? s0_over_rho[i] : 0.0);
+      R G0i = sym_at(k.G, 0, i), H0i = sym_at(k.H, 0, i);
+      R Gij = sym_at(k.G, i, j), Hij = sym_at(k.H, i, j);
+      R Gi0 = G0i;
+      R dG0i = -(G0j * (i == 0 ? R(1) : R(0)) + Gij);
+      R dH0i = -(G0j * Gi0 + Hij + H0j * (i == 0 ? R(1) : R(0)) + k.G.a00 * Gij);
+      R v = dcG * G0i + c.cG * dG0i + dcGG * H0i + c.cGG * dH0i + (i == 0 ? dcI : R(0));
+      om[i + 3 * j] = R(-2) * v - (j == 0 ? s0_over_rho[i] : R(0));
     }
   }
 }
 
 // Eigenvalue moduli of a real 3x3 (column-major). Characteristic polynomial
 // mu^3 - c2 mu^2 + c1 mu - c0; single-precision closed-form seeds
-// (trigonometric for three real roots, Cardano otherwise), three FP64 Newton
-// steps on the seed of largest modulus (a real root r), and deflation to the
+// (trigonometric for three real roots, Cardano otherwise), three Newton steps
+// in R on the seed of largest modulus (a real root r), and deflation to the
 // quadratic mu^2 - (c2 - r) mu + c0/r for the other two (a complex pair has
 // modulus sqrt(c0/r)). Returns |r| and the two other moduli.
-HYP_HD void eig_core(const double* a, double* mods) {
-  double c2 = a[0] + a[4] + a[8];
-  double c1 = (a[0] * a[4] - a[3] * a[1]) + (a[0] * a[8] - a[6] * a[2]) + (a[4] * a[8] - a[7] * a[5]);
-  double c0 = det3(a);
+template <class R> HYP_HD void eig_core(const R* a, R* mods) {
+  R c2 = a[0] + a[4] + a[8];
+  R c1 = (a[0] * a[4] - a[3] * a[1]) + (a[0] * a[8] - a[6] * a[2]) + (a[4] * a[8] - a[7] * a[5]);
+  R c0 = det3(a);
   float C2 = (float)c2, C1 = (float)c1, C0 = (float)c0;
   float p = C1 - C2 * C2 * (1.0f / 3.0f);
   float q = -2.0f / 27.0f * C2 * C2 * C2 + C2 * C1 * (1.0f / 3.0f) - C0;
@@ -264,34 +299,34 @@ HYP_HD void eig_core(const double* a, double* mods) {
     float sd = sqrtf(fmaxf(disc, 0.0f));
     seed = cbrtf(-0.5f * q + sd) + cbrtf(-0.5f * q - sd) + C2 * (1.0f / 3.0f);
   }
-  double r = (double)seed;
+  R r = (R)seed;
   for (int it = 0; it < 3; ++it) {
-    double f = ((r - c2) * r + c1) * r - c0;
-    double fp = (3.0 * r - 2.0 * c2) * r + c1;
-    r = (fp != 0.0) ? r - f / fp : r;
+    R f = ((r - c2) * r + c1) * r - c0;
+    R fp = (R(3) * r - R(2) * c2) * r + c1;
+    r = (fp != R(0)) ? r - f / fp : r;
   }
-  double s, qq;
-  if (r != 0.0) {
+  R s, qq;
+  if (r != R(0)) {
     s = c2 - r;
     qq = c0 / r;
   } else {  // singular: the other roots solve mu^2 - c2 mu + c1
     s = c2;
     qq = c1;
   }
-  double dsc = s * s - 4.0 * qq;
+  R dsc = s * s - R(4) * qq;
   mods[0] = fabs(r);
-  if (dsc < 0.0) {
+  if (dsc < R(0)) {
     mods[1] = mods[2] = sqrt(fabs(qq));
   } else {
-    double sq = sqrt(dsc);
-    double ra = s >= 0.0 ? 0.5 * (s + sq) : 0.5 * (s - sq);
+    R sq = sqrt(dsc);
+    R ra = s >= R(0) ? R(0.5) * (s + sq) : R(0.5) * (s - sq);
     mods[1] = fabs(ra);
-    mods[2] = ra != 0.0 ? fabs(qq / ra) : fabs(s - ra);
+    mods[2] = ra != R(0) ? fabs(qq / ra) : fabs(s - ra);
   }
 }
 // Largest eigenvalue modulus (what the step consumes).
-HYP_HD double spectral_radius(const double* a) {
-  double m[3];
+template <class R> HYP_HD R spectral_radius(const R* a) {
+  R m[3];
   eig_core(a, m);
   return fmax(m[0], fmax(m[1], m[2]));
 }

@@ -1,0 +1,129 @@
+"""The mixed-precision single-phase step (FP32 fluxes, compensated FP32 state,
+float-float cons2prim islands) against FP64 (GPU).
+
+Accuracy target: relative L1 error of the density rho_true (cons2prim's
+density, HyperelasticityMPh.jl:114) <= 1e-6 against the FP64 oracle / FP64
+path; L-infinity is reported alongside."""
+import numpy as np
+import pytest
+
+from helpers import RTOL_FP64
+
+pytestmark = pytest.mark.gpu
+
+L1_TARGET = 1e-6
+
+
+def density(Q, rho0=8.93):
+    """rho_true = sqrt(det(rho A) / rho0) of SoA single-phase states (14, n)."""
+    m = Q[5:14]
+    det = (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[3] * (m[1] * m[8] - m[7] * m[2])
+           + m[6] * (m[1] * m[5] - m[4] * m[2]))
+    return np.sqrt(det / rho0)
+
+
+def errors(Qm, Qref):
+    a, b = density(Qm), density(Qref)
+    l1 = np.sum(np.abs(a - b)) / np.sum(np.abs(b))
+    linf = np.max(np.abs(a - b)) / np.max(np.abs(b))
+    return l1, linf
+
+
+def riemann(orc, nx):
+    from hyperelasticsolver_gb300._cases import riemann_1ph, initial_condition
+    import hyperelasticsolver_gb300 as h
+    Pl, Pr = riemann_1ph(h.Barton2009())
+    pb = orc.problem(nx=nx, cfl=0.5)
+    return initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx), pb
+
+
+def test_riemann_problem_mixed_vs_oracle(hyp, orc):
+    Q0, pb = riemann(orc, 1000)
+    t_end = 0.3 / orc.max_speed(pb, Q0)
+    Qo, so, to, _ = orc.run(pb, Q0, t_end=t_end)
+    with hyp.Solver(hyp.Barton2009(), 1000, precision="mixed", cfl=0.5) as s:
+        s.upload(Q0)
+        n, t = s.step(max_steps=so)
+        assert n == so
+        assert abs(t - to) <= 1e-5 * to  # dt from an FP32 max wave speed
+        l1, linf = errors(s.download(), Qo)
+    print(f"mixed Riemann N=1000, {n} steps: density L1 {l1:.2e}, Linf {linf:.2e}")
+    assert l1 <= L1_TARGET
+
+
+def test_random_states_mixed_vs_oracle(hyp, orc):
+    from test_gpu_1ph import random_prims
+    rng = np.random.default_rng(99)
+    nx, steps = 2048, 200
+    pb = orc.problem(nx=nx, cfl=0.5, bc=orc.BC_TRANSMISSIVE)
+    P = random_prims(nx, rng, strain=0.03, umax=0.3, smax=2e-4)
+    Q0 = np.ascontiguousarray(orc.prim2cons(pb, P).T)
+    Qo, _, to, _ = orc.run(pb, Q0, max_steps=steps)
+    with hyp.Solver(hyp.Barton2009(), nx, precision="mixed", bc="transmissive", cfl=0.5) as s:
+        s.upload(Q0)
+        n, t = s.step(max_steps=steps)
+        l1, linf = errors(s.download(), Qo)
+    print(f"mixed random states N={nx}, {steps} steps: density L1 {l1:.2e}, Linf {linf:.2e}")
+    assert l1 <= L1_TARGET
+
+
+def test_segments_mixed_vs_fp64_gpu(hyp, orc):
+    """The benchmark's initial data (64 seeded segments) at 2^20 cells, 200 steps:
+    mixed against the FP64 GPU path (itself held to 1e-12 of the oracle)."""
+    from hyperelasticsolver_gb300._cases import segment_states, segment_fill
+    eos = hyp.Barton2009()
+    nx = 1 << 20
+    Q0 = segment_fill(orc.prim2cons(orc.problem(), segment_states(eos)), nx)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with hyp.Solver(eos, nx, precision=prec, cfl=0.5) as s:
+            s.upload(Q0)
+            s.step(max_steps=200)
+            out[prec] = (s.download(), s.time()[0])
+    l1, linf = errors(out["mixed"][0], out["fp64"][0])
+    print(f"mixed vs fp64, 2^20 cells, 200 steps: density L1 {l1:.2e}, Linf {linf:.2e}")
+    assert l1 <= L1_TARGET
+    assert abs(out["mixed"][1] - out["fp64"][1]) <= 1e-5 * out["fp64"][1]
+
+
+def test_uniform_state_exact_in_mixed(hyp, orc):
+    nx = 1 << 16
+    P = np.array([8.93 / 1.02, 0.3, -0.2, 0.1, 1e-4, 1.02, 0.01, 0, 0, 1, 0.02, 0, 0, 1.0])
+    q = orc.prim2cons(orc.problem(), P)
+    Q0 = np.ascontiguousarray(np.repeat(q[:, None], nx, axis=1))
+    with hyp.Solver(hyp.Barton2009(), nx, precision="mixed", bc="transmissive") as s:
+        s.upload(Q0)
+        s.step(max_steps=5)
+        Q = s.download()
+    # the compensated pair reproduces the FP64 input to ~48 bits and does not move
+    assert np.max(np.abs(Q - Q0) / np.maximum(np.abs(Q0), 1e-300)) < 1e-13
+
+
+def test_mixed_graph_and_single_launches_agree(hyp, orc):
+    Q0, _ = riemann(orc, 700)
+    with hyp.Solver(hyp.Barton2009(), 700, precision="mixed") as a, \
+            hyp.Solver(hyp.Barton2009(), 700, precision="mixed") as b:
+        a.upload(Q0)
+        b.upload(Q0)
+        a.step(max_steps=41)  # graph replays (12 steps) plus single launches
+        for _ in range(41):
+            b.step(max_steps=1)
+        assert np.array_equal(a.download(), b.download())
+        assert a.time() == b.time()
+        assert a.max_wavespeed() == b.max_wavespeed()
+
+
+def test_mixed_t_end_split_and_wavespeed(hyp, orc):
+    Q0, pb = riemann(orc, 300)
+    with hyp.Solver(hyp.Barton2009(), 300, precision="mixed") as s, \
+            hyp.Solver(hyp.Barton2009(), 300) as d:
+        s.upload(Q0)
+        d.upload(Q0)
+        assert abs(s.max_wavespeed() - d.max_wavespeed()) <= 1e-6 * d.max_wavespeed()
+        n1, _ = s.step(max_steps=9)
+        n2, t2 = s.step(t_end=0.004)
+        lam = s.max_wavespeed()
+        n3, t3 = s.step(t_end=0.004)  # nothing to do; the state's max lambda must survive
+        assert n3 == 0 and t3 == t2 and s.max_wavespeed() == lam
+        m, _ = d.step(t_end=0.004)
+        assert abs((n1 + n2) - m) <= 1
