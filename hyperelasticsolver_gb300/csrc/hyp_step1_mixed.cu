@@ -48,7 +48,7 @@ struct MixedSlots {
   int rd, wr, clr;    // max-lambda slots: read (this step), write (next step), clear
 };
 
-__global__ void __launch_bounds__(kBlock, 3)
+__global__ void __launch_bounds__(kBlock, 4)
     step1_mixed_kernel(const float* __restrict__ Qh, const float* __restrict__ Ql, const float* __restrict__ lam,
                        const float* __restrict__ isl, float* __restrict__ Qh_out, float* __restrict__ Ql_out,
                        float* __restrict__ lam_out, float* __restrict__ isl_out, int64_t n, EosMixed em,
