@@ -34,6 +34,17 @@ def get_eigvals(eos, Q, n=(1, 0, 0)):
     return M.call("hyp_eval_eigvals", _cfg(eos), Q, 30, 12)
 
 
+def noncons_flux(eos, Q):
+    """Non-conservative matrix B(Q), 30x30 (HyperelasticityMPh.jl:178-250): only column 1
+    (phase-1 rows) and column 16 (phase-2 rows) are non-zero. Returns (30, 30) or (n, 30, 30)."""
+    bcol = M.call("hyp_eval_noncons", _cfg(eos), Q, 30, 30)
+    b = np.atleast_2d(bcol)
+    B = np.zeros((b.shape[0], 30, 30))
+    B[:, :15, 0] = b[:, :15]
+    B[:, 15:, 15] = b[:, 15:]
+    return B[0] if bcol.ndim == 1 else B
+
+
 def initial_states(eos, testcase):
     """Left/right conservative states of the Riemann test cases (HyperelasticityMPh.jl:275-426)."""
     from ._cases import mph_case

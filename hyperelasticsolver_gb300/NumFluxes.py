@@ -5,6 +5,20 @@ from . import _lib as L
 from . import _model as M
 
 
+def hll(eos, Q_l, Q_r, eigvals=None):
+    """Two-phase path-conservative HLL (NumFluxes.jl:70-132): returns (zeros(30), D-, D+).
+
+    The wave-speed bounds come from Q_l and Q_r, as main.jl:225 passes the eigenvalues of
+    the two cells; `eigvals` is accepted for signature compatibility and not used."""
+    cfg = M.config(eos, L.HYP_MODEL_MULTI, flux=L.HYP_FLUX_HLL)
+    l, n, single = L.soa(Q_l, 30)
+    r, _, _ = L.soa(Q_r, 30)
+    dm, dp = np.empty((30, n)), np.empty((30, n))
+    L.check(L.load().hyp_eval_hll(cfg, L.ptr(l), L.ptr(r), L.ptr(dm), L.ptr(dp), n), what="hll")
+    zero = np.zeros(30) if single else np.zeros((n, 30))
+    return zero, L.unsoa(dm, single), L.unsoa(dp, single)
+
+
 def lxf(eos, Q_l, Q_r, lam):
     """Lax-Friedrichs / Rusanov face flux (NumFluxes.jl:25-60).
 

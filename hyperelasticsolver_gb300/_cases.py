@@ -109,3 +109,23 @@ def segment_fill(states, nx):
     n_seg = states.shape[0]
     seg = (np.arange(nx, dtype=np.int64) * n_seg) // nx
     return np.ascontiguousarray(states[seg].T)
+
+
+def mph_interface_prims(eos, nx, a_hi=1.0 - 1e-6, a_lo=1e-6, width_cells=8):
+    """Two-phase primitive states (nx, 30) of the volume-fraction interface workload:
+    both phases carry the single-phase Riemann states (riemann_1ph) left and right of
+    x = 0.5, and alpha1 is a smoothed step from a_hi to a_lo over about width_cells
+    cells at x = 0.5 (the tanh profile of main.jl:110-123 with eps = width_cells * dx);
+    alpha2 = 1 - alpha1."""
+    Pl, Pr = riemann_1ph(eos)
+    x = (np.arange(nx) + 0.5) / nx
+    eps = width_cells / nx
+    a1 = a_lo + (a_hi - a_lo) * 0.5 * (1.0 - np.tanh(4.0 * (x - 0.5) / eps))
+    out = np.empty((nx, 30))
+    for i in range(nx):
+        P = Pl if x[i] < 0.5 else Pr
+        out[i, 0] = a1[i]
+        out[i, 1:15] = P
+        out[i, 15] = 1.0 - a1[i]
+        out[i, 16:30] = P
+    return out

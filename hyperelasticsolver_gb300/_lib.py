@@ -99,6 +99,8 @@ _SIGS = {
     "hyp_eval_flux": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_eigvals": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_lxf": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_noncons": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_hll": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
 }
 
 _lib = None

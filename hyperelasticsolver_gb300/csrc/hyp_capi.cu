@@ -48,6 +48,10 @@ static int free_ctx(hyp_ctx* c) {
   }
   cudaFree(c->F);
   cudaFree(c->lam);
+  cudaFree(c->smin);
+  cudaFree(c->smax);
+  cudaFree(c->DM);
+  cudaFree(c->DP);
   cudaFree(c->st);
   if (c->st_host) cudaFreeHost(c->st_host);
   for (auto& e : c->ev)
@@ -67,7 +71,11 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if (cfg->bc != HYP_BC_FROZEN && cfg->bc != HYP_BC_TRANSMISSIVE) return HYP_ERR_INVALID;
   if (cfg->precision != HYP_PREC_FP64 && cfg->precision != HYP_PREC_MIXED) return HYP_ERR_INVALID;
   if (!valid_eos(cfg->eos[0]) || (cfg->model == HYP_MODEL_MULTI && !valid_eos(cfg->eos[1]))) return HYP_ERR_INVALID;
-  if (cfg->model != HYP_MODEL_SINGLE || cfg->flux == HYP_FLUX_HLL) return HYP_ERR_UNSUPPORTED;
+  // single phase: Rusanov or LxF, FP64 or mixed; two phases: path-conservative HLL (the
+  // reference's main.jl:225 choice) in FP64
+  if (cfg->model == HYP_MODEL_SINGLE && cfg->flux == HYP_FLUX_HLL) return HYP_ERR_UNSUPPORTED;
+  if (cfg->model == HYP_MODEL_MULTI && (cfg->flux != HYP_FLUX_HLL || cfg->precision != HYP_PREC_FP64))
+    return HYP_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
   hyp_ctx* c = new (std::nothrow) hyp_ctx();
@@ -89,7 +97,19 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if (rc == HYP_OK && (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
     fail(e, "cudaStreamCreate");
   const size_t nq = (size_t)c->nvar * c->n * sizeof(double);
-  if (!mixed(c)) {
+  c->eos2.e[0] = c->eos[0];
+  c->eos2.e[1] = c->eos[1];
+  c->quad = gauss_legendre6();
+  if (cfg->model == HYP_MODEL_MULTI) {
+    const size_t nfb = (size_t)30 * (c->n + 1) * sizeof(double);
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p)
+      if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->F, nq)) != cudaSuccess) fail(e, "cudaMalloc(F)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->smin, (size_t)c->n * sizeof(double))) != cudaSuccess) fail(e, "cudaMalloc(smin)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->smax, (size_t)c->n * sizeof(double))) != cudaSuccess) fail(e, "cudaMalloc(smax)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->DM, nfb)) != cudaSuccess) fail(e, "cudaMalloc(DM)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->DP, nfb)) != cudaSuccess) fail(e, "cudaMalloc(DP)");
+  } else if (!mixed(c)) {
     for (int p = 0; p < 2 && rc == HYP_OK; ++p)
       if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");
     if (rc == HYP_OK && (e = cudaMalloc(&c->F, (size_t)kNFlux1 * c->n * sizeof(double))) != cudaSuccess)
@@ -208,7 +228,13 @@ static int enqueue_step(hyp_ctx* c, long long k, double t_end, bool prof) {
     if ((rc = prof_event(c, &e0)) || (rc = prof_event(c, &e1)) || (rc = prof_event(c, &e2))) return rc;
     CK(cudaEventRecord(e0, c->stream));
   }
-  if (!mixed(c)) {
+  if (c->cfg.model == HYP_MODEL_MULTI) {
+    const int p = (int)(k & 1);
+    CK(launch_cell2_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
+    CK(launch_face2_f64(c, p, t_end));
+    if (prof) CK(cudaEventRecord(e1, c->stream));
+    CK(launch_update2_f64(c, p, t_end));
+  } else if (!mixed(c)) {
     const int p = (int)(k & 1);
     CK(launch_cell1_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
     if (prof) CK(cudaEventRecord(e1, c->stream));
@@ -344,7 +370,10 @@ extern "C" int hyp_max_wavespeed(hyp_ctx* c, double* out) {
     return check_cell_error(c);
   }
   CK(cudaMemsetAsync(&c->st->lam_query, 0, sizeof(unsigned long long), c->stream));
-  CK(launch_cell1_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
+  if (c->cfg.model == HYP_MODEL_MULTI)
+    CK(launch_cell2_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
+  else
+    CK(launch_cell1_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
   int rc = sync_state(c);
   if (rc != HYP_OK) return rc;
   unsigned long long b = c->st_host->lam_query;

@@ -308,3 +308,51 @@ extern "C" int hyp_eval_lxf(const hyp_config* cfg, const double* Ql, const doubl
              },
              &m);
 }
+
+// ---- two-phase evaluators ----------------------------------------------------
+namespace {
+__global__ void k_noncons(ModelArg m, const double* Q, double* B, int64_t n) {
+  IDX double q[30], b[30];
+  LD(q, Q, 30);
+  noncons_bcol(m.e, q, b);
+  ST(B, b, 30);
+}
+struct HllArg {
+  ModelArg m;
+  Quad6D qd;
+};
+__global__ void k_hll(HllArg a, const double* Ql, const double* Qr, double* DMo, double* DPo, int64_t n) {
+  IDX double ql[30], qr[30], fl[30], fr[30], dm[30], dp[30];
+  LD(ql, Ql, 30);
+  LD(qr, Qr, 30);
+  flux2(a.m.e, ql, fl);
+  flux2(a.m.e, qr, fr);
+  double lo_l, hi_l, lo_r, hi_r;
+  speeds2(a.m.e, ql, lo_l, hi_l);
+  speeds2(a.m.e, qr, lo_r, hi_r);
+  hll_face2(a.m.e, a.qd, ql, qr, fl, fr, lo_l, hi_r, dm, dp);
+  ST(DMo, dm, 30);
+  ST(DPo, dp, 30);
+}
+}  // namespace
+
+extern "C" int hyp_eval_noncons(const hyp_config* cfg, const double* Q, double* bcol, int64_t n) {
+  if (!model_ok(cfg) || cfg->model != HYP_MODEL_MULTI) return HYP_ERR_INVALID;
+  ModelArg m = model_arg(cfg);
+  return run(n, {{Q, nullptr, 30}, {nullptr, bcol, 30}},
+             [](int64_t n, double** d, const void* a) {
+               k_noncons<<<grid(n), kBlock>>>(*(const ModelArg*)a, d[0], d[1], n);
+             },
+             &m);
+}
+
+extern "C" int hyp_eval_hll(const hyp_config* cfg, const double* Ql, const double* Qr, double* dm, double* dp,
+                            int64_t n) {
+  if (!model_ok(cfg) || cfg->model != HYP_MODEL_MULTI) return HYP_ERR_INVALID;
+  HllArg a{model_arg(cfg), gauss_legendre6()};
+  return run(n, {{Ql, nullptr, 30}, {Qr, nullptr, 30}, {nullptr, dm, 30}, {nullptr, dp, 30}},
+             [](int64_t n, double** d, const void* p) {
+               k_hll<<<(unsigned)((n + 63) / 64), 64>>>(*(const HllArg*)p, d[0], d[1], d[2], d[3], n);
+             },
+             &a);
+}

@@ -8,6 +8,7 @@
 #include "../../include/hyperelastic.h"
 #include "hyp_physics.cuh"
 #include "hyp_physics_mixed.cuh"
+#include "hyp_physics_mph.cuh"
 
 namespace hyp {
 
@@ -40,6 +41,11 @@ __host__ __device__ __forceinline__ int flux_slot1(int v) {
   return 5 + 2 * b + (a - 1);
 }
 
+// The two phases' EOS, passed to the two-phase kernels by value.
+struct Eos2 {
+  EosC e[2];
+};
+
 struct StepTiming {
   float ms_total = 0.f, ms_cell = 0.f, ms_update = 0.f;
   int n_cell = 0, n_update = 0;
@@ -65,6 +71,13 @@ struct hyp_ctx {
   float* lamf[2] = {nullptr, nullptr};
   float* isl[2] = {nullptr, nullptr};  // cached float-float island outputs [3][n] (1/rho, e_int, rho/rho0 - 1)
   hyp::EosMixed eos_mixed;
+  // two-phase (FP64): cell fluxes F [30][n], wave-speed bounds, face fluctuations [30][n+1]
+  hyp::Eos2 eos2;
+  hyp::Quad6D quad;
+  double* smin = nullptr;
+  double* smax = nullptr;
+  double* DM = nullptr;
+  double* DP = nullptr;
   hyp::DevState* st = nullptr;
   hyp::DevState* st_host = nullptr;  // pinned mirror
   int cur = 0;             // parity of the buffer that holds the current state
@@ -106,4 +119,9 @@ cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo);
 cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q);
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot);
 cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end);
+// two-phase FP64 launchers (hyp_step2.cu)
+cudaError_t launch_cell2_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
+cudaError_t launch_face2_f64(hyp_ctx* c, int p, double t_end);
+cudaError_t launch_update2_f64(hyp_ctx* c, int p, double t_end);
+Quad6D gauss_legendre6();
 }  // namespace hyp

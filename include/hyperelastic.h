@@ -160,6 +160,15 @@ int hyp_eval_eigvals(const hyp_config* cfg, const double* Q, double* out, int64_
 int hyp_eval_lxf(const hyp_config* cfg, const double* Ql, const double* Qr, const double* lambda, double* cons,
                  double* dm, double* dp, int64_t n);
 
+/* Two-phase non-conservative matrix B(Q) (HyperelasticityMPh.noncons_flux,
+   HyperelasticityMPh.jl:178-250). Only columns 1 and 16 of the 30x30 B are
+   non-zero; bcol[r] = B[r,1] for r < 15 and B[r,16] for r >= 15.  [30][n] */
+int hyp_eval_noncons(const hyp_config* cfg, const double* Q, double* bcol, int64_t n);
+/* Two-phase path-conservative HLL fluctuations (NumFluxes.hll, NumFluxes.jl:70-132)
+   with the wave speeds of Q_l and Q_r as main.jl:225 passes them; the conservative
+   part the reference returns is zeros(30).  Ql, Qr, dm, dp: [30][n] */
+int hyp_eval_hll(const hyp_config* cfg, const double* Ql, const double* Qr, double* dm, double* dp, int64_t n);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,117 @@
+"""Parity of the two-phase FP64 CUDA path (path-conservative HLL, volume-fraction
+and interface terms) with the oracle (GPU), at RTOL_FP64 = 1e-12."""
+import numpy as np
+import pytest
+
+from helpers import RTOL_FP64, assert_close, assert_close_soa
+
+pytestmark = pytest.mark.gpu
+
+B0_SOFT = 2.1 * np.sqrt(0.1)  # phase 2: shear modulus b0^2 scaled by 0.1, c0 held
+
+
+def eos_pair(hyp):
+    return (hyp.Barton2009(), hyp.Barton2009(_b0=B0_SOFT))
+
+
+def oracle_pb(orc, nx=3, cfl=0.5, bc=0):
+    return orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, nx=nx, cfl=cfl, bc=bc,
+                       eos=(orc.barton2009(), orc.barton2009(b0=B0_SOFT)))
+
+
+def random_mph(orc, n, rng):
+    """Random two-phase primitive states: alpha1 in (0.05, 0.95), per-phase strain and velocity."""
+    out = []
+    while len(out) < n:
+        row = []
+        a1 = rng.uniform(0.05, 0.95)
+        for a in (a1, 1 - a1):
+            F = np.eye(3) + 0.04 * rng.standard_normal((3, 3))
+            if np.linalg.det(F) <= 0.5:
+                break
+            row += [a, 8.93 / np.linalg.det(F), *rng.uniform(-0.4, 0.4, 3), rng.uniform(0, 5e-4),
+                    *F.reshape(-1, order="F")]
+        if len(row) == 30:
+            out.append(row)
+    return orc.prim2cons(oracle_pb(orc), np.array(out))
+
+
+def test_twophase_evaluators(hyp, orc):
+    from hyperelasticsolver_gb300 import HyperelasticityMPh as H, NumFluxes as NF
+    rng = np.random.default_rng(5)
+    Q = random_mph(orc, 64, rng)
+    eos, pb = eos_pair(hyp), oracle_pb(orc)
+    assert_close(H.flux_mph(eos, Q), orc.flux(pb, Q), RTOL_FP64, "flux_mph")
+    eg, eo = H.get_eigvals(eos, Q), orc.speeds(pb, Q)
+    assert_close(np.max(np.abs(eg), axis=1), np.max(np.abs(eo), axis=1), RTOL_FP64, "max |speed|")
+    B = H.noncons_flux(eos, Q)
+    bo = orc.noncons(pb, Q)
+    assert_close(B[:, :15, 0], bo[:, :15], RTOL_FP64, "B column 1")
+    assert_close(B[:, 15:, 15], bo[:, 15:], RTOL_FP64, "B column 16")
+    Ql, Qr = Q[:-1], Q[1:]
+    _, dm, dp = NF.hll(eos, Ql, Qr)
+    dmo, dpo = orc.hll(pb, Ql, Qr, eo[:-1], eo[1:])
+    assert_close(dm, dmo, 1e-11, "hll D-")
+    assert_close(dp, dpo, 1e-11, "hll D+")
+
+
+def test_golden_hll_face_on_gpu(hyp):
+    import json
+    import os
+    from hyperelasticsolver_gb300 import HyperelasticityMPh as H, NumFluxes as NF
+    with open(os.path.join(os.path.dirname(__file__), "golden", "golden_literal.json")) as fh:
+        g = json.load(fh)
+    eos = (hyp.Barton2009(), hyp.Barton2009(_b0=g["eos2_b0"]))
+    for c in g["noncons"]:
+        B = H.noncons_flux(eos, np.array(c["Q"]))
+        got = np.concatenate([B[:15, 0], B[15:, 15]])
+        assert_close(got, c["bcol"], RTOL_FP64, "golden noncons")
+    for h in g["hll"]:
+        _, dm, dp = NF.hll(eos, np.array(h["Ql"]), np.array(h["Qr"]))
+        assert_close(dm, h["dm"], 1e-11, "golden hll D-")
+        assert_close(dp, h["dp"], 1e-11, "golden hll D+")
+
+
+@pytest.mark.parametrize("testcase", [4, 6, 7])
+def test_reference_testcases_step(hyp, orc, testcase):
+    """The reference's two-phase Riemann test cases (HyperelasticityMPh.jl:275-426) on
+    100 cells with the HLL flux and frozen ends (main.jl:178-227), 30 steps."""
+    from hyperelasticsolver_gb300._cases import mph_case, initial_condition
+    nx, steps = 100, 30
+    pb = oracle_pb(orc, nx=nx, cfl=0.6)
+    Pl, Pr = mph_case(testcase)
+    Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
+    Qo, so, to, _ = orc.run(pb, Q0, max_steps=steps)
+    with hyp.Solver(eos_pair(hyp), nx, model="multi", flux="hll", cfl=0.6) as s:
+        s.upload(Q0)
+        n, t = s.step(max_steps=steps)
+        assert n == steps and abs(t - to) <= RTOL_FP64 * to
+        err = assert_close_soa(s.download(), Qo, RTOL_FP64, f"test case {testcase}")
+    print(f"two-phase test case {testcase}, {steps} steps: max per-variable relative error {err:.2e}")
+
+
+def test_smoothed_interface_transmissive(hyp, orc):
+    """Volume fraction going from 1 - 1e-6 to 1e-6 across 8 cells (tanh profile as
+    main.jl:110-123), transmissive ends."""
+    from hyperelasticsolver_gb300._cases import mph_interface_prims
+    nx, steps = 64, 12
+    P = mph_interface_prims(hyp.Barton2009(), nx)
+    pb = oracle_pb(orc, nx=nx, cfl=0.5, bc=orc.BC_TRANSMISSIVE)
+    Q0 = np.ascontiguousarray(orc.prim2cons(pb, P).T)
+    Qo, so, to, _ = orc.run(pb, Q0, max_steps=steps)
+    with hyp.Solver(eos_pair(hyp), nx, model="multi", flux="hll", bc="transmissive", cfl=0.5) as s:
+        s.upload(Q0)
+        n, t = s.step(max_steps=steps)
+        assert n == steps
+        err = assert_close_soa(s.download(), Qo, RTOL_FP64, "smoothed interface")
+    print(f"two-phase smoothed interface, {steps} steps: max per-variable relative error {err:.2e}")
+
+
+def test_twophase_uniform_state_preserved(hyp, orc):
+    rng = np.random.default_rng(8)
+    q = random_mph(orc, 1, rng)[0]
+    Q0 = np.ascontiguousarray(np.repeat(q[:, None], 4096, axis=1))
+    with hyp.Solver(eos_pair(hyp), 4096, model="multi", flux="hll", bc="transmissive") as s:
+        s.upload(Q0)
+        s.step(max_steps=3)
+        assert np.array_equal(s.download(), Q0)
