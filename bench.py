@@ -316,6 +316,101 @@ def run_ours(args):
     return 0
 
 
+def run_batch(args):
+    """Batched workload: 4096 independent single-phase Riemann problems, cell counts
+    log-uniform in [256, 65536] (seeded), 500 steps each with per-problem CFL dt, mixed
+    precision with the autotuned kernel variant, the whole run one CUDA-graph launch;
+    per-problem L1 density error against the FP64 batch."""
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300 import Hyperelasticity as H
+    from hyperelasticsolver_gb300._cases import batch_sizes, batch_prims, batch_fill
+    h.build_library()
+    eos = h.Barton2009()
+    sizes = batch_sizes(args.problems)
+    Pl, Pr = batch_prims(eos, len(sizes))
+    Q0 = batch_fill(H.prim2cons(eos, Pl), H.prim2cons(eos, Pr), sizes)
+    K, W = args.steps, args.warmup
+    total = int(sizes.sum())
+    with h.Batch(eos, sizes, precision="mixed") as b:
+        b.upload(Q0)
+        chosen, tune_ms = b.autotune(trial_steps=5)
+        b.upload(Q0)
+        b.step(W)
+        clk = ClockSampler()
+        clk.start()
+        b.step(K)
+        clocks = clk.stop()
+        ms = b.last_ms()
+        Qm = b.download()
+    with h.Batch(eos, sizes, precision="fp64") as b:
+        b.upload(Q0)
+        b.step(W)
+        b.step(K)
+        ms64 = b.last_ms()
+        Q64 = b.download()
+    a, r = density(Qm), density(Q64)
+    offs = np.concatenate([[0], np.cumsum(sizes)])
+    l1 = np.array([np.sum(np.abs(a[o:e] - r[o:e])) / np.sum(np.abs(r[o:e])) for o, e in zip(offs[:-1], offs[1:])])
+    linf = np.array([np.max(np.abs(a[o:e] - r[o:e])) / np.max(np.abs(r[o:e])) for o, e in zip(offs[:-1], offs[1:])])
+    peak, peak_kind = measured_peaks()
+    v = total * K / (ms / 1e3)
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic",
+            "config": {"workload": f"batched: {len(sizes)} single-phase Riemann problems, cell counts log-uniform in "
+                                   f"[256, 65536] (total {total}), per-problem CFL dt, {K} steps in one CUDA graph",
+                       "l2": "inputs larger than L2"},
+            "precision": PRECISION_NOTE["mixed"], "clocks": clocks,
+            "autotune": {"chosen_variant": chosen, "variants": ["128x8", "256x4", "256x3", "512x2"],
+                         "ms_per_step": [float(x) for x in tune_ms]},
+            "roofline": {"bound": "hbm", "achieved": BYTES_PER_CELL_UPDATE["single"] * total / (ms / K / 1e3) / 1e9,
+                         "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                         "frac": BYTES_PER_CELL_UPDATE["single"] * total / (ms / K / 1e3) / 1e9 / peak},
+            "fp64_batch": {"value": total * K / (ms64 / 1e3), "ms_per_step": ms64 / K},
+            "density_error_vs_fp64_per_problem": {"l1_max": float(l1.max()), "l1_median": float(np.median(l1)),
+                                                  "linf_max": float(linf.max())}}
+    print(json.dumps(line))
+    return 0
+
+
+def run_mph(args):
+    """Two-phase workload: 2^22 cells, alpha1 a smoothed step from 1 - 1e-6 to 1e-6 over
+    8 cells at x = 0.5, both phases carrying the single-phase Riemann states, phase 2 with
+    the shear modulus scaled by 0.1 (c0 held), path-conservative HLL, frozen ends, FP64."""
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300 import HyperelasticityMPh as HM
+    from hyperelasticsolver_gb300._cases import mph_interface_prims
+    h.build_library()
+    eos = (h.Barton2009(), h.Barton2009(_b0=2.1 * np.sqrt(0.1)))
+    n, K, W = args.n_cells, args.steps, args.warmup
+    Q0 = np.ascontiguousarray(HM.prim2cons_mph(eos, mph_interface_prims(eos[0], n)).T)
+    s = h.Solver(eos, n, model="multi", flux="hll", cfl=0.5)
+    s.upload(Q0)
+    s.step(max_steps=W)
+    s.set_profiling(True)
+    clk = ClockSampler()
+    clk.start()
+    s.step(max_steps=K)
+    clocks = clk.stop()
+    tm = s.timing()
+    s.close()
+    peak, peak_kind = measured_peaks()
+    v = n * K / (tm["ms_total"] / 1e3)
+    line = {"metric": METRIC, "value": v, "unit": METRIC, "n_gpus": 1, "steps": K, "warmup": W,
+            "ms_per_step": tm["ms_total"] / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"two-phase HLL path-conservative step, {n} cells, alpha1 1-1e-6 -> 1e-6 over "
+                                   "8 cells, phase 2 shear modulus x0.1", "l2": "inputs larger than L2"},
+            "precision": PRECISION_NOTE["fp64"], "clocks": clocks,
+            "kernels_ms_per_step": {"cell+face": tm["ms_cell"] / max(1, tm["n_cell"]),
+                                    "update": tm["ms_update"] / max(1, tm["n_update"])},
+            "roofline": {"bound": "hbm", "achieved": BYTES_PER_CELL_UPDATE["multi"] * n / (tm["ms_total"] / K / 1e3) / 1e9,
+                         "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
+                         "frac": BYTES_PER_CELL_UPDATE["multi"] * n / (tm["ms_total"] / K / 1e3) / 1e9 / peak}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -327,10 +422,21 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--workload", choices=["single", "batch", "mph"], default="single",
+                    help="single: the headline single-phase step; batch: 4096 ragged problems; mph: two-phase HLL")
+    ap.add_argument("--problems", type=int, default=4096)
     args = ap.parse_args()
     if args.warmup < 1:
         ap.error("--warmup must be >= 1")
-    return run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    if args.workload == "batch":
+        return run_batch(args)
+    if args.workload == "mph":
+        if args.n_cells == 1 << 24:
+            args.n_cells = 1 << 22
+        return run_mph(args)
+    return run_ours(args)
 
 
 if __name__ == "__main__":

@@ -11,7 +11,7 @@ from . import _lib
 from .build import build as build_library
 from . import EquationsOfState, Strains, Hyperelasticity, HyperelasticityMPh, NumFluxes, solver, _cases
 from .EquationsOfState import Barton2009
-from .solver import Solver
+from .solver import Solver, Batch
 
-__all__ = ["Barton2009", "Solver", "EquationsOfState", "Strains", "Hyperelasticity", "HyperelasticityMPh",
+__all__ = ["Barton2009", "Solver", "Batch", "EquationsOfState", "Strains", "Hyperelasticity", "HyperelasticityMPh",
            "NumFluxes", "solver", "build_library"]

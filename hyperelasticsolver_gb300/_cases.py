@@ -129,3 +129,37 @@ def mph_interface_prims(eos, nx, a_hi=1.0 - 1e-6, a_lo=1e-6, width_cells=8):
         out[i, 15] = 1.0 - a1[i]
         out[i, 16:30] = P
     return out
+
+
+def batch_sizes(n_problems=4096, lo=256, hi=65536, seed=SEGMENT_SEED):
+    """Cell counts floor(exp(U[ln lo, ln hi])) of the batched workload (seeded)."""
+    rng = np.random.default_rng(seed)
+    return np.floor(np.exp(rng.uniform(np.log(lo), np.log(hi), n_problems))).astype(np.int64)
+
+
+def batch_prims(eos, n_problems, seed=SEGMENT_SEED):
+    """Per-problem primitive Riemann states (left, right), each (n_problems, 14): the
+    single-phase Riemann states of riemann_1ph with a seeded jitter per problem
+    (velocity scale in [0.8, 1.2], left compression 1/A11 in [0.97, 0.99])."""
+    rng = np.random.default_rng(seed + 7)
+    L, R = [], []
+    for _ in range(n_problems):
+        su = rng.uniform(0.8, 1.2)
+        a11 = 1.0 / rng.uniform(0.97, 0.99)
+        pl, pr = riemann_1ph(eos, u_l=(0.0, 0.5 * su, 1.0 * su), u_r=(0.0, -0.5 * su, -1.0 * su),
+                             A_l=(a11, 1.0, 1.0))
+        L.append(pl)
+        R.append(pr)
+    return np.array(L), np.array(R)
+
+
+def batch_fill(Ql, Qr, sizes):
+    """Batch state SoA (14, sum(sizes)): problem p gets Ql[p] on (i-1) < N_p/2, Qr[p] after."""
+    total = int(np.sum(sizes))
+    out = np.empty((Ql.shape[1], total))
+    o = 0
+    for p, n in enumerate(sizes):
+        left = np.arange(n) < n / 2
+        out[:, o:o + n] = np.where(left[None, :], Ql[p][:, None], Qr[p][:, None])
+        o += n
+    return out

@@ -86,6 +86,17 @@ _SIGS = {
                         ctypes.c_int),
     "hyp_step_noalloc_f64": ([ctypes.POINTER(ConfigC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_double, ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "hyp_batch_create": ([ctypes.POINTER(ConfigC), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
+                          ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
+    "hyp_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
+    "hyp_batch_last_error": ([ctypes.c_void_p], ctypes.c_char_p),
+    "hyp_batch_upload": ([ctypes.c_void_p, _dp, ctypes.c_double], ctypes.c_int),
+    "hyp_batch_download": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "hyp_batch_step": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double], ctypes.c_int),
+    "hyp_batch_status": ([ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "hyp_batch_last_ms": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "hyp_batch_autotune": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp], ctypes.c_int),
+    "hyp_batch_set_variant": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "hyp_host_alloc": ([ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "hyp_host_free": ([ctypes.c_void_p], ctypes.c_int),
     "hyp_eval_finger": ([_dp, _dp, _i64], ctypes.c_int),

@@ -87,3 +87,85 @@ class Solver:
                                          ctypes.byref(nu)), self._h, "hyp_last_timing")
         return {"ms_total": a.value, "ms_cell": b.value, "n_cell": nc.value, "ms_update": d.value,
                 "n_update": nu.value}
+
+
+class Batch:
+    """Many independent single-phase problems of uneven size, advanced together.
+
+    `sizes` are the problems' cell counts; each problem lives on [0, X] with
+    dx = X / N_p and its own CFL time step and time (main.jl:202-227 per problem).
+    States are SoA (14, total) with problem p in columns offsets[p]:offsets[p+1]."""
+
+    def __init__(self, eos, sizes, flux="rusanov", bc="frozen", precision="mixed", X=1.0, cfl=0.5):
+        sizes = np.asarray(sizes, dtype=np.int64)
+        self.offsets = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+        self.n_problems = len(sizes)
+        self.total = int(self.offsets[-1])
+        self.cfg = M.config(eos, L.HYP_MODEL_SINGLE, self.total, _FLUXES[flux], _BCS[bc], _PRECS[precision], X, cfl)
+        h = ctypes.c_void_p()
+        off = self.offsets.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))
+        rc = L.load().hyp_batch_create(self.cfg, off, self.n_problems, ctypes.byref(h))
+        L.check(rc, what="hyp_batch_create")
+        self._h = h
+
+    def _check(self, rc, what):
+        if rc != L.HYP_OK:
+            msg = L.load().hyp_batch_last_error(self._h).decode()
+            raise L._ERRS.get(rc, L.HypError)(rc, f"{what}: {L._NAMES.get(rc, 'error')} ({msg})")
+
+    def close(self):
+        if getattr(self, "_h", None):
+            L.load().hyp_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def upload(self, Q, t0=0.0):
+        Q = np.ascontiguousarray(Q, dtype=np.float64)
+        if Q.shape != (14, self.total):
+            raise ValueError(f"batch state must be SoA (14, {self.total})")
+        self._check(L.load().hyp_batch_upload(self._h, L.ptr(Q), float(t0)), "hyp_batch_upload")
+
+    def download(self, out=None):
+        out = np.empty((14, self.total)) if out is None else out
+        self._check(L.load().hyp_batch_download(self._h, L.ptr(out)), "hyp_batch_download")
+        return out
+
+    def step(self, n_steps, t_end=math.inf):
+        self._check(L.load().hyp_batch_step(self._h, int(n_steps), float(t_end)), "hyp_batch_step")
+
+    def status(self):
+        t = np.empty(self.n_problems)
+        s = np.empty(self.n_problems, dtype=np.int64)
+        self._check(L.load().hyp_batch_status(self._h, L.ptr(t), s.ctypes.data_as(ctypes.POINTER(ctypes.c_int64))),
+                    "hyp_batch_status")
+        return t, s
+
+    def last_ms(self):
+        v = ctypes.c_double()
+        self._check(L.load().hyp_batch_last_ms(self._h, ctypes.byref(v)), "hyp_batch_last_ms")
+        return v.value
+
+    def autotune(self, trial_steps=10):
+        chosen = ctypes.c_int(-1)
+        ms = np.zeros(4)
+        self._check(L.load().hyp_batch_autotune(self._h, int(trial_steps), ctypes.byref(chosen), L.ptr(ms)),
+                    "hyp_batch_autotune")
+        return chosen.value, ms
+
+    def set_variant(self, v):
+        self._check(L.load().hyp_batch_set_variant(self._h, int(v)), "hyp_batch_set_variant")
+
+    def problem(self, Q, p):
+        """Columns of problem p in a SoA batch state."""
+        return Q[:, self.offsets[p]:self.offsets[p + 1]]

@@ -124,6 +124,31 @@ int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel
 int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_Q_out, int64_t n_cells, int n_steps,
                          double t0, void* stream, double* t_out, int64_t* err_cell);
 
+/* ---- batches of independent single-phase problems -------------------------- */
+/* The reference advances one problem per main.jl run (main.jl:202-241). A batch
+   advances n_problems independent problems of uneven size in lockstep, each with
+   its own dx = X / N_p, CFL time step (main.jl:212) and time. Problem p owns cells
+   [offsets[p], offsets[p+1]) of the SoA state [14][offsets[n_problems]]; cfg is
+   single-phase (Rusanov or LxF, FP64 or mixed) with cfg->n_cells == offsets[n_problems]. */
+typedef struct hyp_batch hyp_batch;
+int hyp_batch_create(const hyp_config* cfg, const int64_t* offsets, int n_problems, hyp_batch** out);
+int hyp_batch_destroy(hyp_batch* b);
+const char* hyp_batch_last_error(const hyp_batch* b);
+int hyp_batch_upload(hyp_batch* b, const double* Q, double t0);
+int hyp_batch_download(hyp_batch* b, double* Q);
+/* Every problem takes n_steps steps (one whose time reaches t_end stops there);
+   the n_steps launches run as one CUDA graph. */
+int hyp_batch_step(hyp_batch* b, int n_steps, double t_end);
+/* Per-problem time and step count (arrays of n_problems). */
+int hyp_batch_status(hyp_batch* b, double* t, int64_t* steps);
+/* Device time of the last hyp_batch_step. */
+int hyp_batch_last_ms(const hyp_batch* b, double* ms);
+/* Mixed precision: time each tile-kernel variant (block of 128/256/256/512 threads
+   at 8/4/3/2 resident blocks per SM) for trial_steps steps on the batch's own state
+   (restored afterwards) and keep the fastest; ms_per_step receives 4 timings. */
+int hyp_batch_autotune(hyp_batch* b, int trial_steps, int* chosen, double* ms_per_step);
+int hyp_batch_set_variant(hyp_batch* b, int variant);
+
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);
 int hyp_host_free(void* p);
