@@ -411,32 +411,91 @@ def run_mph(args):
     return 0
 
 
+def run_adjoint(args):
+    """Adjoint workload: 1000 FP64 Rusanov steps of a single-phase two-state problem on
+    65536 cells, gradient of L = 1/2 |rho_T - target|^2 with respect to the 13 left-state
+    parameters and the moduli (b0sq, k0), checkpoints every 50 steps with recompute in
+    between; target = the forward run at parameters perturbed by a seeded 2% Gaussian.
+    Reports the reverse pass (recompute + adjoint steps) against the plain forward run,
+    and the central-difference check (step 1e-6 relative) of all 15 components."""
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300.adjoint import RiemannMisfit, PARAM_NAMES
+    from hyperelasticsolver_gb300._cases import adjoint_states, adjoint_target_theta
+    h.build_library()
+    eos = h.Barton2009()
+    n, K = args.n_cells, args.steps
+    pl, pr = adjoint_states(eos)
+    pb = RiemannMisfit(eos, pl, pr, n, K, ckpt_every=args.ckpt_every)
+    th0 = pb.theta0()
+    target = pb.final_density(adjoint_target_theta(th0))
+    e, _, _, Q0 = pb.setup(th0)
+    with h.Solver(e, n, flux="rusanov", precision="fp64") as s:  # the plain forward run, for the ratio
+        for _ in range(max(1, args.warmup)):
+            s.upload(Q0)
+            s.step(max_steps=K)
+        s.upload(Q0)
+        clk = ClockSampler()
+        clk.start()
+        s.step(max_steps=K)
+        ms_fwd = s.timing()["ms_total"]
+        for _ in range(max(1, args.warmup) - 1):
+            pb.loss_and_grad(th0, target)
+        L, g, tm = pb.loss_and_grad(th0, target)
+        clocks = clk.stop()
+    fd = pb.fd_grad(th0, target)
+    scale = np.maximum(np.abs(fd), 1e-3 * np.max(np.abs(fd)))
+    rel = np.abs(g - fd) / scale
+    ms_rev = tm["ms_recompute"] + tm["ms_adjoint"]
+    line = {"metric": "adjoint cell-updates/s", "value": n * K / (ms_rev / 1e3), "unit": "cell-updates/s",
+            "n_gpus": 1, "steps": K, "warmup": args.warmup, "ms_per_step": ms_rev / K, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"adjoint of {K} FP64 Rusanov steps, {n} cells, gradient w.r.t. 13 left-state "
+                                   f"parameters + (b0sq, k0), checkpoint every {args.ckpt_every} steps",
+                       "l2": "state (7.3 MB) resident in L2"},
+            "clocks": clocks,
+            "adjoint_over_forward": ms_rev / ms_fwd,
+            "adjoint_steps_over_forward": tm["ms_adjoint"] / ms_fwd,
+            "ms": {"forward": ms_fwd, "record": tm["ms_record"], "recompute": tm["ms_recompute"],
+                   "adjoint": tm["ms_adjoint"]},
+            "loss": L,
+            "fd_check": {"max_rel": float(rel.max()), "per_param": {PARAM_NAMES[k]: float(rel[k]) for k in range(15)},
+                         "step_rel": 1e-6}}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--steps", type=int, default=None,
+                    help="timed steps (default: 200 single, 500 batch, 300 mph, 1000 adjoint)")
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    ap.add_argument("--n-cells", type=int, default=1 << 24)
+    ap.add_argument("--n-cells", type=int, default=None,
+                    help="cells (default: 2^24 single, 2^22 mph, 65536 adjoint)")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["single", "batch", "mph"], default="single",
-                    help="single: the headline single-phase step; batch: 4096 ragged problems; mph: two-phase HLL")
+    ap.add_argument("--workload", choices=["single", "batch", "mph", "adjoint"], default="single",
+                    help="single: the headline single-phase step; batch: 4096 ragged problems; mph: two-phase HLL; "
+                         "adjoint: gradient of a 1000-step run")
+    ap.add_argument("--ckpt-every", type=int, default=50)
     ap.add_argument("--problems", type=int, default=4096)
     args = ap.parse_args()
     if args.warmup < 1:
         ap.error("--warmup must be >= 1")
+    steps = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000}
+    cells = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536}
+    wl = "single" if args.impl == "reference" else args.workload
+    if args.steps is None:
+        args.steps = steps[wl]
+    if args.n_cells is None:
+        args.n_cells = cells[wl]
     if args.impl == "reference":
         return run_reference(args)
-    if args.workload == "batch":
-        return run_batch(args)
-    if args.workload == "mph":
-        if args.n_cells == 1 << 24:
-            args.n_cells = 1 << 22
-        return run_mph(args)
-    return run_ours(args)
+    runner = {"batch": run_batch, "adjoint": run_adjoint, "mph": run_mph}.get(args.workload, run_ours)
+    return runner(args)
 
 
 if __name__ == "__main__":

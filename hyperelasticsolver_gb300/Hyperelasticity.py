@@ -20,6 +20,19 @@ def prim2cons(eos, P):
     return M.call("hyp_eval_prim2cons", _cfg(eos), P, 14, 14)
 
 
+def prim2cons_vjp(eos, P, Qbar):
+    """Pullback of prim2cons: ((dQ/dP)^T Qbar per state, sum over states of (dL/d b0sq, dL/d k0))."""
+    p, n, single = L.soa(P, 14)
+    qb, n2, _ = L.soa(Qbar, 14)
+    if n2 != n:
+        raise ValueError("P and Qbar hold different numbers of states")
+    pb = np.empty((14, n))
+    eb = np.zeros(2)
+    L.check(L.load().hyp_eval_prim2cons_vjp(_cfg(eos), L.ptr(p), L.ptr(qb), L.ptr(pb), L.ptr(eb), n),
+            what="hyp_eval_prim2cons_vjp")
+    return L.unsoa(pb, single), eb
+
+
 def cons2prim(eos, Q):
     """(HyperelasticityMPh.jl:106-133 at alpha = 1); rho = sqrt(det(rho A)/rho0)."""
     return M.call("hyp_eval_cons2prim", _cfg(eos), Q, 14, 14)

@@ -9,7 +9,7 @@ call raises.
 """
 from . import _lib
 from .build import build as build_library
-from . import EquationsOfState, Strains, Hyperelasticity, HyperelasticityMPh, NumFluxes, solver, _cases
+from . import EquationsOfState, Strains, Hyperelasticity, HyperelasticityMPh, NumFluxes, solver, _cases, adjoint
 from .EquationsOfState import Barton2009
 from .solver import Solver, Batch
 

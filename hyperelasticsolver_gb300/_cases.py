@@ -53,6 +53,26 @@ def riemann_1ph(eos, u_l=(0.0, 0.5, 1.0), u_r=(0.0, -0.5, -1.0), A_l=(1 / 0.98, 
     return prim(u_l, A_l), prim(u_r, A_r)
 
 
+ADJOINT_SEED = 20261205
+
+
+def adjoint_states(eos):
+    """Primitive states of the adjoint workload: the two-state problem of riemann_1ph with a
+    normal velocity of +-0.1 b0 (|u1| in the wave-speed bound has a kink at u1 = 0, where the
+    loss would have no derivative) and a small shear in the left distortion, so that every
+    one of the 13 left-state parameters is non-zero."""
+    A_l = np.array([[1 / 0.98, 0.01, 0.0], [0.0, 1.0, 0.02], [0.0, 0.0, 1.0]])
+    def prim(u, A):
+        return np.array([eos.rho0 / np.linalg.det(A), *(np.asarray(u) * eos.b0), 0.0, *_col(A)])
+    return prim((0.1, 0.5, 1.0), A_l), prim((-0.1, -0.5, -1.0), np.eye(3))
+
+
+def adjoint_target_theta(theta0, seed=ADJOINT_SEED, scale=0.02):
+    """Parameters of the target run: theta0 * (1 + scale * N(0, 1)), seeded."""
+    rng = np.random.default_rng(seed)
+    return np.asarray(theta0) * (1.0 + scale * rng.standard_normal(len(theta0)))
+
+
 def initial_condition(Ql, Qr, nx):
     """Two-state Riemann fill, (i-1) < nx/2 on the left (main.jl:99-106). Returns SoA (nvar, nx)."""
     Ql, Qr = np.asarray(Ql, dtype=np.float64), np.asarray(Qr, dtype=np.float64)

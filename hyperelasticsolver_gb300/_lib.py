@@ -97,6 +97,10 @@ _SIGS = {
     "hyp_batch_last_ms": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "hyp_batch_autotune": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), _dp], ctypes.c_int),
     "hyp_batch_set_variant": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "hyp_adjoint_record": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_int, _dp], ctypes.c_int),
+    "hyp_adjoint": ([ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, _dp], ctypes.c_int),
+    "hyp_adjoint_timing": ([ctypes.c_void_p, _dp, _dp, _dp], ctypes.c_int),
+    "hyp_density_misfit": ([ctypes.c_void_p, _dp, _dp, ctypes.c_void_p], ctypes.c_int),
     "hyp_host_alloc": ([ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "hyp_host_free": ([ctypes.c_void_p], ctypes.c_int),
     "hyp_eval_finger": ([_dp, _dp, _i64], ctypes.c_int),
@@ -107,6 +111,7 @@ _SIGS = {
     "hyp_eval_acoustic": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_cons2prim": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_prim2cons": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_prim2cons_vjp": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_flux": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_eigvals": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_lxf": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _dp, _dp, _i64], ctypes.c_int),

@@ -38,6 +38,7 @@ static int free_ctx(hyp_ctx* c) {
   if (!c) return HYP_OK;
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
+  free_tape(c);
   for (auto& g : c->graph)
     if (g) cudaGraphExecDestroy(g);
   for (int p = 0; p < 2; ++p) {
@@ -152,6 +153,11 @@ static int sync_state(hyp_ctx* c) {
   CK(cudaStreamSynchronize(c->stream));
   return HYP_OK;
 }
+
+int ctx_set_err(hyp_ctx* c, int code, const std::string& msg) { return set_err(c, code, msg); }
+int ctx_sync_state(hyp_ctx* c) { return sync_state(c); }
+static int check_cell_error(hyp_ctx* c);
+int ctx_check_cell_error(hyp_ctx* c) { return check_cell_error(c); }
 
 static int check_cell_error(hyp_ctx* c) {
   int code = c->st_host->err_code;

@@ -53,6 +53,10 @@ struct StepTiming {
 
 }  // namespace hyp
 
+namespace hyp {
+struct AdjTape;
+}
+
 struct hyp_ctx {
   hyp_config cfg;
   hyp::EosC eos[2];
@@ -96,9 +100,19 @@ struct hyp_ctx {
   double graph_t_end = 0.0;
   std::string err;
   int64_t err_cell = -1;
+  hyp::AdjTape* tape = nullptr;  // checkpoints and buffers of the adjoint (hyp_adjoint.cu)
 };
 
+// Context helpers shared by the C-ABI files (hyp_capi.cu): record an error
+// message, copy the device status word to the host, turn a cell status into an
+// error code.
+int ctx_set_err(hyp_ctx* c, int code, const std::string& msg);
+int ctx_sync_state(hyp_ctx* c);
+int ctx_check_cell_error(hyp_ctx* c);
+
 namespace hyp {
+// adjoint buffers of a context (hyp_adjoint.cu)
+void free_tape(hyp_ctx* c);
 // single-phase FP64 step kernels (defined in hyp_step1.cu)
 __global__ void __launch_bounds__(kBlock) cell1_f64_kernel(const double* __restrict__ Q, int64_t n, EosC e,
                                                            double* __restrict__ F, double* __restrict__ lam,

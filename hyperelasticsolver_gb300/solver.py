@@ -88,6 +88,46 @@ class Solver:
         return {"ms_total": a.value, "ms_cell": b.value, "n_cell": nc.value, "ms_update": d.value,
                 "n_update": nu.value}
 
+    # ---- adjoint (single-phase FP64 Rusanov) ----
+    def record(self, n_steps, ckpt_every=50):
+        """n_steps steps (as step(n_steps)) that keep the state every ckpt_every
+        steps for adjoint(); returns the new time."""
+        t = ctypes.c_double(0.0)
+        L.check(L.load().hyp_adjoint_record(self._h, int(n_steps), int(ckpt_every), ctypes.byref(t)), self._h,
+                "hyp_adjoint_record")
+        return t.value
+
+    def adjoint(self, dQ_final):
+        """Pullback of the recorded run: dL/dQ of its initial state (nvar, nx) and
+        dL/d(b0sq, k0), from dL/dQ of the current (final) state."""
+        g = np.ascontiguousarray(dQ_final, dtype=np.float64)
+        if g.shape != (self.nvar, self.nx):
+            raise ValueError(f"dQ_final must be SoA {(self.nvar, self.nx)}, got {g.shape}")
+        out = np.empty((self.nvar, self.nx))
+        de = np.zeros(2)
+        L.check(L.load().hyp_adjoint(self._h, g.ctypes.data_as(ctypes.c_void_p), out.ctypes.data_as(ctypes.c_void_p),
+                                     L.ptr(de)), self._h, "hyp_adjoint")
+        return out, de
+
+    def adjoint_timing(self):
+        a, b, d = ctypes.c_double(), ctypes.c_double(), ctypes.c_double()
+        L.check(L.load().hyp_adjoint_timing(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(d)), self._h,
+                "hyp_adjoint_timing")
+        return {"ms_record": a.value, "ms_recompute": b.value, "ms_adjoint": d.value}
+
+    def density_misfit(self, target, grad=True):
+        """L = 1/2 sum (rho_i - target_i)^2 of the current state (rho = sqrt(det(rho A)/rho0))
+        and, with grad, dL/dQ (nvar, nx)."""
+        tg = np.ascontiguousarray(target, dtype=np.float64)
+        if tg.shape != (self.nx,):
+            raise ValueError(f"target must have shape ({self.nx},)")
+        loss = ctypes.c_double(0.0)
+        g = np.empty((self.nvar, self.nx)) if grad else None
+        L.check(L.load().hyp_density_misfit(self._h, L.ptr(tg), ctypes.byref(loss),
+                                            g.ctypes.data_as(ctypes.c_void_p) if grad else None), self._h,
+                "hyp_density_misfit")
+        return (loss.value, g) if grad else loss.value
+
 
 class Batch:
     """Many independent single-phase problems of uneven size, advanced together.

@@ -149,6 +149,32 @@ int hyp_batch_last_ms(const hyp_batch* b, double* ms);
 int hyp_batch_autotune(hyp_batch* b, int trial_steps, int* chosen, double* ms_per_step);
 int hyp_batch_set_variant(hyp_batch* b, int variant);
 
+/* ---- adjoint of the single-phase FP64 Rusanov run -------------------------- */
+/* The reference has no derivative code; these entry points are what a Julia
+   ChainRulesCore.rrule around a run of hyp_step binds: the forward pass records,
+   the pullback calls hyp_adjoint. They cover single-phase FP64 contexts with the
+   Rusanov flux (main.jl:45-48, 225), frozen or transmissive ends.
+
+   hyp_adjoint_record: n_steps steps from the current state, as hyp_step with no
+   t_end, keeping the state every ckpt_every steps (the first one included). */
+int hyp_adjoint_record(hyp_ctx* ctx, int n_steps, int ckpt_every, double* t_out);
+/* Reverse pass through the recorded run, which must end at the context's current
+   state: from dL/dQ of the final state (host [14][n]) it returns dL/dQ of the
+   recorded run's initial state (host [14][n], may be NULL) and dL_deos[2] =
+   (dL/d b0sq, dL/d k0), the Barton2009 shear and bulk moduli of
+   EquationsOfState.jl:111-112, each with the other held fixed. Segments between
+   checkpoints are recomputed with the forward step kernels (bit-identical), then
+   stepped backwards. dt = cfl dx / max lambda is differentiated through the
+   arg-max cell (the smallest index among equal maxima). */
+int hyp_adjoint(hyp_ctx* ctx, const double* dL_dQ_final, double* dL_dQ0, double* dL_deos);
+/* Device times (ms) of the last hyp_adjoint_record and of the recompute and
+   adjoint phases of the last hyp_adjoint. */
+int hyp_adjoint_timing(const hyp_ctx* ctx, double* ms_record, double* ms_recompute, double* ms_adjoint);
+/* Density misfit of the current state, L = 1/2 sum_i (rho_i - target_i)^2 with
+   rho_i = sqrt(det(rho A)_i / rho0) (HyperelasticityMPh.jl:114; the density
+   main.jl:71 writes), and dL/dQ (host [14][n], may be NULL). */
+int hyp_density_misfit(hyp_ctx* ctx, const double* rho_target, double* loss, double* dL_dQ);
+
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);
 int hyp_host_free(void* p);
@@ -174,6 +200,10 @@ int hyp_eval_acoustic(const hyp_barton2009* eos, const double* S, const double* 
    [alpha, rho_true, u(3), S, A(9)] (single phase: alpha dropped). [nvar][n] */
 int hyp_eval_cons2prim(const hyp_config* cfg, const double* Q, double* P, int64_t n);
 int hyp_eval_prim2cons(const hyp_config* cfg, const double* P, double* Q, int64_t n);
+/* Pullback of single-phase prim2cons: Pbar = (dQ/dP)^T Qbar per item ([14][n]),
+   eos_bar[2] = sum over items of (dL/d b0sq, dL/d k0). */
+int hyp_eval_prim2cons_vjp(const hyp_config* cfg, const double* P, const double* Qbar, double* Pbar, double* eos_bar,
+                           int64_t n);
 /* flux_mph / flux (HyperelasticityMPh.jl:140-175).  [nvar][n] */
 int hyp_eval_flux(const hyp_config* cfg, const double* Q, double* F, int64_t n);
 /* get_eigvals (HyperelasticityMPh.jl:252-266) with n = e1: per phase

@@ -2,6 +2,7 @@
 // CPU unit tests: lets tests compare the GPU math against the oracle without a
 // GPU. Compiled by tests/test_physics_host.py into a temporary shared library.
 #include "../hyperelasticsolver_gb300/csrc/hyp_physics.cuh"
+#include "../hyperelasticsolver_gb300/csrc/hyp_adjoint.cuh"
 
 using namespace hyp;
 
@@ -30,5 +31,46 @@ void hs_cell(const double* ep, const double* q, double* out) {
   out[15] = phase_cmax(e, P, c);
   out[16] = e.cv * log(P.xm1 + 1.0);
   out[17] = st;
+}
+
+// single-phase cell at alpha = 1: q (14) -> out = [flux (14), lambda]
+void hs_cell1(const double* ep, const double* q, double* out) {
+  EosC e = mk(ep);
+  CellFwd F = cell_forward(e, q);
+  double s0[3];
+  phase_flux(e, 1.0, F.P, F.c, out, s0);
+  out[14] = fabs(F.P.u[0]) + phase_cmax(e, F.P, F.c);
+}
+// qb (14) += (df/dq)^T fb + (dlambda/dq) lb; eb = (dL/db0sq, dL/dk0)
+int hs_cell1_vjp(const double* ep, const double* q, const double* fb, double lb, double* qb, double* eb) {
+  EosC e = mk(ep);
+  EosBar b{0.0, 0.0};
+  int st = cell_vjp(e, q, fb, lb, qb, b);
+  eb[0] = b.b0sq;
+  eb[1] = b.k0;
+  return st;
+}
+void hs_prim2cons1(const double* ep, const double* p, double* q) {
+  EosC e = mk(ep);
+  double p15[15], q15[15];
+  p15[0] = 1.0;
+  for (int t = 0; t < 14; ++t) p15[1 + t] = p[t];
+  double den = p15[1];
+  Kin k = kinematics(p15 + 6, det3(p15 + 6));
+  Pows w = powers(e, k);
+  double eint = e_cold(e, w) + e.cvt0 * w.Pg * (exp(p15[5] / e.cv) - 1.0) + e_shear(e, k, w);
+  double ek = 0.5 * (p15[2] * p15[2] + p15[3] * p15[3] + p15[4] * p15[4]);
+  q[0] = den;
+  for (int c = 0; c < 3; ++c) q[1 + c] = den * p15[2 + c];
+  q[4] = den * (eint + ek);
+  for (int c = 0; c < 9; ++c) q[5 + c] = den * p15[6 + c];
+  (void)q15;
+}
+void hs_prim2cons1_vjp(const double* ep, const double* p, const double* qb, double* pb, double* eb) {
+  EosC e = mk(ep);
+  EosBar b{0.0, 0.0};
+  prim2cons_vjp(e, p, qb, pb, b);
+  eb[0] = b.b0sq;
+  eb[1] = b.k0;
 }
 }

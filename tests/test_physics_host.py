@@ -24,6 +24,7 @@ def shim():
     L = ctypes.CDLL(so)
     for n in ("hs_energy", "hs_entropy", "hs_spectral_radius"):
         getattr(L, n).restype = ctypes.c_double
+    L.hs_cell1_vjp.restype = ctypes.c_int
     return L
 
 
@@ -88,3 +89,74 @@ def test_cell_flux_and_speed(shim, orc):
     out = np.zeros(18)
     shim.hs_cell(P(ea), P(np.concatenate([[1.0], Qbad])), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
     assert int(out[17]) & 1
+
+
+def _ep_moduli(ep, db0sq=0.0, dk0=0.0):
+    ep = np.array(ep, dtype=np.float64)
+    b0sq = ep[4] ** 2 + db0sq
+    k0 = ep[1] ** 2 - 4 / 3 * ep[4] ** 2 + dk0
+    ep[4], ep[1] = np.sqrt(b0sq), np.sqrt(k0 + 4 / 3 * b0sq)
+    return ep
+
+
+@pytest.mark.parametrize("ep", EOS)
+def test_cell_vjp_matches_central_differences(shim, ep):
+    """The hand-written reverse pass of the cell flux and wave speed (hyp_adjoint.cuh)
+    against central differences of the forward cell functions, for the 14 state
+    components and the moduli b0sq, k0 (each with the other held fixed)."""
+    ea = np.array(ep, dtype=np.float64)
+
+    def cell(e, q):
+        o = np.zeros(15)
+        shim.hs_cell1(P(e), P(q), P(o))
+        return o
+
+    rng = np.random.default_rng(7)
+    for trial in range(12):
+        A = np.eye(3) + 0.08 * rng.standard_normal((3, 3))
+        p = np.concatenate([[ep[0] * np.exp(0.05 * rng.standard_normal())], rng.standard_normal(3),
+                            [1e-4 * abs(rng.standard_normal()) * (trial % 2)], A.reshape(-1, order="F")])
+        q = np.zeros(14)
+        shim.hs_prim2cons1(P(ea), P(p), P(q))
+        w = rng.standard_normal(15)
+        qb, eb = np.zeros(14), np.zeros(2)
+        shim.hs_cell1_vjp(P(ea), P(q), P(w[:14]), ctypes.c_double(w[14]), P(qb), P(eb))
+        phi = lambda qq, e=ea: w @ cell(e, qq)
+        fd = np.zeros(14)
+        for t in range(14):
+            hq = 1e-6 * max(1.0, abs(q[t]))
+            d = np.zeros(14)
+            d[t] = hq
+            fd[t] = (phi(q + d) - phi(q - d)) / (2 * hq)
+        fe = np.array([(phi(q, _ep_moduli(ep, db0sq=1e-5)) - phi(q, _ep_moduli(ep, db0sq=-1e-5))) / 2e-5,
+                       (phi(q, _ep_moduli(ep, dk0=1e-5)) - phi(q, _ep_moduli(ep, dk0=-1e-5))) / 2e-5])
+        assert np.max(np.abs(qb - fd)) <= 1e-7 * np.max(np.abs(fd)), (trial, qb, fd)
+        assert np.max(np.abs(eb - fe)) <= 1e-7 * np.max(np.abs(fe)), (trial, eb, fe)
+
+
+def test_prim2cons_vjp_matches_central_differences(shim):
+    ea = np.array(EOS[0], dtype=np.float64)
+
+    def p2c(e, p):
+        o = np.zeros(14)
+        shim.hs_prim2cons1(P(e), P(p), P(o))
+        return o
+
+    rng = np.random.default_rng(8)
+    for trial in range(8):
+        A = np.eye(3) + 0.08 * rng.standard_normal((3, 3))
+        p = np.concatenate([[8.9], rng.standard_normal(3), [0.0], A.reshape(-1, order="F")])
+        qb = rng.standard_normal(14)
+        pb, eb = np.zeros(14), np.zeros(2)
+        shim.hs_prim2cons1_vjp(P(ea), P(p), P(qb), P(pb), P(eb))
+        phi = lambda pp, e=ea: qb @ p2c(e, pp)
+        fd = np.zeros(14)
+        for t in range(14):
+            hp = 1e-6 * max(1.0, abs(p[t])) if t != 4 else 1e-9  # S is on the scale of cv = 3.9e-4
+            d = np.zeros(14)
+            d[t] = hp
+            fd[t] = (phi(p + d) - phi(p - d)) / (2 * hp)
+        fe = np.array([(phi(p, _ep_moduli(EOS[0], db0sq=1e-5)) - phi(p, _ep_moduli(EOS[0], db0sq=-1e-5))) / 2e-5,
+                       (phi(p, _ep_moduli(EOS[0], dk0=1e-5)) - phi(p, _ep_moduli(EOS[0], dk0=-1e-5))) / 2e-5])
+        assert np.max(np.abs(pb - fd)) <= 1e-7 * np.max(np.abs(fd)), (trial, pb, fd)
+        assert np.max(np.abs(eb - fe)) <= 1e-7 * np.max(np.abs(fe)), (trial, eb, fe)
