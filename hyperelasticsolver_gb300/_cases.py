@@ -59,9 +59,9 @@ ADJOINT_SEED = 20261205
 def adjoint_states(eos):
     """Primitive states of the adjoint workload: the two-state problem of riemann_1ph with a
     normal velocity of +-0.1 b0 (|u1| in the wave-speed bound has a kink at u1 = 0, where the
-    loss would have no derivative) and a small shear in the left distortion, so that every
-    one of the 13 left-state parameters is non-zero."""
-    A_l = np.array([[1 / 0.98, 0.01, 0.0], [0.0, 1.0, 0.02], [0.0, 0.0, 1.0]])
+    loss would have no derivative) and small off-diagonal entries in the left distortion, so
+    that every one of the 13 left-state parameters is non-zero."""
+    A_l = np.array([[1 / 0.98, 0.01, 0.015], [0.012, 1.0, 0.02], [-0.01, 0.008, 1.0]])
     def prim(u, A):
         return np.array([eos.rho0 / np.linalg.det(A), *(np.asarray(u) * eos.b0), 0.0, *_col(A)])
     return prim((0.1, 0.5, 1.0), A_l), prim((-0.1, -0.5, -1.0), np.eye(3))

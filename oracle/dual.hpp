@@ -123,6 +123,21 @@ template <class T, int N, class S> Dual<T, N>& operator+=(Dual<T, N>& x, const S
 template <class T, int N, class S> Dual<T, N>& operator-=(Dual<T, N>& x, const S& y) { x = x - y; return x; }
 template <class T, int N, class S> Dual<T, N>& operator*=(Dual<T, N>& x, const S& y) { x = x * y; return x; }
 
+// ---- a dual of a lower nesting level (S convertible to T) is lifted into T --
+// (a constant with respect to the inner partials): lets an EOS modulus that
+// carries outer partials multiply the nested duals of the stress derivatives.
+template <class T, int N, class S>
+using lift_r = std::enable_if_t<is_dual<S>::value && !std::is_same<S, T>::value && std::is_convertible<S, T>::value,
+                                Dual<T, N>>;
+template <class T, int N, class S> lift_r<T, N, S> operator+(const Dual<T, N>& x, const S& y) { return x + T(y); }
+template <class T, int N, class S> lift_r<T, N, S> operator+(const S& y, const Dual<T, N>& x) { return T(y) + x; }
+template <class T, int N, class S> lift_r<T, N, S> operator-(const Dual<T, N>& x, const S& y) { return x - T(y); }
+template <class T, int N, class S> lift_r<T, N, S> operator-(const S& y, const Dual<T, N>& x) { return T(y) - x; }
+template <class T, int N, class S> lift_r<T, N, S> operator*(const Dual<T, N>& x, const S& y) { return x * T(y); }
+template <class T, int N, class S> lift_r<T, N, S> operator*(const S& y, const Dual<T, N>& x) { return T(y) * x; }
+template <class T, int N, class S> lift_r<T, N, S> operator/(const Dual<T, N>& x, const S& y) { return x / T(y); }
+template <class T, int N, class S> lift_r<T, N, S> operator/(const S& y, const Dual<T, N>& x) { return T(y) / x; }
+
 // ---- comparisons act on values --------------------------------------------
 template <class A, class B, class = std::enable_if_t<is_dual<A>::value || is_dual<B>::value>>
 bool operator<(const A& a, const B& b) { return value_of(a) < value_of(b); }

@@ -33,10 +33,13 @@ namespace hyp_oracle {
 
 // ---------------------------------------------------------------------------
 // EquationsOfState.jl:71-116  Barton2009 parameters and the derived b0sq, k0.
-struct Barton {
+// The moduli b0sq and k0 have the type PM: double, or a dual number when the
+// oracle differentiates a run with respect to them (forward mode).
+template <class PM> struct BartonT {
   double rho0, c0, cv, t0, b0, alpha, beta, gamma;
-  double b0sq, k0;
+  PM b0sq, k0;
 };
+using Barton = BartonT<double>;
 inline Barton make_barton(double rho0 = 8.93, double c0 = 4.6, double cv = 3.9e-4, double t0 = 300,
                           double b0 = 2.1, double alpha = 1, double beta = 3, double gamma = 2) {
   Barton e{rho0, c0, cv, t0, b0, alpha, beta, gamma, 0, 0};
@@ -127,7 +130,7 @@ template <class T> void invariants(const T* g, T* out) {
 
 // ---------------------------------------------------------------------------
 // EquationsOfState.jl:118-137  Barton2009 internal energy e(S, G).
-template <class T, class S> T energy(const Barton& e, const S& ent, const T* G) {
+template <class T, class S, class PM> T energy(const BartonT<PM>& e, const S& ent, const T* G) {
   T i[3];
   invariants(G, i);
   T U = ((0.5 * e.k0) / (e.alpha * e.alpha)) * ipow2(pow(i[2], 0.5 * e.alpha) - 1.0) +
@@ -136,7 +139,7 @@ template <class T, class S> T energy(const Barton& e, const S& ent, const T* G) 
   return U + W;
 }
 // EquationsOfState.jl:139-156  entropy from internal energy, argument clamped at 1e-6.
-template <class T> T entropy(const Barton& e, const T& e_int, const T* G) {
+template <class T, class PM> T entropy(const BartonT<PM>& e, const T& e_int, const T* G) {
   T i[3];
   invariants(G, i);
   T S = (e_int - ((0.5 * e.b0sq) * pow(i[2], 0.5 * e.beta)) * (ipow2(i[0]) / 3.0 - i[1])) -
@@ -147,7 +150,7 @@ template <class T> T entropy(const Barton& e, const T& e_int, const T* G) {
 }
 
 // ForwardDiff.gradient(G -> energy(eos, ent, G), G) with one chunk of 9.
-template <class T, class S> void denergy_dG(const Barton& e, const S& ent, const T* G, T* dedG) {
+template <class T, class S, class PM> void denergy_dG(const BartonT<PM>& e, const S& ent, const T* G, T* dedG) {
   using D = Dual<T, 9>;
   D g[9];
   for (int k = 0; k < 9; ++k) {
@@ -160,7 +163,7 @@ template <class T, class S> void denergy_dG(const Barton& e, const S& ent, const
 
 // EquationsOfState.jl:179-190  Cauchy stress sigma = -2 rho G dE/dG,
 // rho = rho0/det(F) (LU), G = finger(F).
-template <class T, class S> void stress(const Barton& e, const S& ent, const T* F, T* sig) {
+template <class T, class S, class PM> void stress(const BartonT<PM>& e, const S& ent, const T* F, T* sig) {
   T den = e.rho0 / det_lu(F);
   T G[9], dedG[9], a[9];
   finger(F, G);
@@ -173,7 +176,7 @@ template <class T, class S> void stress(const Barton& e, const S& ent, const T* 
 // EquationsOfState.jl:223-246  acoustic tensor for direction n:
 // dTdF = jacobian(F -> stress(eos, ent, F), F) reshaped (3,3,3,3),
 // A = (1/den) * dTdF, acoustic[i,j] = sum_{k,l,m} A[m,i,j,l] F[k,l] n[m] n[k].
-template <class T, class S> void acoustic(const Barton& e, const S& ent, const T* F, const double* n, T* ac) {
+template <class T, class S, class PM> void acoustic(const BartonT<PM>& e, const S& ent, const T* F, const double* n, T* ac) {
   using D = Dual<T, 9>;
   D f[9], sd[9];
   for (int k = 0; k < 9; ++k) {
@@ -278,7 +281,7 @@ template <class T> void eig3_moduli(const T* a, T* mods) {
 // ---------------------------------------------------------------------------
 // HyperelasticityMPh.jl:106-133  cons2prim for one phase.
 // Q[1] (alpha*rho) is never read: density comes from det(Q[7:15]/alpha).
-template <class T> void cons2prim(const Barton& e, const T* Q, T* P) {
+template <class T, class PM> void cons2prim(const BartonT<PM>& e, const T* Q, T* P) {
   T frac = Q[0];
   T FQ[9];
   for (int k = 0; k < 9; ++k) FQ[k] = Q[6 + k] / frac;
@@ -300,7 +303,7 @@ template <class T> void cons2prim(const Barton& e, const T* Q, T* P) {
   for (int k = 0; k < 9; ++k) P[6 + k] = A[k];
 }
 // HyperelasticityMPh.jl:66-87  prim2cons for one phase.
-template <class T> void prim2cons(const Barton& e, const T* P, T* Q) {
+template <class T, class PM> void prim2cons(const BartonT<PM>& e, const T* P, T* Q) {
   T frac = P[0], true_den = P[1];
   T den = frac * true_den;
   T G[9];
@@ -316,7 +319,7 @@ template <class T> void prim2cons(const Barton& e, const T* P, T* Q) {
 }
 
 // HyperelasticityMPh.jl:146-175  physical x-flux for one phase.
-template <class T> void flux(const Barton& e, const T* Q, T* Fx) {
+template <class T, class PM> void flux(const BartonT<PM>& e, const T* Q, T* Fx) {
   T frac = Q[0];
   T FQ[9];
   for (int k = 0; k < 9; ++k) FQ[k] = Q[6 + k] / frac;
@@ -349,7 +352,7 @@ template <class T> void flux(const Barton& e, const T* Q, T* Fx) {
 }
 
 // HyperelasticityMPh.jl:258-266  wave speeds u1 +- sqrt|eig(acoustic)| for one phase, n = e1.
-template <class T> void eigvals_phase(const Barton& e, const T* Q, T* spd6) {
+template <class T, class PM> void eigvals_phase(const BartonT<PM>& e, const T* Q, T* spd6) {
   T P[15];
   cons2prim(e, Q, P);
   const double n[3] = {1.0, 0.0, 0.0};
@@ -367,7 +370,7 @@ template <class T> void eigvals_phase(const Barton& e, const T* Q, T* spd6) {
 // HyperelasticityMPh.jl:178-250  non-conservative matrix B of the two-phase
 // model. Only column 1 of each 15x15 phase block is non-zero, so it is returned
 // as bcol[30]: bcol[r] = B[r, 1] for r in phase 1 and B[r, 16] for phase 2.
-template <class T> void noncons_cols(const Barton* eos, const T* Q, T* bcol) {
+template <class T, class PM> void noncons_cols(const BartonT<PM>* eos, const T* Q, T* bcol) {
   T frac[2], true_den[2], den[2], vel[2][3], e_total[2], e_int[2], A[2][9], G[2][9], ent[2], strs[2][9], temp[2];
   for (int p = 0; p < 2; ++p) {
     const T* q = Q + 15 * p;
@@ -490,15 +493,16 @@ enum { MODEL_SINGLE = 1, MODEL_MULTI = 2 };
 enum { FLUX_RUSANOV = 0, FLUX_LXF = 1, FLUX_HLL = 2 };
 enum { BC_FROZEN = 0, BC_TRANSMISSIVE = 1 };
 
-struct Problem {
+template <class PM> struct ProblemT {
   int model;
-  Barton eos[2];
+  BartonT<PM> eos[2];
   int flux;
   int bc;
   int nx;
   double X;
   double cfl;
 };
+using Problem = ProblemT<double>;
 inline int nvar_of(int model) { return model == MODEL_SINGLE ? 14 : 30; }
 inline int nspd_of(int model) { return model == MODEL_SINGLE ? 6 : 12; }
 
@@ -507,7 +511,7 @@ template <class T> void expand1(const T* q14, T* q15) {
   for (int k = 0; k < 14; ++k) q15[1 + k] = q14[k];
 }
 // flux_mph (HyperelasticityMPh.jl:140-144) / single-phase flux at alpha == 1.
-template <class T> void cell_flux(const Problem& pb, const T* Q, T* Fx) {
+template <class T, class PM> void cell_flux(const ProblemT<PM>& pb, const T* Q, T* Fx) {
   if (pb.model == MODEL_SINGLE) {
     T q15[15], f15[15];
     expand1(Q, q15);
@@ -519,7 +523,7 @@ template <class T> void cell_flux(const Problem& pb, const T* Q, T* Fx) {
   }
 }
 // get_eigvals (HyperelasticityMPh.jl:252-256): all phases' speeds.
-template <class T> void cell_speeds(const Problem& pb, const T* Q, T* spd) {
+template <class T, class PM> void cell_speeds(const ProblemT<PM>& pb, const T* Q, T* spd) {
   if (pb.model == MODEL_SINGLE) {
     T q15[15];
     expand1(Q, q15);
@@ -547,7 +551,7 @@ template <class T> T max_of(const T* v, int n) {
 
 // Path integral int_0^1 B(psi(s)) psi'(s) ds with psi(s) = Qa (1-s) + Qb s
 // (NumFluxes.jl:97-107 / :39-47): sum_i (w_i * B_i) * (Qb - Qa).
-template <class T> void path_integral(const Problem& pb, const Quad6& qd, const T* Qa, const T* Qb, T* out) {
+template <class T, class PM> void path_integral(const ProblemT<PM>& pb, const Quad6& qd, const T* Qa, const T* Qb, T* out) {
   T dv[30], u[30], bcol[30], acc[30];
   for (int k = 0; k < 30; ++k) dv[k] = Qb[k] - Qa[k];
   for (int i = 0; i < 6; ++i) {
@@ -565,7 +569,7 @@ template <class T> void path_integral(const Problem& pb, const Quad6& qd, const 
 
 // NumFluxes.jl:25-60  lxf: cons = 0.5 (f_l + f_r) - 0.5 lambda (Q_r - Q_l),
 // noncons D- = D+ = 0.5 * Gauss-Lobatto path integral (two-phase only).
-template <class T> void lxf_face(const Problem& pb, const T* Ql, const T* Qr, const T& lambda, T* cons, T* dm, T* dp,
+template <class T, class PM> void lxf_face(const ProblemT<PM>& pb, const T* Ql, const T* Qr, const T& lambda, T* cons, T* dm, T* dp,
                                  const T* fl = nullptr, const T* fr = nullptr) {
   int nv = nvar_of(pb.model);
   T fl_[30], fr_[30];
@@ -587,7 +591,7 @@ template <class T> void lxf_face(const Problem& pb, const T* Ql, const T* Qr, co
 // literal = 1 repeats the evaluations the reference repeats (get_eigvals(Q_m)
 // twice, flux_mph six times, B_int(Q_l,Q_hll) and B_int(Q_hll,Q_r) twice each);
 // the results are identical, only the cost differs.
-template <class T> void hll_face(const Problem& pb, const T* Ql, const T* Qr, const T* spdL, const T* spdR, T* dm, T* dp,
+template <class T, class PM> void hll_face(const ProblemT<PM>& pb, const T* Ql, const T* Qr, const T* spdL, const T* spdR, T* dm, T* dp,
                                  int literal = 0) {
   const int reps = literal ? 2 : 1;
   T Qm[30], spdM[12];
@@ -627,7 +631,7 @@ template <class T> void hll_face(const Problem& pb, const T* Ql, const T* Qr, co
 // (main.jl:30-60); literal = 0: each face once. Both give identical results.
 // dt_given (optional): use this time step instead of cfl*dx/max lambda (for checking a
 // window of a larger run whose dt came from cells outside the window).
-template <class T> T step(const Problem& pb, std::vector<T>& Q, int literal, int nthreads, T* lam_max_out = nullptr,
+template <class T, class PM> T step(const ProblemT<PM>& pb, std::vector<T>& Q, int literal, int nthreads, T* lam_max_out = nullptr,
                           const T* dt_given = nullptr) {
   const int nx = pb.nx, nv = nvar_of(pb.model), ns = nspd_of(pb.model);
   const bool trans = pb.bc == BC_TRANSMISSIVE;

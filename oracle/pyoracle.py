@@ -98,6 +98,8 @@ def lib():
         L.hyo_quadrature.restype = None
         L.hyo_max_speed.argtypes = [pp, dp, ctypes.c_int]
         L.hyo_max_speed.restype = ctypes.c_double
+        L.hyo_misfit_grad_dual.argtypes = [pp, dp, dp, ctypes.c_int, dp, ctypes.c_int, dp, dp]
+        L.hyo_misfit_grad_dual.restype = ctypes.c_int
         _lib = L
     return _lib
 
@@ -267,3 +269,22 @@ def run_dts(pb, Q_soa, dts, nthreads=0):
     if rc != 0:
         raise ValueError(f"hyo_run_dts failed ({rc})")
     return Q
+
+
+def misfit_grad_dual(pb, prim_left, prim_right, n_steps, target, nthreads=1):
+    """Forward-mode (15 partials) value and gradient of L = 1/2 sum (rho_i - target_i)^2
+    after n_steps of the single-phase two-state problem (cells i < nx/2 left), with
+    respect to the left state (rho, u(3), A(9) column-major) and the moduli (b0sq, k0).
+    Every scalar of the oracle run is a dual number, so the reference's nested-dual
+    stress and acoustic tensor carry the outer partials too. Returns (L, grad(15))."""
+    tg = np.ascontiguousarray(target, dtype=np.float64)
+    pb.nx = len(tg)
+    pl = np.ascontiguousarray(prim_left, dtype=np.float64)
+    pr = np.ascontiguousarray(prim_right, dtype=np.float64)
+    loss = np.zeros(1)
+    g = np.zeros(15)
+    rc = lib().hyo_misfit_grad_dual(ctypes.byref(pb), _ptr(pl), _ptr(pr), int(n_steps), _ptr(tg), int(nthreads),
+                                    _ptr(loss), _ptr(g))
+    if rc != 0:
+        raise ValueError(f"hyo_misfit_grad_dual failed ({rc})")
+    return loss[0], g

@@ -43,6 +43,20 @@ def test_gradient_matches_central_differences(bc):
     print(f"adjoint vs central differences ({bc}): max rel {worst:.2e}")
 
 
+def test_gradient_matches_forward_mode_dual_oracle(orc):
+    """Against a forward-mode dual-number run of the oracle (the reference
+    restatement with every scalar carrying the 15 partials), same target."""
+    import os
+    pb, th0, target = _problem(nx=128, n_steps=60, K=16)
+    L, g, _ = pb.loss_and_grad(th0, target)
+    Lo, go = orc.misfit_grad_dual(orc.problem(nx=128, cfl=0.5), pb.prim_left, pb.prim_right, 60, target,
+                                  nthreads=min(8, os.cpu_count() or 1))
+    assert abs(L - Lo) <= 1e-10 * Lo
+    rel = np.abs(g - go) / np.maximum(np.abs(go), 1e-3 * np.max(np.abs(go)))
+    print(f"adjoint vs dual-number oracle: max rel {rel.max():.2e}")
+    assert rel.max() <= 1e-8, [(PARAM_NAMES[k], g[k], go[k]) for k in np.argsort(-rel)[:4]]
+
+
 def test_checkpoint_interval_does_not_change_the_gradient():
     pb, th0, target = _problem(n_steps=50)
     gs = []

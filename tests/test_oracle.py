@@ -173,3 +173,39 @@ def test_literal_and_face_modes_agree_bitwise(orc, model, flux):
     a = orc.run(pb, Q0, max_steps=3, literal=True, nthreads=2)[0]
     b = orc.run(pb, Q0, max_steps=3, literal=False, nthreads=2)[0]
     assert np.array_equal(a, b)
+
+
+def test_dual_run_gradient_matches_central_differences(orc):
+    """The oracle's forward-mode run (every scalar a dual with 15 partials: the left
+    state and the moduli b0sq, k0) against central differences of plain oracle runs."""
+    from hyperelasticsolver_gb300._cases import adjoint_states, initial_condition
+    from hyperelasticsolver_gb300.EquationsOfState import Barton2009
+    eos = Barton2009()
+    pl, pr = adjoint_states(eos)
+    nx, steps = 24, 8
+    idx = [0, 1, 2, 3, 5, 6, 7, 8, 9, 10, 11, 12, 13]
+    theta0 = np.concatenate([pl[idx], [eos.b0sq, eos.k0]])
+    target = np.full(nx, eos.rho0)
+
+    def loss(th):
+        b0sq, k0 = th[13], th[14]
+        e = orc.barton2009(b0=np.sqrt(b0sq), c0=np.sqrt(k0 + 4 / 3 * b0sq))
+        pb = orc.problem(nx=nx, cfl=0.5, eos=(e, e))
+        p = pl.copy()
+        p[idx] = th[:13]
+        Q, _, _, _ = orc.run(pb, initial_condition(orc.prim2cons(pb, p), orc.prim2cons(pb, pr), nx),
+                             max_steps=steps, nthreads=2)
+        rho = orc.cons2prim(pb, Q.T)[:, 0]
+        return 0.5 * np.sum((rho - target) ** 2)
+
+    L, g = orc.misfit_grad_dual(orc.problem(nx=nx, cfl=0.5), pl, pr, steps, target, nthreads=2)
+    assert abs(L - loss(theta0)) <= 1e-13 * L
+    fd = np.zeros(15)
+    for k in range(15):
+        h = 1e-6 * max(abs(theta0[k]), 1.0)  # an absolute floor keeps rounding out of the small entries
+        tp, tm = theta0.copy(), theta0.copy()
+        tp[k] += h
+        tm[k] -= h
+        fd[k] = (loss(tp) - loss(tm)) / (tp[k] - tm[k])
+    rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * np.max(np.abs(fd)))
+    assert rel.max() <= 1e-6, rel
