@@ -23,6 +23,7 @@ HYP_MODEL_SINGLE, HYP_MODEL_MULTI = 1, 2
 HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = 0, 1, 2
 HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = 0, 1
 HYP_PREC_FP64, HYP_PREC_MIXED = 0, 1
+HYP_BATCH_NUM_VARIANTS = 6
 
 
 class HypError(RuntimeError):

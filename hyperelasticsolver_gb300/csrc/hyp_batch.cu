@@ -201,11 +201,15 @@ __global__ void __launch_bounds__(kBlock) batch_f64_update_kernel(const double* 
 }
 
 // ---- mixed kernel variants (autotuned) -------------------------------------------
+// A variant: block size, resident blocks per SM the registers are budgeted for,
+// and whether the grid is persistent (one wave of blocks striding over the tile
+// table) or one block per tile.
 struct Variant {
-  int block, minb;
+  int block, minb, persist;
 };
-constexpr Variant kVariants[] = {{128, 8}, {256, 4}, {256, 3}, {512, 2}};
-constexpr int kNumVariants = 4;
+constexpr Variant kVariants[] = {{128, 8, 1}, {256, 4, 1}, {256, 3, 1}, {512, 2, 1}, {128, 8, 0}, {256, 4, 0}};
+constexpr int kNumVariants = HYP_BATCH_NUM_VARIANTS;
+static_assert(sizeof(kVariants) / sizeof(kVariants[0]) == kNumVariants, "variant table");
 
 template <int BLOCK, int MINB>
 cudaError_t launch_batch_mixed_t(cudaStream_t s, int grid, const MixedArrays& a, const EosMixed& em,
@@ -301,18 +305,19 @@ static int select_variant(hyp_batch* b, int v) {
   if (v < 0 || v >= kNumVariants) return berr(b, HYP_ERR_INVALID, "no such kernel variant");
   int res = 0;
   switch (v) {
-    case 0: res = resident_blocks<128, 8>(); break;
-    case 1: res = resident_blocks<256, 4>(); break;
+    case 0: case 4: res = resident_blocks<128, 8>(); break;
+    case 1: case 5: res = resident_blocks<256, 4>(); break;
     case 2: res = resident_blocks<256, 3>(); break;
     default: res = resident_blocks<512, 2>(); break;
   }
   b->variant = v;
-  b->grid = b->sms * (res > 0 ? res : 1);
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
-  return build_tiles(b, kVariants[v].block - 2);
+  const int rc = build_tiles(b, kVariants[v].block - 2);
+  b->grid = kVariants[v].persist ? b->sms * (res > 0 ? res : 1) : b->ntiles;
+  return rc;
 }
 
 static MixedArrays batch_arrays(hyp_batch* b, int p) {
@@ -338,6 +343,8 @@ static int enqueue_batch_step(hyp_batch* b, long long k, double t_end) {
     switch (b->variant) {
       case 0: e = launch_batch_mixed_t<128, 8>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
       case 1: e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
+      case 4: e = launch_batch_mixed_t<128, 8>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
+      case 5: e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
       case 2: e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
       default: e = launch_batch_mixed_t<512, 2>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
     }

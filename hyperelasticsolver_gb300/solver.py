@@ -198,7 +198,7 @@ class Batch:
 
     def autotune(self, trial_steps=10):
         chosen = ctypes.c_int(-1)
-        ms = np.zeros(4)
+        ms = np.zeros(L.HYP_BATCH_NUM_VARIANTS)
         self._check(L.load().hyp_batch_autotune(self._h, int(trial_steps), ctypes.byref(chosen), L.ptr(ms)),
                     "hyp_batch_autotune")
         return chosen.value, ms

@@ -80,8 +80,9 @@ def test_mixed_batch_accuracy_and_autotune(hyp, orc):
     with hyp.Batch(hyp.Barton2009(), sizes, precision="mixed") as b:
         b.upload(Q0)
         chosen, ms = b.autotune(trial_steps=5)
-        assert 0 <= chosen < 4 and np.all(ms > 0)
-        for v in range(4):
+        nv = hyp._lib.HYP_BATCH_NUM_VARIANTS
+        assert 0 <= chosen < nv and len(ms) == nv and np.all(ms > 0)
+        for v in range(nv):
             b.set_variant(v)
             b.upload(Q0)
             b.step(500)
