@@ -472,6 +472,8 @@ extern "C" int hyp_eval_prim2cons_vjp(const hyp_config* cfg, const double* P, co
                                       double* eos_bar, int64_t n) {
   if (!cfg || !P || !Qbar || !Pbar || !eos_bar || n <= 0) return HYP_ERR_INVALID;
   if (cfg->model != HYP_MODEL_SINGLE) return HYP_ERR_UNSUPPORTED;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
   const hyp_barton2009& b = cfg->eos[0];
   const EosC e = make_eos(b.rho0, b.c0, b.cv, b.t0, b.b0, b.alpha, b.beta, b.gamma);
   double *dP = nullptr, *dQ = nullptr, *dR = nullptr, *dE = nullptr;
