@@ -30,6 +30,13 @@ struct TileDesc {
   int lead;       // 1 for the problem's first tile: it advances the problem's time
 };
 
+// A tile's step control, written each step by batch_mixed_ctl_kernel so that the
+// tile kernel reads it alongside the tile descriptor (no dependent load).
+struct TileCtl {
+  float dtdx;
+  int active;
+};
+
 // Per-problem loop control on the device.
 struct BatchDev {
   double* t;                   // [2][P] time before the step of parity p
@@ -39,43 +46,62 @@ struct BatchDev {
   int P;
 };
 
-cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int64_t m);
-cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int64_t m);
 
 // ---- mixed precision ---------------------------------------------------------
+// Step control of every tile: dt/dx and whether its problem is still running;
+// the problem's lead tile advances the problem's time and step count and
+// rotates its max-lambda slots (read rd, write wr, clear clr; a finished
+// problem carries its max lambda from rd to wr).
+__global__ void batch_mixed_ctl_kernel(const TileDesc* __restrict__ tiles, int ntiles, BatchDev b, int par, int rd,
+                                       int wr, int clr, double t_end, double cfl, TileCtl* __restrict__ ctl) {
+  const int tix = blockIdx.x * blockDim.x + threadIdx.x;
+  if (tix >= ntiles) return;
+  const int P = b.P;
+  const TileDesc d = tiles[tix];
+  const int p = d.problem;
+  const double tn = b.t[par * P + p];
+  const bool active = tn < t_end;
+  const float lmax = __uint_as_float((unsigned)b.slots[rd * P + p]);
+  ctl[tix] = TileCtl{(float)cfl / lmax, active ? 1 : 0};
+  if (d.lead) {
+    const double dt = (cfl * b.dx[p]) / (double)lmax;
+    b.t[(1 - par) * P + p] = active ? tn + dt : tn;
+    b.slots[clr * P + p] = 0ull;
+    if (active) b.steps[p] += 1;
+    else b.slots[wr * P + p] = b.slots[rd * P + p];  // a finished problem keeps its max lambda
+  }
+}
+
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB)
-    batch_mixed_kernel(MixedArrays a, EosMixed em, const TileDesc* __restrict__ tiles, int ntiles, BatchDev b, int par,
-                       int rd, int wr, int clr, double t_end, double cfl, int flux, int bc, DevState* S) {
-  const int P = b.P;
+    batch_mixed_kernel(MixedArrays a, EosMixed em, const TileDesc* __restrict__ tiles,
+                       const TileCtl* __restrict__ ctl, int ntiles, unsigned long long* __restrict__ slots_wr,
+                       int flux, int bc, DevState* S) {
   for (int tix = blockIdx.x; tix < ntiles; tix += gridDim.x) {
     const TileDesc d = tiles[tix];
-    const int p = d.problem;
-    const double tn = b.t[par * P + p];
-    const bool active = tn < t_end;
-    const float lmax = __uint_as_float((unsigned)b.slots[rd * P + p]);
-    const float dtdx = (float)cfl / lmax;
-    if (d.lead && threadIdx.x == 0) {
-      const double dt = (cfl * b.dx[p]) / (double)lmax;
-      b.t[(1 - par) * P + p] = active ? tn + dt : tn;
-      b.slots[clr * P + p] = 0ull;
-      if (active) b.steps[p] += 1;
-      else b.slots[wr * P + p] = b.slots[rd * P + p];  // a finished problem keeps its max lambda
-    }
-    if (!active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
+    const TileCtl k = ctl[tix];
+    const MixedGlobalLoader<BLOCK> ld{a};
+    MixedCellIn c;
+    mixed_tile_load(d.first, d.lo, d.hi, ld, c);
+    if (!k.active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
       const int64_t n = a.stride;
-      for (int64_t i = d.first + threadIdx.x; i < d.first + (BLOCK - 2) && i < d.hi; i += BLOCK) {
+      const int64_t i = d.first - 1 + threadIdx.x;
+      if (threadIdx.x > 0 && threadIdx.x < BLOCK - 1 && i < d.hi) {
         for (int v = 0; v < 14; ++v) {
-          a.Qh_out[v * n + i] = a.Qh[v * n + i];
-          a.Ql_out[v * n + i] = a.Ql[v * n + i];
+          a.Qh_out[v * n + i] = c.qh[v];
+          a.Ql_out[v * n + i] = c.ql[v];
         }
-        a.lam_out[i] = a.lam[i];
-        for (int v = 0; v < 3; ++v) a.isl_out[v * n + i] = a.isl[v * n + i];
+        a.lam_out[i] = c.li;
+        a.isl_out[i] = c.I0.ir;
+        a.isl_out[n + i] = c.I0.e_int;
+        a.isl_out[2 * n + i] = c.I0.sm1;
       }
       continue;
     }
-    const float m = mixed_tile<BLOCK>(a, em, d.first, d.lo, d.hi, dtdx, flux, bc, S);
-    if (threadIdx.x == 0) atomicMax(&b.slots[wr * P + p], (unsigned long long)__float_as_uint(m));
+    const float l = mixed_tile_run<BLOCK>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
+    const float m = mixed_block_max<BLOCK>(l);
+    if (threadIdx.x == 0) atomicMax(&slots_wr[d.problem], (unsigned long long)__float_as_uint(m));
+    __syncthreads();  // the block-max scratch is reused by the next tile
   }
 }
 
@@ -213,10 +239,9 @@ static_assert(sizeof(kVariants) / sizeof(kVariants[0]) == kNumVariants, "variant
 
 template <int BLOCK, int MINB>
 cudaError_t launch_batch_mixed_t(cudaStream_t s, int grid, const MixedArrays& a, const EosMixed& em,
-                                 const TileDesc* tiles, int ntiles, const BatchDev& b, int par, int rd, int wr,
-                                 int clr, double t_end, double cfl, int flux, int bc, DevState* S) {
-  batch_mixed_kernel<BLOCK, MINB><<<grid, BLOCK, 0, s>>>(a, em, tiles, ntiles, b, par, rd, wr, clr, t_end, cfl, flux,
-                                                         bc, S);
+                                 const TileDesc* tiles, const TileCtl* ctl, int ntiles, unsigned long long* slots_wr,
+                                 int flux, int bc, DevState* S) {
+  batch_mixed_kernel<BLOCK, MINB><<<grid, BLOCK, 0, s>>>(a, em, tiles, ctl, ntiles, slots_wr, flux, bc, S);
   return cudaGetLastError();
 }
 
@@ -241,7 +266,10 @@ struct hyp_batch {
   cudaStream_t stream = nullptr;
   EosC eos;
   EosMixed eos_mixed;
-  // mixed state: per parity one block of 2 x 14 x total floats (also the FP64 staging buffer)
+  // mixed state: one block [2][32][mpitch] floats (hyp_mixed_tile.cuh layout); a parity's
+  // block also stages FP64 uploads and downloads
+  float* mixed_base = nullptr;
+  int64_t mpitch = 0;
   float* Qh[2] = {nullptr, nullptr};
   float* Ql[2] = {nullptr, nullptr};
   float* lamf[2] = {nullptr, nullptr};
@@ -255,6 +283,7 @@ struct hyp_batch {
   DevState* st = nullptr;
   // tile table of the current variant
   TileDesc* tiles = nullptr;
+  TileCtl* ctl = nullptr;  // mixed: per-tile step control
   int ntiles = 0;
   int tile_cells = 0;
   int variant = 1;
@@ -287,8 +316,11 @@ static int build_tiles(hyp_batch* b, int cells_per_tile) {
       t.push_back(TileDesc{f, lo, hi, p, f == lo ? 1 : 0});
   }
   if (b->tiles) cudaFree(b->tiles);
+  if (b->ctl) cudaFree(b->ctl);
   b->tiles = nullptr;
+  b->ctl = nullptr;
   BCK(cudaMalloc(&b->tiles, t.size() * sizeof(TileDesc)));
+  if (b->mixed) BCK(cudaMalloc(&b->ctl, t.size() * sizeof(TileCtl)));
   BCK(cudaMemcpy(b->tiles, t.data(), t.size() * sizeof(TileDesc), cudaMemcpyHostToDevice));
   b->ntiles = (int)t.size();
   b->tile_cells = cells_per_tile;
@@ -330,7 +362,8 @@ static MixedArrays batch_arrays(hyp_batch* b, int p) {
   a.Ql_out = b->Ql[1 - p];
   a.lam_out = b->lamf[1 - p];
   a.isl_out = b->isl[1 - p];
-  a.stride = b->total;
+  a.stride = b->mpitch;
+  a.n = b->total;
   return a;
 }
 
@@ -339,14 +372,17 @@ static int enqueue_batch_step(hyp_batch* b, long long k, double t_end) {
   if (b->mixed) {
     const MixedArrays a = batch_arrays(b, par);
     const int rd = (int)(k % 3), wr = (int)((k + 1) % 3), clr = (int)((k + 2) % 3);
+    batch_mixed_ctl_kernel<<<(b->ntiles + 255) / 256, 256, 0, b->stream>>>(b->tiles, b->ntiles, b->b, par, rd, wr, clr,
+                                                                          t_end, b->cfg.cfl, b->ctl);
+    BCK(cudaGetLastError());
+    unsigned long long* sw = b->b.slots + (size_t)wr * b->P;
+    const int fl = b->cfg.flux, bc = b->cfg.bc;
     cudaError_t e;
     switch (b->variant) {
-      case 0: e = launch_batch_mixed_t<128, 8>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
-      case 1: e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
-      case 4: e = launch_batch_mixed_t<128, 8>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
-      case 5: e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
-      case 2: e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
-      default: e = launch_batch_mixed_t<512, 2>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ntiles, b->b, par, rd, wr, clr, t_end, b->cfg.cfl, b->cfg.flux, b->cfg.bc, b->st); break;
+      case 0: case 4: e = launch_batch_mixed_t<128, 8>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
+      case 1: case 5: e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
+      case 2: e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
+      default: e = launch_batch_mixed_t<512, 2>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
     }
     BCK(e);
   } else {
@@ -367,12 +403,8 @@ static void free_batch(hyp_batch* b) {
   cudaSetDevice(b->device);
   if (b->stream) cudaStreamSynchronize(b->stream);
   if (b->graph) cudaGraphExecDestroy(b->graph);
-  for (int p = 0; p < 2; ++p) {
-    cudaFree(b->Qh[p]);
-    cudaFree(b->lamf[p]);
-    cudaFree(b->isl[p]);
-    cudaFree(b->Q[p]);
-  }
+  for (int p = 0; p < 2; ++p) cudaFree(b->Q[p]);
+  cudaFree(b->mixed_base);
   cudaFree(b->F);
   cudaFree(b->lam);
   cudaFree(b->b.t);
@@ -381,6 +413,7 @@ static void free_batch(hyp_batch* b) {
   cudaFree(b->b.dx);
   cudaFree(b->st);
   cudaFree(b->tiles);
+  cudaFree(b->ctl);
   for (auto& e : b->ev)
     if (e) cudaEventDestroy(e);
   if (b->stream) cudaStreamDestroy(b->stream);
@@ -419,15 +452,17 @@ extern "C" int hyp_batch_create(const hyp_config* cfg, const int64_t* offsets, i
   ck(cudaDeviceGetAttribute(&b->sms, cudaDevAttrMultiProcessorCount, b->device));
   ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   const size_t nq = (size_t)14 * b->total;
-  for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
-    if (b->mixed) {
-      ck(cudaMalloc(&b->Qh[p], nq * sizeof(double)));
-      if (rc == HYP_OK) b->Ql[p] = b->Qh[p] + nq;
-      ck(cudaMalloc(&b->lamf[p], (size_t)b->total * sizeof(float)));
-      ck(cudaMalloc(&b->isl[p], (size_t)3 * b->total * sizeof(float)));
-    } else {
-      ck(cudaMalloc(&b->Q[p], nq * sizeof(double)));
+  if (b->mixed) {
+    b->mpitch = mixed_pitch(b->total);
+    ck(cudaMalloc(&b->mixed_base, (size_t)2 * kMixedRows * b->mpitch * sizeof(float)));
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
+      b->Qh[p] = b->mixed_base + (size_t)p * kMixedRows * b->mpitch;
+      b->Ql[p] = b->Qh[p] + (size_t)14 * b->mpitch;
+      b->lamf[p] = b->Qh[p] + (size_t)28 * b->mpitch;
+      b->isl[p] = b->Qh[p] + (size_t)29 * b->mpitch;
     }
+  } else {
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p) ck(cudaMalloc(&b->Q[p], nq * sizeof(double)));
   }
   if (!b->mixed) {
     ck(cudaMalloc(&b->F, (size_t)kNFlux1 * b->total * sizeof(double)));
@@ -467,7 +502,10 @@ static int batch_check_error(hyp_batch* b) {
   if (!h.err_code) return HYP_OK;
   char buf[128];
   snprintf(buf, sizeof buf, "cell %lld (global index)", (long long)h.err_cell);
-  return berr(b, (h.err_code & HYP_CELL_NEG_DET) ? HYP_ERR_NEG_DET : HYP_ERR_NONFINITE, buf);
+  const int code = (h.err_code & HYP_CELL_TIMEOUT)   ? HYP_ERR_TIMEOUT
+                   : (h.err_code & HYP_CELL_NEG_DET) ? HYP_ERR_NEG_DET
+                                                     : HYP_ERR_NONFINITE;
+  return berr(b, code, buf);
 }
 
 extern "C" int hyp_batch_upload(hyp_batch* b, const double* Q, double t0) {
@@ -482,7 +520,7 @@ extern "C" int hyp_batch_upload(hyp_batch* b, const double* Q, double t0) {
   if (b->mixed) {
     double* stage = (double*)b->Qh[1];
     BCK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, b->stream));
-    BCK(launch_split_n(b->stream, stage, b->Qh[0], b->Ql[0], (int64_t)14 * b->total));
+    BCK(launch_split_n(b->stream, stage, b->Qh[0], b->Ql[0], b->total, b->mpitch));
     MixedArrays a = batch_arrays(b, 0);
     a.lam_out = b->lamf[0];
     a.isl_out = b->isl[0];
@@ -503,7 +541,7 @@ extern "C" int hyp_batch_download(hyp_batch* b, double* Q) {
   const size_t bytes = (size_t)14 * b->total * sizeof(double);
   if (b->mixed) {
     double* stage = (double*)b->Qh[1 - b->cur];
-    BCK(launch_join_n(b->stream, b->Qh[b->cur], b->Ql[b->cur], stage, (int64_t)14 * b->total));
+    BCK(launch_join_n(b->stream, b->Qh[b->cur], b->Ql[b->cur], stage, b->total, b->mpitch));
     BCK(cudaMemcpyAsync(Q, stage, bytes, cudaMemcpyDeviceToHost, b->stream));
   } else {
     BCK(cudaMemcpyAsync(Q, b->Q[b->cur], bytes, cudaMemcpyDeviceToHost, b->stream));
@@ -588,20 +626,18 @@ extern "C" int hyp_batch_autotune(hyp_batch* b, int trial_steps, int* chosen, do
   // control in one device buffer; every trial starts from it
   const int p0 = b->cur;
   const long long k0 = b->k;
-  const size_t bq = (size_t)28 * b->total * sizeof(float), bl = (size_t)b->total * sizeof(float),
-               bi = (size_t)3 * b->total * sizeof(float), bt = (size_t)2 * b->P * sizeof(double),
+  // the parity block holds hi, lo, lambda and islands
+  const size_t bq = (size_t)kMixedRows * b->mpitch * sizeof(float), bt = (size_t)2 * b->P * sizeof(double),
                bs = (size_t)3 * b->P * sizeof(unsigned long long), bk = (size_t)b->P * sizeof(long long);
   char* save = nullptr;
-  BCK(cudaMalloc(&save, bq + bl + bi + bt + bs + bk));
+  BCK(cudaMalloc(&save, bq + bt + bs + bk));
   struct Seg {
     void* dev;
     size_t off, bytes;
   } segs[] = {{b->Qh[p0], 0, bq},
-              {b->lamf[p0], bq, bl},
-              {b->isl[p0], bq + bl, bi},
-              {b->b.t, bq + bl + bi, bt},
-              {b->b.slots, bq + bl + bi + bt, bs},
-              {b->b.steps, bq + bl + bi + bt + bs, bk}};
+              {b->b.t, bq, bt},
+              {b->b.slots, bq + bt, bs},
+              {b->b.steps, bq + bt + bs, bk}};
   // The copies go on the batch's own (non-blocking) stream: a device-to-device
   // cudaMemcpy would run on the legacy stream, which that stream does not wait for.
   for (auto& s : segs)

@@ -41,12 +41,8 @@ static int free_ctx(hyp_ctx* c) {
   free_tape(c);
   for (auto& g : c->graph)
     if (g) cudaGraphExecDestroy(g);
-  for (int p = 0; p < 2; ++p) {
-    cudaFree(c->Q[p]);
-    cudaFree(c->Qh[p]);  // the (hi, lo) block
-    cudaFree(c->lamf[p]);
-    cudaFree(c->isl[p]);
-  }
+  for (int p = 0; p < 2; ++p) cudaFree(c->Q[p]);
+  cudaFree(c->mixed_base);
   cudaFree(c->F);
   cudaFree(c->lam);
   cudaFree(c->smin);
@@ -118,16 +114,18 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
     if (rc == HYP_OK && (e = cudaMalloc(&c->lam, (size_t)c->n * sizeof(double))) != cudaSuccess)
       fail(e, "cudaMalloc(lam)");
   } else {
+    // one block [2][32][pitch] floats: per parity 14 hi rows, 14 lo rows, lambda, 3 island rows
+    // (hyp_mixed_tile.cuh); a parity's block also stages FP64 uploads and downloads (16 pitch >= 14 n doubles)
+    c->mpitch = mixed_pitch(c->n);
+    if ((e = cudaMalloc(&c->mixed_base, (size_t)2 * kMixedRows * c->mpitch * sizeof(float))) != cudaSuccess)
+      fail(e, "cudaMalloc(mixed state)");
     for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
-      if ((e = cudaMalloc(&c->Qh[p], nq)) != cudaSuccess) {  // 2 x 14 x n floats = 14 x n doubles
-        fail(e, "cudaMalloc(Q hi/lo)");
-        break;
-      }
-      c->Ql[p] = c->Qh[p] + (size_t)c->nvar * c->n;
-      if ((e = cudaMalloc(&c->lamf[p], (size_t)c->n * sizeof(float))) != cudaSuccess) fail(e, "cudaMalloc(lambda)");
-      if (rc == HYP_OK && (e = cudaMalloc(&c->isl[p], (size_t)3 * c->n * sizeof(float))) != cudaSuccess)
-        fail(e, "cudaMalloc(islands)");
+      c->Qh[p] = c->mixed_base + (size_t)p * kMixedRows * c->mpitch;
+      c->Ql[p] = c->Qh[p] + (size_t)14 * c->mpitch;
+      c->lamf[p] = c->Qh[p] + (size_t)28 * c->mpitch;
+      c->isl[p] = c->Qh[p] + (size_t)29 * c->mpitch;
     }
+    if (rc == HYP_OK && setup_mixed_tma(c) != 0) c->tma_grid = 0;  // TMA kernel unavailable
   }
   if (rc == HYP_OK && (e = cudaMalloc(&c->st, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMalloc(state)");
   if (rc == HYP_OK && (e = cudaMallocHost(&c->st_host, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMallocHost");
@@ -164,6 +162,10 @@ static int check_cell_error(hyp_ctx* c) {
   if (!code) return HYP_OK;
   c->err_cell = c->st_host->err_cell;
   char buf[160];
+  if (code & HYP_CELL_TIMEOUT) {
+    snprintf(buf, sizeof buf, "a device wait for a tile load timed out (tile starting at cell %lld)", (long long)c->err_cell);
+    return set_err(c, HYP_ERR_TIMEOUT, buf);
+  }
   if (code & HYP_CELL_NEG_DET) {
     snprintf(buf, sizeof buf, "det(rho A) <= 0 in cell %lld (reference: DomainError in sqrt)", (long long)c->err_cell);
     return set_err(c, HYP_ERR_NEG_DET, buf);
@@ -361,6 +363,21 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
   if (steps_done) *steps_done = (int)active;
   if (t_out) *t_out = c->t_host;
   return check_cell_error(c);
+}
+
+extern "C" int hyp_set_mixed_kernel(hyp_ctx* c, int tma) {
+  if (!c) return HYP_ERR_INVALID;
+  if (!mixed(c) || c->cfg.model != HYP_MODEL_SINGLE)
+    return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: single-phase mixed-precision contexts only");
+  if (tma && !c->tma_grid) return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: TMA is not available");
+  c->mixed_tma = tma ? 1 : 0;
+  for (auto& g : c->graph)  // graphs hold the previous kernel
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  c->graph_steps = 0;
+  return HYP_OK;
 }
 
 extern "C" int hyp_max_wavespeed(hyp_ctx* c, double* out) {

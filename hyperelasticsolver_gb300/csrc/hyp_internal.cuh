@@ -9,6 +9,7 @@
 #include "hyp_physics.cuh"
 #include "hyp_physics_mixed.cuh"
 #include "hyp_physics_mph.cuh"
+#include "hyp_tma.cuh"
 
 namespace hyp {
 
@@ -55,6 +56,12 @@ struct StepTiming {
 
 namespace hyp {
 struct AdjTape;
+// Mixed-precision state of one parity: kMixedRows rows of a pitch of floats,
+// rows 0-13 hi parts, 14-27 lo parts, 28 the cell's wave speed, 29-31 its
+// island outputs. The two parities are consecutive blocks of one allocation, so
+// the whole state is one 2D array [2 x 32][pitch] that a TMA tensor map can box.
+constexpr int kMixedRows = 32;
+__host__ __device__ __forceinline__ int64_t mixed_pitch(int64_t n) { return (n + 3) & ~int64_t(3); }
 }
 
 struct hyp_ctx {
@@ -74,6 +81,11 @@ struct hyp_ctx {
   float* Ql[2] = {nullptr, nullptr};
   float* lamf[2] = {nullptr, nullptr};
   float* isl[2] = {nullptr, nullptr};  // cached float-float island outputs [3][n] (1/rho, e_int, rho/rho0 - 1)
+  float* mixed_base = nullptr;          // one allocation [2 parities][32 rows][mpitch] holding all of the above
+  int64_t mpitch = 0;                   // row pitch (floats, a multiple of 4)
+  CUtensorMap tmap;                     // TMA map over mixed_base (both parities)
+  int mixed_tma = 0;                    // step with the TMA-prefetched persistent kernel
+  int tma_grid = 0;
   hyp::EosMixed eos_mixed;
   // two-phase (FP64): cell fluxes F [30][n], wave-speed bounds, face fluctuations [30][n+1]
   hyp::Eos2 eos2;
@@ -130,6 +142,9 @@ cudaError_t launch_cell1_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, co
 cudaError_t launch_update1_f64(hyp_ctx* c, int p, double t_end);
 // single-phase mixed-precision launchers (hyp_step1_mixed.cu)
 cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo);
+cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int64_t n, int64_t pitch);
+cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int64_t n, int64_t pitch);
+int setup_mixed_tma(hyp_ctx* c);
 cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q);
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot);
 cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end);

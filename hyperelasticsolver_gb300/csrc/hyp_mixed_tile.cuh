@@ -11,7 +11,7 @@
 //      (NumFluxes.jl:25-33; main.jl:45-48), lambda_face = max(lambda_L, lambda_R);
 //   3. Q += -dt/dx (F_{i+1/2} - F_{i-1/2}) accumulated into (hi, lo) (main.jl:43-60);
 //   4. islands, cons2prim and wave speed of the NEW state, stored per cell.
-// Returns the block max of the new wave speeds (valid in thread 0).
+// Returns the thread's new wave speed; the caller reduces the block max.
 #pragma once
 #include "hyp_internal.cuh"
 
@@ -26,7 +26,48 @@ struct MixedArrays {
   float* Ql_out;
   float* lam_out;
   float* isl_out;
-  int64_t stride;   // cells per variable row
+  int64_t stride;   // floats between rows (a multiple of 4)
+  int64_t n;        // cells
+};
+
+// One cell's inputs to a tile.
+struct MixedCellIn {
+  float qh[14], ql[14];
+  float li;
+  Islands I0;
+};
+
+// Loads the cell's inputs straight from the state arrays and keeps the hi parts
+// the face phase reads in shared memory.
+// Loader interface used by mixed_tile: operator()(j, ic, c) fills cell ic's
+// inputs for local index j; keep(j, c) stores what face_q needs; face_q(v, j, ic)
+// returns the hi part of variable v of local cell j (cell ic); release() runs
+// once the face phase has read its inputs.
+template <int BLOCK>
+struct MixedGlobalLoader {
+  const MixedArrays& a;
+  __device__ __forceinline__ static float (&sQ())[14][BLOCK] {
+    __shared__ float q[14][BLOCK];
+    return q;
+  }
+  __device__ __forceinline__ void operator()(int, int64_t ic, MixedCellIn& c) const {
+    const int64_t n = a.stride;
+#pragma unroll
+    for (int v = 0; v < 14; ++v) {
+      c.qh[v] = a.Qh[v * n + ic];
+      c.ql[v] = a.Ql[v * n + ic];
+    }
+    c.li = a.lam[ic];
+    c.I0.ir = a.isl[ic];
+    c.I0.e_int = a.isl[n + ic];
+    c.I0.sm1 = a.isl[2 * n + ic];
+  }
+  __device__ __forceinline__ void keep(int j, const MixedCellIn& c) const {
+#pragma unroll
+    for (int v = 0; v < 14; ++v) sQ()[v][j] = c.qh[v];
+  }
+  __device__ __forceinline__ float face_q(int v, int j, int64_t) const { return sQ()[v][j]; }
+  __device__ __forceinline__ void release() const {}
 };
 
 __device__ __forceinline__ void mixed_record_err(DevState* S, int code, long long cell) {
@@ -48,87 +89,104 @@ __device__ __forceinline__ float mixed_block_max(float v) {
 }
 
 // first: first owned cell (global index); [lo, hi): the problem's cells.
-template <int BLOCK>
-__device__ __forceinline__ float mixed_tile(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
-                                            int64_t hi, float dtdx, int flux, int bc, DevState* S) {
-  __shared__ float sF[kNFlux1][BLOCK];
-  __shared__ float sQ[14][BLOCK];
-  __shared__ float sFace[14][BLOCK];
+// mixed_tile_load fills this thread's cell inputs; kernels call it before they
+// read the step's control data (time, max lambda), so that the cell loads do not
+// wait behind those. mixed_tile_run then takes the step and returns this
+// thread's new wave speed (0 if it owns no cell).
+__device__ __forceinline__ int64_t tile_cell(int64_t first, int64_t lo, int64_t hi) {
+  const int64_t i = first - 1 + threadIdx.x;     // cell of this thread (halo at j = 0, BLOCK - 1)
+  return i < lo ? lo : (i >= hi ? hi - 1 : i);  // ghost cells copy the end cells
+}
+template <class Loader>
+__device__ __forceinline__ void mixed_tile_load(int64_t first, int64_t lo, int64_t hi, const Loader& load,
+                                                MixedCellIn& c) {
+  load((int)threadIdx.x, tile_cell(first, lo, hi), c);
+}
+template <int BLOCK, class Loader>
+__device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
+                                                int64_t hi, float dtdx, int flux, int bc, DevState* S,
+                                                const Loader& load, MixedCellIn& c) {
+  __shared__ float sFF[14][BLOCK];  // cell fluxes (11 slots), then the face fluxes (14)
   __shared__ float sL[BLOCK];
   const int64_t n = a.stride;
   const int j = threadIdx.x;
-  const int64_t i = first - 1 + j;                         // cell of this thread (halo at j = 0, BLOCK - 1)
-  const int64_t ic = i < lo ? lo : (i >= hi ? hi - 1 : i);  // ghost cells copy the end cells
-  float qh[14], ql[14];
-#pragma unroll
-  for (int v = 0; v < 14; ++v) {
-    qh[v] = a.Qh[v * n + ic];
-    ql[v] = a.Ql[v * n + ic];
-  }
-  const float li = a.lam[ic];
-  Islands I0;  // this state's island outputs, cached by the step that produced it
-  I0.ir = a.isl[ic];
-  I0.e_int = a.isl[n + ic];
-  I0.sm1 = a.isl[2 * n + ic];
+  const int64_t i = first - 1 + j;
+  const int64_t ic = tile_cell(first, lo, hi);
   {
     PrimM P;
-    int st = prim_from_islands(em, qh, ql, I0, P);
-    StressCT<float> c = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
+    int st = prim_from_islands(em, c.qh, c.ql, c.I0, P);
+    StressCT<float> sc = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
     float f11[kNFlux1];
-    flux_mixed(em, qh, P, c, f11);
+    flux_mixed(em, c.qh, P, sc, f11);
 #pragma unroll
-    for (int s = 0; s < kNFlux1; ++s) sF[s][j] = f11[s];
-#pragma unroll
-    for (int v = 0; v < 14; ++v) sQ[v][j] = qh[v];
-    sL[j] = li;
+    for (int s = 0; s < kNFlux1; ++s) sFF[s][j] = f11[s];
+    load.keep(j, c);
+    sL[j] = c.li;
     if (st && i == ic && j > 0 && j < BLOCK - 1) mixed_record_err(S, st, i);
   }
   __syncthreads();
   // face j + 1/2 between local cells j and j + 1
+  float fv[14];
   if (j < BLOCK - 1) {
     const float lf = flux == HYP_FLUX_LXF ? 1.0f / dtdx : fmaxf(sL[j], sL[j + 1]);
     const float hl = 0.5f * lf;
+    const int64_t i1 = i + 1, ic1 = i1 < lo ? lo : (i1 >= hi ? hi - 1 : i1);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
       const int s = flux_slot1(v);
-      const float fl = s >= 0 ? sF[s][j] : 0.0f, fr = s >= 0 ? sF[s][j + 1] : 0.0f;
-      sFace[v][j] = 0.5f * (fl + fr) - hl * (sQ[v][j + 1] - sQ[v][j]);
+      const float fl = s >= 0 ? sFF[s][j] : 0.0f, fr = s >= 0 ? sFF[s][j + 1] : 0.0f;
+      fv[v] = 0.5f * (fl + fr) - hl * (load.face_q(v, j + 1, ic1) - load.face_q(v, j, ic));
     }
+  }
+  __syncthreads();
+  load.release();
+  if (j < BLOCK - 1) {
+#pragma unroll
+    for (int v = 0; v < 14; ++v) sFF[v][j] = fv[v];
   }
   __syncthreads();
   float lnew = 0.0f;
   const bool own = j > 0 && j < BLOCK - 1 && i < hi;
   if (own) {
     const bool frozen = bc == HYP_BC_FROZEN && (i == lo || i == hi - 1);
-    Islands I = I0;
+    Islands I = c.I0;
     if (frozen) {
-      lnew = li;
+      lnew = c.li;
     } else {
 #pragma unroll
       for (int v = 0; v < 14; ++v) {
-        const float delta = -dtdx * (sFace[v][j] - sFace[v][j - 1]);
-        ff q = ff_add_f(ff{qh[v], ql[v]}, delta);
-        qh[v] = q.hi;
-        ql[v] = q.lo;
+        const float delta = -dtdx * (sFF[v][j] - sFF[v][j - 1]);
+        ff q = ff_add_f(ff{c.qh[v], c.ql[v]}, delta);
+        c.qh[v] = q.hi;
+        c.ql[v] = q.lo;
       }
       PrimM P;
-      int st = prim_mixed(em, qh, ql, P, I);
-      StressCT<float> c = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
-      lnew = lambda_mixed(em, P, c);
+      int st = prim_mixed(em, c.qh, c.ql, P, I);
+      StressCT<float> sc = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
+      lnew = lambda_mixed(em, P, sc);
       if (!(lnew <= 3.0e38f)) st |= HYP_CELL_NONFINITE;
       if (st) mixed_record_err(S, st, i);
     }
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
-      a.Qh_out[v * n + i] = qh[v];
-      a.Ql_out[v * n + i] = ql[v];
+      a.Qh_out[v * n + i] = c.qh[v];
+      a.Ql_out[v * n + i] = c.ql[v];
     }
     a.lam_out[i] = lnew;
     a.isl_out[i] = I.ir;
     a.isl_out[n + i] = I.e_int;
     a.isl_out[2 * n + i] = I.sm1;
   }
-  return mixed_block_max<BLOCK>(own ? lnew : 0.0f);
+  __syncthreads();  // the shared arrays are reused by the block's next tile
+  return lnew;
+}
+template <int BLOCK, class Loader>
+__device__ __forceinline__ float mixed_tile(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
+                                            int64_t hi, float dtdx, int flux, int bc, DevState* S,
+                                            const Loader& load) {
+  MixedCellIn c;
+  mixed_tile_load(first, lo, hi, load, c);
+  return mixed_tile_run<BLOCK>(a, em, first, lo, hi, dtdx, flux, bc, S, load, c);
 }
 
 // Wave speed and island outputs of one cell of a freshly uploaded state.

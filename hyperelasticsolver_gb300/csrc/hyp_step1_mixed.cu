@@ -2,17 +2,25 @@
 // wave speeds, a compensated (hi, lo) FP32 state, float-float islands in
 // cons2prim (hyp_physics_mixed.cuh).
 //
-// One fused kernel per step; each block runs one tile of hyp_mixed_tile.cuh
-// (kBlock - 2 owned cells plus a halo cell each side): flux phase, Rusanov
-// faces, compensated update, then the wave speed of the NEW state, stored per
-// cell and max-reduced (warp shuffles, one shared-memory pass, one atomicMax
-// per block) for the next step's dt = cfl dx / max lambda (main.jl:204-212).
+// One fused kernel per step; each tile of hyp_mixed_tile.cuh (block - 2 owned
+// cells plus a halo cell each side) runs the flux phase, the Rusanov faces, the
+// compensated update, then the wave speed of the NEW state, stored per cell and
+// max-reduced (warp shuffles, one shared-memory pass, one atomicMax per block)
+// for the next step's dt = cfl dx / max lambda (main.jl:204-212).
 // HBM traffic per cell-update: the state read and written (14 x 2 x 4 B each
 // way) plus, each way, the cell's FP32 lambda and the three outputs of its
 // float-float islands (1/rho, e_int, rho/rho0 - 1), so that the flux phase needs
 // no float-float work: 256 B, against 224 B for the state alone.
 // The three max-lambda slots rotate (read k%3, write (k+1)%3, clear (k+2)%3)
 // so one launch per step needs no separate reset.
+//
+// Two kernels run the same tile body:
+//   step1_mixed_kernel      one block per tile, each thread loading its cell;
+//   step1_mixed_tma_kernel  a persistent grid; thread 0 of a block prefetches
+//                           the block's next tile (all 32 rows of its cells) with
+//                           2D TMA boxes into shared memory while the block
+//                           computes the current tile from its copy, so loads
+//                           overlap compute.
 #include "hyp_internal.cuh"
 #include "hyp_mixed_tile.cuh"
 
@@ -25,13 +33,14 @@ struct MixedSlots {
   int rd, wr, clr;    // max-lambda slots: read (this step), write (next step), clear
 };
 
-__global__ void __launch_bounds__(kBlock, 4)
-    step1_mixed_kernel(MixedArrays a, EosMixed em, MixedSlots sl, DevState* S, double t_end, double cfl, double dx,
-                       int flux, int bc) {
+// t, the step count and the max-lambda slots (block 0, thread 0); returns
+// whether the step is active and dt/dx.
+__device__ __forceinline__ bool mixed_step_prologue(const MixedSlots& sl, DevState* S, double t_end, double cfl,
+                                                    double dx, float& dtdx) {
   const double tn = S->t[sl.p];
   const bool active = tn < t_end;
   const float lmax = __uint_as_float((unsigned)S->lam_slots[sl.rd]);
-  const float dtdx = (float)cfl / lmax;  // dt/dx = cfl / max lambda
+  dtdx = (float)cfl / lmax;  // dt/dx = cfl / max lambda
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const double dt = (cfl * dx) / (double)lmax;
     S->t[1 - sl.p] = active ? tn + dt : tn;
@@ -40,33 +49,152 @@ __global__ void __launch_bounds__(kBlock, 4)
       S->steps += 1;
     }
   }
-  if (!active) return;
-  const float m = mixed_tile<kBlock>(a, em, (int64_t)blockIdx.x * kTileM, 0, a.stride, dtdx, flux, bc, S);
+  return active;
+}
+
+__global__ void __launch_bounds__(kBlock, 4)
+    step1_mixed_kernel(MixedArrays a, EosMixed em, MixedSlots sl, DevState* S, double t_end, double cfl, double dx,
+                       int flux, int bc) {
+  const int64_t first = (int64_t)blockIdx.x * kTileM;
+  const MixedGlobalLoader<kBlock> ld{a};
+  MixedCellIn c;
+  mixed_tile_load(first, 0, a.n, ld, c);  // issued before the control reads below
+  float dtdx;
+  if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
+  const float l = mixed_tile_run<kBlock>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld, c);
+  const float m = mixed_block_max<kBlock>(l);
   if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
 }
+
+// ---- TMA-prefetched persistent kernel ----------------------------------------
+
+constexpr int kBoxW = 132;  // box width: 128 cells + 4 so that a box starting at the
+                            // 16-byte boundary below the tile's first cell covers it
+template <int BLOCK>
+struct TmaTile {
+  // boxes at 128-column steps; a tile needs BLOCK + 3 columns: 128 (kBoxes - 1) + kBoxW >= BLOCK + 3
+  static constexpr int kBoxes = (BLOCK - 2) / 128 + 1;
+  static_assert(128 * (kBoxes - 1) + kBoxW >= BLOCK + 3, "boxes cover the tile");
+  static constexpr int kStageFloats = kBoxes * kMixedRows * kBoxW;
+  static constexpr unsigned kBytes = kStageFloats * 4u;  // bytes one tile load delivers
+  static constexpr unsigned kSmem = kBytes + 128u;        // dynamic shared memory (alignment slack)
+};
+
+// Loads a cell's inputs from the staged tile: column c of the stage holds cell
+// x0 + c. The face phase reads neighbours' hi parts from the stage as well, so
+// the next tile is prefetched (release) once the faces are computed.
+template <int BLOCK>
+struct MixedStageLoader {
+  const float* stage;  // [kBoxes][32][kBoxW]
+  int64_t x0;          // first staged cell
+  uint64_t* bar;
+  const CUtensorMap* map;
+  int64_t next_x0;     // the block's next tile (< -4: none)
+  int row0;            // first row of the state's parity in the tensor
+  __device__ __forceinline__ const float* column(int64_t ic) const {
+    const int col = (int)(ic - x0);
+    const int b = min(col >> 7, TmaTile<BLOCK>::kBoxes - 1);
+    return stage + b * (kMixedRows * kBoxW) + (col - 128 * b);
+  }
+  __device__ __forceinline__ void operator()(int, int64_t ic, MixedCellIn& c) const {
+    const float* s = column(ic);
+#pragma unroll
+    for (int v = 0; v < 14; ++v) {
+      c.qh[v] = s[v * kBoxW];
+      c.ql[v] = s[(14 + v) * kBoxW];
+    }
+    c.li = s[28 * kBoxW];
+    c.I0.ir = s[29 * kBoxW];
+    c.I0.e_int = s[30 * kBoxW];
+    c.I0.sm1 = s[31 * kBoxW];
+  }
+  __device__ __forceinline__ void keep(int, const MixedCellIn&) const {}
+  __device__ __forceinline__ float face_q(int v, int, int64_t ic) const { return column(ic)[v * kBoxW]; }
+  // called after a barrier that follows the block's last read of the stage
+  __device__ __forceinline__ void release() const {
+    if (threadIdx.x == 0 && next_x0 >= -4) {
+      fence_proxy_async_smem();
+      mbar_arrive_expect_tx(bar, TmaTile<BLOCK>::kBytes);
+      for (int b = 0; b < TmaTile<BLOCK>::kBoxes; ++b)
+        tma_load_2d(const_cast<float*>(stage) + b * (kMixedRows * kBoxW), map, bar, (int)(next_x0 + 128 * b), row0);
+    }
+  }
+};
+
+// x of the first staged cell of a tile whose first owned cell is `first`: the
+// halo cell first - 1 rounded down to a multiple of 4 (the TMA x alignment).
+__device__ __forceinline__ int64_t stage_x0(int64_t first) { return (first - 1) & ~int64_t(3); }
+
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
+    step1_mixed_tma_kernel(const __grid_constant__ CUtensorMap map, MixedArrays a, EosMixed em, MixedSlots sl,
+                           DevState* S, double t_end, double cfl, double dx, int flux, int bc, int ntiles) {
+  extern __shared__ __align__(128) float stage_raw[];
+  __shared__ __align__(8) uint64_t bar;
+  float dtdx;
+  if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
+  // TMA destinations must be 128-byte aligned in shared memory (the launch adds 128 bytes of slack)
+  float* stage = stage_raw + ((128u - (smem_addr(stage_raw) & 127u)) & 127u) / 4u;
+  constexpr int64_t kT = BLOCK - 2;
+  const int row0 = kMixedRows * sl.p;
+  int tile = blockIdx.x;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    if (tile < ntiles) {
+      mbar_arrive_expect_tx(&bar, TmaTile<BLOCK>::kBytes);
+      const int64_t x0 = stage_x0(tile * kT);
+      for (int b = 0; b < TmaTile<BLOCK>::kBoxes; ++b)
+        tma_load_2d(stage + b * (kMixedRows * kBoxW), &map, &bar, (int)(x0 + 128 * b), row0);
+    }
+  }
+  __syncthreads();
+  unsigned phase = 0;
+  float m = 0.0f;
+  for (; tile < ntiles; tile += gridDim.x) {
+    const bool ok = mbar_wait_bounded(&bar, phase);
+    if (__syncthreads_or(!ok)) {
+      if (threadIdx.x == 0) mixed_record_err(S, HYP_CELL_TIMEOUT, tile * kT);
+      return;
+    }
+    phase ^= 1u;
+    const int64_t first = tile * kT;
+    const int next = tile + gridDim.x;
+    MixedStageLoader<BLOCK> ld{stage, stage_x0(first), &bar, &map, next < ntiles ? stage_x0(next * kT) : -8, row0};
+    m = fmaxf(m, mixed_tile<BLOCK>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld));
+  }
+  m = mixed_block_max<BLOCK>(m);
+  if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
+}
+
+constexpr int kTmaBlock = 256, kTmaMinB = 3;
 
 // lambda of every cell of the state (after an upload) and its max into a slot.
 __global__ void __launch_bounds__(kBlock) lam1_mixed_kernel(MixedArrays a, EosMixed em, unsigned long long* slot,
                                                             DevState* S) {
   const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
   float l = 0.0f;
-  if (i < a.stride) l = mixed_cell_lambda(a, em, i, S, a.lam_out, a.isl_out);
+  if (i < a.n) l = mixed_cell_lambda(a, em, i, S, a.lam_out, a.isl_out);
   const float m = mixed_block_max<kBlock>(l);
   if (threadIdx.x == 0) atomicMax(slot, (unsigned long long)__float_as_uint(m));
 }
 
-// FP64 -> (hi, lo) and back.
-__global__ void split_kernel(const double* __restrict__ q, float* __restrict__ hi, float* __restrict__ lo, int64_t m) {
+// FP64 [14][n] -> (hi, lo) rows of pitch `pitch`, and back.
+__global__ void split_kernel(const double* __restrict__ q, float* __restrict__ hi, float* __restrict__ lo, int64_t n,
+                             int64_t pitch, int64_t m) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
     const double x = q[k];
     const float h = (float)x;
-    hi[k] = h;
-    lo[k] = (float)(x - (double)h);
+    const int64_t d = (k / n) * pitch + k % n;
+    hi[d] = h;
+    lo[d] = (float)(x - (double)h);
   }
 }
-__global__ void join_kernel(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ q, int64_t m) {
-  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x)
-    q[k] = (double)hi[k] + (double)lo[k];
+__global__ void join_kernel(const float* __restrict__ hi, const float* __restrict__ lo, double* __restrict__ q,
+                            int64_t n, int64_t pitch, int64_t m) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t d = (k / n) * pitch + k % n;
+    q[k] = (double)hi[d] + (double)lo[d];
+  }
 }
 
 unsigned elementwise_grid(int64_t m) {
@@ -74,19 +202,19 @@ unsigned elementwise_grid(int64_t m) {
   return (unsigned)(g > 152 * 64 ? 152 * 64 : (g < 1 ? 1 : g));
 }
 
-cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int64_t m) {
-  split_kernel<<<elementwise_grid(m), kBlock, 0, s>>>(q, hi, lo, m);
+cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int64_t n, int64_t pitch) {
+  split_kernel<<<elementwise_grid(14 * n), kBlock, 0, s>>>(q, hi, lo, n, pitch, 14 * n);
   return cudaGetLastError();
 }
-cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int64_t m) {
-  join_kernel<<<elementwise_grid(m), kBlock, 0, s>>>(hi, lo, q, m);
+cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int64_t n, int64_t pitch) {
+  join_kernel<<<elementwise_grid(14 * n), kBlock, 0, s>>>(hi, lo, q, n, pitch, 14 * n);
   return cudaGetLastError();
 }
 cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo) {
-  return launch_split_n(c->stream, q, hi, lo, (int64_t)14 * c->n);
+  return launch_split_n(c->stream, q, hi, lo, c->n, c->mpitch);
 }
 cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q) {
-  return launch_join_n(c->stream, hi, lo, q, (int64_t)14 * c->n);
+  return launch_join_n(c->stream, hi, lo, q, c->n, c->mpitch);
 }
 
 static MixedArrays arrays_of(hyp_ctx* c, int p) {
@@ -99,7 +227,8 @@ static MixedArrays arrays_of(hyp_ctx* c, int p) {
   a.Ql_out = c->Ql[1 - p];
   a.lam_out = c->lamf[1 - p];
   a.isl_out = c->isl[1 - p];
-  a.stride = c->n;
+  a.stride = c->mpitch;
+  a.n = c->n;
   return a;
 }
 
@@ -111,6 +240,26 @@ cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot) {
   lam1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(a, c->eos_mixed, slot, c->st);
   return cudaGetLastError();
 }
+
+// Prepares the TMA kernel for a context: tensor map over both parities, grid.
+// The one-block-per-tile kernel stays the default: on GB300 it measured faster
+// (0.89 vs 0.96 ms per step at 2^24 cells), the TMA body needing more registers
+// than 4 resident blocks per SM allow.
+int setup_mixed_tma(hyp_ctx* c) {
+  if (encode_tmap_2d_f32(&c->tmap, c->mixed_base, c->mpitch, 2 * kMixedRows, kBoxW, kMixedRows) != 0) return 1;
+  auto kern = step1_mixed_tma_kernel<kTmaBlock, kTmaMinB>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TmaTile<kTmaBlock>::kSmem) !=
+      cudaSuccess)
+    return 1;
+  int nb = 0, sms = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kTmaBlock, TmaTile<kTmaBlock>::kSmem) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nb < 1)
+    return 1;
+  const int64_t ntiles = (c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2);
+  c->tma_grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * nb);
+  return 0;
+}
+
 cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   const int p = (int)(k & 1);
   MixedSlots sl;
@@ -118,11 +267,39 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   sl.rd = (int)(k % 3);
   sl.wr = (int)((k + 1) % 3);
   sl.clr = (int)((k + 2) % 3);
-  const unsigned grid = (unsigned)((c->n + kTileM - 1) / kTileM);
   const double dx = c->cfg.x_length / (double)c->n;
-  step1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx,
-                                                     c->cfg.flux, c->cfg.bc);
+  if (c->mixed_tma) {
+    const int ntiles = (int)((c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2));
+    step1_mixed_tma_kernel<kTmaBlock, kTmaMinB><<<c->tma_grid, kTmaBlock, TmaTile<kTmaBlock>::kSmem, c->stream>>>(
+        c->tmap, arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc, ntiles);
+  } else {
+    const unsigned grid = (unsigned)((c->n + kTileM - 1) / kTileM);
+    step1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl,
+                                                       dx, c->cfg.flux, c->cfg.bc);
+  }
   return cudaGetLastError();
 }
 
 }  // namespace hyp
+
+// ---- host: tensor-map encoding through the driver entry point ------------------
+int hyp::encode_tmap_2d_f32(CUtensorMap* map, const float* base, int64_t pitch, int64_t rows, int box_w, int box_h) {
+  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
+  if (!encode) {
+    void* fn = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+        q != cudaDriverEntryPointSuccess || !fn)
+      return 1;
+    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
+  }
+  if (pitch % 4 != 0 || box_w % 4 != 0 || box_w > 256 || box_h > 256) return 1;
+  cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
+  cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
+                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? 0 : 1;
+}

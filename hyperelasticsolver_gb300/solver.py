@@ -77,6 +77,12 @@ class Solver:
         L.check(L.load().hyp_get_time(self._h, ctypes.byref(t), ctypes.byref(s)), self._h, "hyp_get_time")
         return t.value, s.value
 
+    def set_mixed_kernel(self, kernel):
+        """Mixed precision: "tma" (persistent, TMA-prefetched tiles) or "tile" (one block per tile)."""
+        if kernel not in ("tma", "tile"):
+            raise ValueError("kernel must be 'tma' or 'tile'")
+        L.check(L.load().hyp_set_mixed_kernel(self._h, int(kernel == "tma")), self._h, "hyp_set_mixed_kernel")
+
     def set_profiling(self, on):
         L.check(L.load().hyp_set_profiling(self._h, int(bool(on))), self._h, "hyp_set_profiling")
 

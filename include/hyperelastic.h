@@ -124,6 +124,11 @@ int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel
 int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_Q_out, int64_t n_cells, int n_steps,
                          double t0, void* stream, double* t_out, int64_t* err_cell);
 
+/* Single-phase mixed precision: step with the persistent kernel whose tiles are
+   prefetched by TMA (tma = 1) or with one block per tile loading its own cells
+   (tma = 0, the default, faster on GB300). Both run the same tile arithmetic. */
+int hyp_set_mixed_kernel(hyp_ctx* ctx, int tma);
+
 /* ---- batches of independent single-phase problems -------------------------- */
 /* The reference advances one problem per main.jl run (main.jl:202-241). A batch
    advances n_problems independent problems of uneven size in lockstep, each with
