@@ -22,16 +22,18 @@ def hll(eos, Q_l, Q_r, eigvals=None):
 def lxf(eos, Q_l, Q_r, lam):
     """Lax-Friedrichs / Rusanov face flux (NumFluxes.jl:25-60).
 
-    Returns (cons, D-, D+): cons = 0.5 (f(Q_l) + f(Q_r)) - 0.5 lam (Q_r - Q_l); the
-    path-conservative parts are zero for one phase. `eos` a Barton2009 selects the
-    single-phase model (14 values)."""
-    if isinstance(eos, (tuple, list)):
-        raise NotImplementedError("two-phase lxf is evaluated inside the solver step")
-    cfg = M.config(eos, L.HYP_MODEL_SINGLE)
-    l, n, single = L.soa(Q_l, 14)
-    r, _, _ = L.soa(Q_r, 14)
+    Returns (cons, D-, D+): cons = 0.5 (f(Q_l) + f(Q_r)) - 0.5 lam (Q_r - Q_l). `eos` a
+    Barton2009 selects the single-phase model (14 values), whose path-conservative parts
+    are zero; a pair of them the two-phase model (30 values), with D- = D+ = half the
+    6-point Gauss-Lobatto path integral of the non-conservative matrix."""
+    two = isinstance(eos, (tuple, list))
+    nv = 30 if two else 14
+    cfg = M.config(eos, L.HYP_MODEL_MULTI if two else L.HYP_MODEL_SINGLE,
+                   flux=L.HYP_FLUX_LXF) if two else M.config(eos, L.HYP_MODEL_SINGLE)
+    l, n, single = L.soa(Q_l, nv)
+    r, _, _ = L.soa(Q_r, nv)
     lam = np.ascontiguousarray(np.broadcast_to(np.asarray(lam, dtype=np.float64), (n,)))
-    cons, dm, dp = (np.empty((14, n)) for _ in range(3))
+    cons, dm, dp = (np.empty((nv, n)) for _ in range(3))
     L.check(L.load().hyp_eval_lxf(cfg, L.ptr(l), L.ptr(r), L.ptr(lam), L.ptr(cons), L.ptr(dm), L.ptr(dp), n),
             what="lxf")
     return L.unsoa(cons, single), L.unsoa(dm, single), L.unsoa(dp, single)

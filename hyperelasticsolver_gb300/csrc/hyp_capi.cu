@@ -49,6 +49,7 @@ static int free_ctx(hyp_ctx* c) {
   cudaFree(c->smax);
   cudaFree(c->DM);
   cudaFree(c->DP);
+  cudaFree(c->FF);
   cudaFree(c->st);
   if (c->st_host) cudaFreeHost(c->st_host);
   for (auto& e : c->ev)
@@ -69,9 +70,9 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if (cfg->precision != HYP_PREC_FP64 && cfg->precision != HYP_PREC_MIXED) return HYP_ERR_INVALID;
   if (!valid_eos(cfg->eos[0]) || (cfg->model == HYP_MODEL_MULTI && !valid_eos(cfg->eos[1]))) return HYP_ERR_INVALID;
   // single phase: Rusanov or LxF, FP64 or mixed; two phases: path-conservative HLL (the
-  // reference's main.jl:225 choice) in FP64
+  // reference's main.jl:225 choice) or path-conservative LxF (main.jl:223), in FP64
   if (cfg->model == HYP_MODEL_SINGLE && cfg->flux == HYP_FLUX_HLL) return HYP_ERR_UNSUPPORTED;
-  if (cfg->model == HYP_MODEL_MULTI && (cfg->flux != HYP_FLUX_HLL || cfg->precision != HYP_PREC_FP64))
+  if (cfg->model == HYP_MODEL_MULTI && (cfg->flux == HYP_FLUX_RUSANOV || cfg->precision != HYP_PREC_FP64))
     return HYP_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
@@ -97,6 +98,7 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   c->eos2.e[0] = c->eos[0];
   c->eos2.e[1] = c->eos[1];
   c->quad = gauss_legendre6();
+  c->lobatto = gauss_lobatto6();
   if (cfg->model == HYP_MODEL_MULTI) {
     const size_t nfb = (size_t)30 * (c->n + 1) * sizeof(double);
     for (int p = 0; p < 2 && rc == HYP_OK; ++p)
@@ -106,6 +108,8 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
     if (rc == HYP_OK && (e = cudaMalloc(&c->smax, (size_t)c->n * sizeof(double))) != cudaSuccess) fail(e, "cudaMalloc(smax)");
     if (rc == HYP_OK && (e = cudaMalloc(&c->DM, nfb)) != cudaSuccess) fail(e, "cudaMalloc(DM)");
     if (rc == HYP_OK && (e = cudaMalloc(&c->DP, nfb)) != cudaSuccess) fail(e, "cudaMalloc(DP)");
+    if (rc == HYP_OK && cfg->flux == HYP_FLUX_LXF && (e = cudaMalloc(&c->FF, nfb)) != cudaSuccess)
+      fail(e, "cudaMalloc(face fluxes)");
   } else if (!mixed(c)) {
     for (int p = 0; p < 2 && rc == HYP_OK; ++p)
       if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");

@@ -295,10 +295,38 @@ extern "C" int hyp_eval_eigvals(const hyp_config* cfg, const double* Q, double* 
              },
              &m);
 }
+namespace {
+struct LxfArg2 {
+  ModelArg m;
+  Quad6D qd;
+};
+__global__ void k_lxf2(LxfArg2 a, const double* Ql, const double* Qr, const double* lam, double* cons, double* DMo,
+                       double* DPo, int64_t n) {
+  IDX double ql[30], qr[30], fl[30], fr[30], ff[30], dm[30], dp[30];
+  LD(ql, Ql, 30);
+  LD(qr, Qr, 30);
+  flux2(a.m.e, ql, fl);
+  flux2(a.m.e, qr, fr);
+  lxf_face2(a.m.e, a.qd, ql, qr, fl, fr, lam[i], ff, dm, dp);
+  ST(cons, ff, 30);
+  ST(DMo, dm, 30);
+  ST(DPo, dp, 30);
+}
+}  // namespace
+
 extern "C" int hyp_eval_lxf(const hyp_config* cfg, const double* Ql, const double* Qr, const double* lambda,
                             double* cons, double* dm, double* dp, int64_t n) {
   if (!model_ok(cfg)) return HYP_ERR_INVALID;
-  if (cfg->model != HYP_MODEL_SINGLE) return HYP_ERR_UNSUPPORTED;
+  if (cfg->model == HYP_MODEL_MULTI) {
+    LxfArg2 a2{model_arg(cfg), gauss_lobatto6()};
+    return run(n,
+               {{Ql, nullptr, 30}, {Qr, nullptr, 30}, {lambda, nullptr, 1}, {nullptr, cons, 30}, {nullptr, dm, 30},
+                {nullptr, dp, 30}},
+               [](int64_t n, double** d, const void* a) {
+                 k_lxf2<<<grid(n), kBlock>>>(*(const LxfArg2*)a, d[0], d[1], d[2], d[3], d[4], d[5], n);
+               },
+               &a2);
+  }
   ModelArg m = model_arg(cfg);
   return run(n,
              {{Ql, nullptr, 14}, {Qr, nullptr, 14}, {lambda, nullptr, 1}, {nullptr, cons, 14}, {nullptr, dm, 14},

@@ -89,7 +89,9 @@ struct hyp_ctx {
   hyp::EosMixed eos_mixed;
   // two-phase (FP64): cell fluxes F [30][n], wave-speed bounds, face fluctuations [30][n+1]
   hyp::Eos2 eos2;
-  hyp::Quad6D quad;
+  hyp::Quad6D quad;        // Gauss-Legendre 6 on [0,1] (HLL path integrals)
+  hyp::Quad6D lobatto;     // Gauss-Lobatto 6 on [0,1] (LxF path integrals)
+  double* FF = nullptr;    // two-phase LxF: conservative face fluxes [30][n+1]
   double* smin = nullptr;
   double* smax = nullptr;
   double* DM = nullptr;
@@ -153,4 +155,5 @@ cudaError_t launch_cell2_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, co
 cudaError_t launch_face2_f64(hyp_ctx* c, int p, double t_end);
 cudaError_t launch_update2_f64(hyp_ctx* c, int p, double t_end);
 Quad6D gauss_legendre6();
+Quad6D gauss_lobatto6();
 }  // namespace hyp

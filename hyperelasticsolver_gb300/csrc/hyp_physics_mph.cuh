@@ -151,4 +151,18 @@ HYP_HD int hll_face2(const EosC* eos, const Quad6D& qd, const double* QL, const 
   return st;
 }
 
+// Path-conservative Lax-Friedrichs face of the two-phase model (NumFluxes.jl:25-60):
+// conservative part F = (f_l + f_r)/2 - lambda (Q_r - Q_l)/2 and D- = D+ = half the
+// path integral of B with the 6-point Gauss-Lobatto rule (NumFluxes.jl:36-47).
+HYP_HD int lxf_face2(const EosC* eos, const Quad6D& lobatto, const double* QL, const double* QR, const double* fl,
+                     const double* fr, double lambda, double* F, double* dm, double* dp) {
+  const double hl = lambda * 0.5;
+  for (int k = 0; k < 30; ++k) F[k] = 0.5 * (fl[k] + fr[k]) - hl * (QR[k] - QL[k]);
+  double acc[30];
+  for (int k = 0; k < 30; ++k) acc[k] = 0.0;
+  const int st = path_integral_add(eos, lobatto, QL, QR, acc);
+  for (int k = 0; k < 30; ++k) dm[k] = dp[k] = 0.5 * acc[k];
+  return st;
+}
+
 }  // namespace hyp

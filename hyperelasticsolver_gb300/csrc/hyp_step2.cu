@@ -1,5 +1,6 @@
 // hyp_step2.cu -- two-phase FP64 step with the path-conservative HLL flux
-// (main.jl:202-241 with update_cell :43-60 and NumFluxes.hll :70-132).
+// (main.jl:202-241 with update_cell :43-60 and NumFluxes.hll :70-132) or the
+// path-conservative Lax-Friedrichs flux (update_cell :30-41, NumFluxes.lxf :25-60).
 //
 // Three kernels per step on the context stream:
 //   cell   : per cell, both phases' flux (HyperelasticityMPh.jl:140-175) and
@@ -10,8 +11,12 @@
 //            thread per face -- 18 evaluations of B per face instead of the 30
 //            the reference makes, since the integrals repeated in D- and D+ are
 //            the same;
-//   update : dt = cfl dx / max lambda, t += dt, Q_i - dt/dx ((0 - 0) + (D-_{i+1/2} + D+_{i-1/2}))
-//            with frozen or transmissive ends.
+//   update : dt = cfl dx / max lambda, t += dt, Q_i - dt/dx ((F_r - F_l) + (D-_{i+1/2} + D+_{i-1/2}))
+//            with frozen or transmissive ends; F = 0 for HLL (it folds the conservative
+//            part into D+-), the LxF face flux otherwise.
+// The LxF face kernel takes lambda = dx/dt of this step (main.jl:223) from the
+// max wave speed the cell kernel has just reduced, and integrates B with the
+// 6-point Gauss-Lobatto rule.
 #include "hyp_internal.cuh"
 #include "hyp_physics_mph.cuh"
 
@@ -91,8 +96,37 @@ __global__ void __launch_bounds__(kFaceBlock) face2_f64_kernel(const double* __r
   }
 }
 
+__global__ void __launch_bounds__(kFaceBlock) face2_lxf_f64_kernel(
+    const double* __restrict__ Q, int64_t n, Eos2 E, Quad6D lobatto, const double* __restrict__ F,
+    const unsigned long long* lam_now, double cfl, double dx, double* __restrict__ FF, double* __restrict__ DM,
+    double* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
+  if (!(*t_now < t_end)) return;
+  const int64_t f = (int64_t)blockIdx.x * kFaceBlock + threadIdx.x;  // face between cells f-1 and f
+  if (f > n) return;
+  const int64_t nf = n + 1;
+  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+  const double lmax = __longlong_as_double((long long)*lam_now);
+  const double dt = (cfl * dx) / lmax;
+  const double lam = dx / dt;  // lambda = dx/dt (main.jl:223)
+  double QL[30], QR[30], fl[30], fr[30], ff[30], dm[30], dp[30];
+  for (int v = 0; v < 30; ++v) {
+    QL[v] = Q[v * n + L];
+    QR[v] = Q[v * n + R];
+    fl[v] = F[v * n + L];
+    fr[v] = F[v * n + R];
+  }
+  const int st = lxf_face2(E.e, lobatto, QL, QR, fl, fr, lam, ff, dm, dp);
+  if (st) record_err2(S, st, R);
+  for (int v = 0; v < 30; ++v) {
+    FF[v * nf + f] = ff[v];
+    DM[v * nf + f] = dm[v];
+    DP[v * nf + f] = dp[v];
+  }
+}
+
 __global__ void __launch_bounds__(kBlock) update2_f64_kernel(const double* __restrict__ Q, double* __restrict__ Qn,
-                                                             int64_t n, const double* __restrict__ DM,
+                                                             int64_t n, const double* __restrict__ FF,
+                                                             const double* __restrict__ DM,
                                                              const double* __restrict__ DP,
                                                              const unsigned long long* lam_in,
                                                              unsigned long long* lam_next, const double* t_in,
@@ -118,8 +152,9 @@ __global__ void __launch_bounds__(kBlock) update2_f64_kernel(const double* __res
   }
   for (int v = 0; v < 30; ++v) {
     // F_r = F_l = zeros(30) for hll (NumFluxes.jl:82), NF_r = D- of face i+1/2, NF_l = D+ of face i-1/2
+    const double fr = FF ? FF[v * nf + i + 1] : 0.0, fl = FF ? FF[v * nf + i] : 0.0;
     const double nfr = DM[v * nf + i + 1], nfl = DP[v * nf + i];
-    Qn[v * n + i] = Q[v * n + i] - dtdx * ((0.0 - 0.0) + (nfr + nfl));
+    Qn[v * n + i] = Q[v * n + i] - dtdx * ((fr - fl) + (nfr + nfl));
   }
 }
 
@@ -131,14 +166,21 @@ cudaError_t launch_cell2_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, co
   return cudaGetLastError();
 }
 cudaError_t launch_face2_f64(hyp_ctx* c, int p, double t_end) {
-  face2_f64_kernel<<<grid_n(c->n + 1, kFaceBlock), kFaceBlock, 0, c->stream>>>(
-      c->Q[p], c->n, c->eos2, c->quad, c->F, c->smin, c->smax, c->DM, c->DP, &c->st->t[p], t_end, c->st);
+  if (c->cfg.flux == HYP_FLUX_LXF) {
+    const double dx = c->cfg.x_length / (double)c->n;
+    face2_lxf_f64_kernel<<<grid_n(c->n + 1, kFaceBlock), kFaceBlock, 0, c->stream>>>(
+        c->Q[p], c->n, c->eos2, c->lobatto, c->F, &c->st->lam_bits[p], c->cfg.cfl, dx, c->FF, c->DM, c->DP,
+        &c->st->t[p], t_end, c->st);
+  } else {
+    face2_f64_kernel<<<grid_n(c->n + 1, kFaceBlock), kFaceBlock, 0, c->stream>>>(
+        c->Q[p], c->n, c->eos2, c->quad, c->F, c->smin, c->smax, c->DM, c->DP, &c->st->t[p], t_end, c->st);
+  }
   return cudaGetLastError();
 }
 cudaError_t launch_update2_f64(hyp_ctx* c, int p, double t_end) {
   const double dx = c->cfg.x_length / (double)c->n;
   update2_f64_kernel<<<grid_n(c->n, kBlock), kBlock, 0, c->stream>>>(
-      c->Q[p], c->Q[1 - p], c->n, c->DM, c->DP, &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p],
+      c->Q[p], c->Q[1 - p], c->n, c->FF, c->DM, c->DP, &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p],
       &c->st->t[1 - p], &c->st->steps, t_end, c->cfg.cfl, dx, c->cfg.bc);
   return cudaGetLastError();
 }
@@ -179,6 +221,23 @@ Quad6D gauss_legendre6() {
     const double nx = (double)xs[5 - i], nw = (double)ws[5 - i];
     q.x[i] = (nx + 1.0) / 2.0;
     q.w[i] = nw / 2.0;
+  }
+  return q;
+}
+
+// Gauss-Lobatto 6 on [0,1] (FastGaussQuadrature.gausslobatto(6), NumFluxes.jl:36):
+// nodes -1, -a, -b, b, a, 1 with a, b = sqrt(1/3 +- 2 sqrt(7)/21), weights 1/15 at the
+// ends and (14 -+ sqrt 7)/30 inside, mapped (x + 1)/2, w/2; evaluated in long double.
+Quad6D gauss_lobatto6() {
+  const long double s7 = sqrtl(7.0L);
+  const long double a = sqrtl(1.0L / 3.0L + 2.0L * s7 / 21.0L), b = sqrtl(1.0L / 3.0L - 2.0L * s7 / 21.0L);
+  const long double xs[6] = {-1.0L, -a, -b, b, a, 1.0L};
+  const long double ws[6] = {1.0L / 15.0L, (14.0L - s7) / 30.0L, (14.0L + s7) / 30.0L,
+                             (14.0L + s7) / 30.0L, (14.0L - s7) / 30.0L, 1.0L / 15.0L};
+  Quad6D q;
+  for (int i = 0; i < 6; ++i) {
+    q.x[i] = ((double)xs[i] + 1.0) / 2.0;
+    q.w[i] = (double)ws[i] / 2.0;
   }
   return q;
 }

@@ -14,8 +14,8 @@ def eos_pair(hyp):
     return (hyp.Barton2009(), hyp.Barton2009(_b0=B0_SOFT))
 
 
-def oracle_pb(orc, nx=3, cfl=0.5, bc=0):
-    return orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, nx=nx, cfl=cfl, bc=bc,
+def oracle_pb(orc, nx=3, cfl=0.5, bc=0, flux=None):
+    return orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL if flux is None else flux, nx=nx, cfl=cfl, bc=bc,
                        eos=(orc.barton2009(), orc.barton2009(b0=B0_SOFT)))
 
 
@@ -53,6 +53,12 @@ def test_twophase_evaluators(hyp, orc):
     dmo, dpo = orc.hll(pb, Ql, Qr, eo[:-1], eo[1:])
     assert_close(dm, dmo, 1e-11, "hll D-")
     assert_close(dp, dpo, 1e-11, "hll D+")
+    lam = rng.uniform(5.0, 8.0, len(Ql))
+    cons, dm, dp = NF.lxf(eos, Ql, Qr, lam)
+    co, dmo, dpo = orc.lxf(oracle_pb(orc, flux=orc.FLUX_LXF), Ql, Qr, lam)
+    assert_close(cons, co, RTOL_FP64, "two-phase lxf cons")
+    assert_close(dm, dmo, 1e-11, "two-phase lxf D-")
+    assert_close(dp, dpo, 1e-11, "two-phase lxf D+")
 
 
 def test_golden_hll_face_on_gpu(hyp):
@@ -72,34 +78,38 @@ def test_golden_hll_face_on_gpu(hyp):
         assert_close(dp, h["dp"], 1e-11, "golden hll D+")
 
 
+@pytest.mark.parametrize("flux", ["hll", "lxf"])
 @pytest.mark.parametrize("testcase", [4, 6, 7])
-def test_reference_testcases_step(hyp, orc, testcase):
+def test_reference_testcases_step(hyp, orc, testcase, flux):
     """The reference's two-phase Riemann test cases (HyperelasticityMPh.jl:275-426) on
-    100 cells with the HLL flux and frozen ends (main.jl:178-227), 30 steps."""
+    100 cells with the HLL flux (main.jl:225) or the path-conservative LxF flux
+    (main.jl:223) and frozen ends (main.jl:178-227), 30 steps."""
     from hyperelasticsolver_gb300._cases import mph_case, initial_condition
     nx, steps = 100, 30
-    pb = oracle_pb(orc, nx=nx, cfl=0.6)
+    pb = oracle_pb(orc, nx=nx, cfl=0.6, flux=orc.FLUX_HLL if flux == "hll" else orc.FLUX_LXF)
     Pl, Pr = mph_case(testcase)
     Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
     Qo, so, to, _ = orc.run(pb, Q0, max_steps=steps)
-    with hyp.Solver(eos_pair(hyp), nx, model="multi", flux="hll", cfl=0.6) as s:
+    with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, cfl=0.6) as s:
         s.upload(Q0)
         n, t = s.step(max_steps=steps)
         assert n == steps and abs(t - to) <= RTOL_FP64 * to
-        err = assert_close_soa(s.download(), Qo, RTOL_FP64, f"test case {testcase}")
-    print(f"two-phase test case {testcase}, {steps} steps: max per-variable relative error {err:.2e}")
+        err = assert_close_soa(s.download(), Qo, RTOL_FP64, f"test case {testcase} ({flux})")
+    print(f"two-phase test case {testcase} ({flux}), {steps} steps: max per-variable relative error {err:.2e}")
 
 
-def test_smoothed_interface_transmissive(hyp, orc):
+@pytest.mark.parametrize("flux", ["hll", "lxf"])
+def test_smoothed_interface_transmissive(hyp, orc, flux):
     """Volume fraction going from 1 - 1e-6 to 1e-6 across 8 cells (tanh profile as
     main.jl:110-123), transmissive ends."""
     from hyperelasticsolver_gb300._cases import mph_interface_prims
     nx, steps = 64, 12
     P = mph_interface_prims(hyp.Barton2009(), nx)
-    pb = oracle_pb(orc, nx=nx, cfl=0.5, bc=orc.BC_TRANSMISSIVE)
+    pb = oracle_pb(orc, nx=nx, cfl=0.5, bc=orc.BC_TRANSMISSIVE,
+                   flux=orc.FLUX_HLL if flux == "hll" else orc.FLUX_LXF)
     Q0 = np.ascontiguousarray(orc.prim2cons(pb, P).T)
     Qo, so, to, _ = orc.run(pb, Q0, max_steps=steps)
-    with hyp.Solver(eos_pair(hyp), nx, model="multi", flux="hll", bc="transmissive", cfl=0.5) as s:
+    with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, bc="transmissive", cfl=0.5) as s:
         s.upload(Q0)
         n, t = s.step(max_steps=steps)
         assert n == steps
