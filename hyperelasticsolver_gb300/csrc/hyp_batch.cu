@@ -520,7 +520,7 @@ extern "C" int hyp_batch_upload(hyp_batch* b, const double* Q, double t0) {
   if (b->mixed) {
     double* stage = (double*)b->Qh[1];
     BCK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, b->stream));
-    BCK(launch_split_n(b->stream, stage, b->Qh[0], b->Ql[0], b->total, b->mpitch));
+    BCK(launch_split_n(b->stream, stage, b->Qh[0], b->Ql[0], 14, b->total, b->mpitch));
     MixedArrays a = batch_arrays(b, 0);
     a.lam_out = b->lamf[0];
     a.isl_out = b->isl[0];
@@ -541,7 +541,7 @@ extern "C" int hyp_batch_download(hyp_batch* b, double* Q) {
   const size_t bytes = (size_t)14 * b->total * sizeof(double);
   if (b->mixed) {
     double* stage = (double*)b->Qh[1 - b->cur];
-    BCK(launch_join_n(b->stream, b->Qh[b->cur], b->Ql[b->cur], stage, b->total, b->mpitch));
+    BCK(launch_join_n(b->stream, b->Qh[b->cur], b->Ql[b->cur], stage, 14, b->total, b->mpitch));
     BCK(cudaMemcpyAsync(Q, stage, bytes, cudaMemcpyDeviceToHost, b->stream));
   } else {
     BCK(cudaMemcpyAsync(Q, b->Q[b->cur], bytes, cudaMemcpyDeviceToHost, b->stream));

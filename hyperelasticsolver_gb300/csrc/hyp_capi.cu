@@ -33,6 +33,7 @@ static bool valid_eos(const hyp_barton2009& b) {
 }
 
 static bool mixed(const hyp_ctx* c) { return c->cfg.precision == HYP_PREC_MIXED; }
+static bool mixed1(const hyp_ctx* c) { return mixed(c) && c->cfg.model == HYP_MODEL_SINGLE; }
 
 static int free_ctx(hyp_ctx* c) {
   if (!c) return HYP_OK;
@@ -50,6 +51,12 @@ static int free_ctx(hyp_ctx* c) {
   cudaFree(c->DM);
   cudaFree(c->DP);
   cudaFree(c->FF);
+  cudaFree(c->F32);
+  cudaFree(c->smin32);
+  cudaFree(c->smax32);
+  cudaFree(c->DM32);
+  cudaFree(c->DP32);
+  cudaFree(c->FF32);
   cudaFree(c->st);
   if (c->st_host) cudaFreeHost(c->st_host);
   for (auto& e : c->ev)
@@ -70,10 +77,9 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if (cfg->precision != HYP_PREC_FP64 && cfg->precision != HYP_PREC_MIXED) return HYP_ERR_INVALID;
   if (!valid_eos(cfg->eos[0]) || (cfg->model == HYP_MODEL_MULTI && !valid_eos(cfg->eos[1]))) return HYP_ERR_INVALID;
   // single phase: Rusanov or LxF, FP64 or mixed; two phases: path-conservative HLL (the
-  // reference's main.jl:225 choice) or path-conservative LxF (main.jl:223), in FP64
+  // reference's main.jl:225 choice) or path-conservative LxF (main.jl:223), FP64 or mixed
   if (cfg->model == HYP_MODEL_SINGLE && cfg->flux == HYP_FLUX_HLL) return HYP_ERR_UNSUPPORTED;
-  if (cfg->model == HYP_MODEL_MULTI && (cfg->flux == HYP_FLUX_RUSANOV || cfg->precision != HYP_PREC_FP64))
-    return HYP_ERR_UNSUPPORTED;
+  if (cfg->model == HYP_MODEL_MULTI && cfg->flux == HYP_FLUX_RUSANOV) return HYP_ERR_UNSUPPORTED;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
   hyp_ctx* c = new (std::nothrow) hyp_ctx();
@@ -99,7 +105,26 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   c->eos2.e[1] = c->eos[1];
   c->quad = gauss_legendre6();
   c->lobatto = gauss_lobatto6();
-  if (cfg->model == HYP_MODEL_MULTI) {
+  if (cfg->model == HYP_MODEL_MULTI && mixed(c)) {
+    // state [2 parities][30 hi + 30 lo rows][pitch] floats; a parity's block also stages
+    // FP64 uploads and downloads (30 pitch doubles >= 30 n)
+    c->mpitch = mixed_pitch(c->n);
+    const size_t nf4 = (size_t)30 * (c->n + 1) * sizeof(float);
+    if ((e = cudaMalloc(&c->mixed_base, (size_t)2 * 60 * c->mpitch * sizeof(float))) != cudaSuccess)
+      fail(e, "cudaMalloc(mixed state)");
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
+      c->Qh[p] = c->mixed_base + (size_t)p * 60 * c->mpitch;
+      c->Ql[p] = c->Qh[p] + (size_t)30 * c->mpitch;
+    }
+    if (rc == HYP_OK && (e = cudaMalloc(&c->F32, (size_t)30 * c->n * sizeof(float))) != cudaSuccess)
+      fail(e, "cudaMalloc(F)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->smin32, (size_t)c->n * sizeof(float))) != cudaSuccess) fail(e, "cudaMalloc(smin)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->smax32, (size_t)c->n * sizeof(float))) != cudaSuccess) fail(e, "cudaMalloc(smax)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->DM32, nf4)) != cudaSuccess) fail(e, "cudaMalloc(DM)");
+    if (rc == HYP_OK && (e = cudaMalloc(&c->DP32, nf4)) != cudaSuccess) fail(e, "cudaMalloc(DP)");
+    if (rc == HYP_OK && cfg->flux == HYP_FLUX_LXF && (e = cudaMalloc(&c->FF32, nf4)) != cudaSuccess)
+      fail(e, "cudaMalloc(face fluxes)");
+  } else if (cfg->model == HYP_MODEL_MULTI) {
     const size_t nfb = (size_t)30 * (c->n + 1) * sizeof(double);
     for (int p = 0; p < 2 && rc == HYP_OK; ++p)
       if ((e = cudaMalloc(&c->Q[p], nq)) != cudaSuccess) fail(e, "cudaMalloc(Q)");
@@ -192,7 +217,7 @@ extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_va
     double* stage = (double*)c->Qh[1];
     CK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, c->stream));
     CK(launch_split(c, stage, c->Qh[0], c->Ql[0]));
-    CK(launch_lam1_mixed(c, 0, &c->st->lam_slots[0]));
+    if (mixed1(c)) CK(launch_lam1_mixed(c, 0, &c->st->lam_slots[0]));
   }
   int rc = sync_state(c);
   if (rc != HYP_OK) return rc;
@@ -240,7 +265,13 @@ static int enqueue_step(hyp_ctx* c, long long k, double t_end, bool prof) {
     if ((rc = prof_event(c, &e0)) || (rc = prof_event(c, &e1)) || (rc = prof_event(c, &e2))) return rc;
     CK(cudaEventRecord(e0, c->stream));
   }
-  if (c->cfg.model == HYP_MODEL_MULTI) {
+  if (c->cfg.model == HYP_MODEL_MULTI && mixed(c)) {
+    const int p = (int)(k & 1);
+    CK(launch_cell2_mixed(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
+    CK(launch_face2_mixed(c, p, t_end));
+    if (prof) CK(cudaEventRecord(e1, c->stream));
+    CK(launch_update2_mixed(c, p, t_end));
+  } else if (c->cfg.model == HYP_MODEL_MULTI) {
     const int p = (int)(k & 1);
     CK(launch_cell2_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
     CK(launch_face2_f64(c, p, t_end));
@@ -276,8 +307,8 @@ static int collect_profile(hyp_ctx* c) {
 }
 
 // steps per captured graph: a multiple of the launch pattern's period
-static int graph_period(const hyp_ctx* c) { return mixed(c) ? 6 : 2; }
-static int graph_steps(const hyp_ctx* c) { return mixed(c) ? 12 : 16; }
+static int graph_period(const hyp_ctx* c) { return mixed1(c) ? 6 : 2; }
+static int graph_steps(const hyp_ctx* c) { return mixed1(c) ? 12 : 16; }
 
 static int ensure_graph(hyp_ctx* c, long long k0, double t_end) {
   const int key = (int)(k0 % graph_period(c));
@@ -387,7 +418,7 @@ extern "C" int hyp_set_mixed_kernel(hyp_ctx* c, int tma) {
 extern "C" int hyp_max_wavespeed(hyp_ctx* c, double* out) {
   if (!c || !out) return HYP_ERR_INVALID;
   CK(cudaSetDevice(c->device));
-  if (mixed(c)) {  // kept by the last step (or the upload) for the current state
+  if (mixed1(c)) {  // kept by the last step (or the upload) for the current state
     int rc = sync_state(c);
     if (rc != HYP_OK) return rc;
     unsigned bits = (unsigned)c->st_host->lam_slots[c->steps_host % 3];
@@ -397,7 +428,9 @@ extern "C" int hyp_max_wavespeed(hyp_ctx* c, double* out) {
     return check_cell_error(c);
   }
   CK(cudaMemsetAsync(&c->st->lam_query, 0, sizeof(unsigned long long), c->stream));
-  if (c->cfg.model == HYP_MODEL_MULTI)
+  if (c->cfg.model == HYP_MODEL_MULTI && mixed(c))
+    CK(launch_cell2_mixed(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
+  else if (c->cfg.model == HYP_MODEL_MULTI)
     CK(launch_cell2_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));
   else
     CK(launch_cell1_f64(c, c->cur, &c->st->lam_query, &c->st->t[c->cur], INFINITY));

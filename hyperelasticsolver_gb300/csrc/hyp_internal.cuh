@@ -92,6 +92,13 @@ struct hyp_ctx {
   hyp::Quad6D quad;        // Gauss-Legendre 6 on [0,1] (HLL path integrals)
   hyp::Quad6D lobatto;     // Gauss-Lobatto 6 on [0,1] (LxF path integrals)
   double* FF = nullptr;    // two-phase LxF: conservative face fluxes [30][n+1]
+  // two-phase mixed precision (FP32): cell fluxes [30][n], speed bounds, face fluctuations [30][n+1]
+  float* F32 = nullptr;
+  float* smin32 = nullptr;
+  float* smax32 = nullptr;
+  float* DM32 = nullptr;
+  float* DP32 = nullptr;
+  float* FF32 = nullptr;
   double* smin = nullptr;
   double* smax = nullptr;
   double* DM = nullptr;
@@ -144,8 +151,12 @@ cudaError_t launch_cell1_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, co
 cudaError_t launch_update1_f64(hyp_ctx* c, int p, double t_end);
 // single-phase mixed-precision launchers (hyp_step1_mixed.cu)
 cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo);
-cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int64_t n, int64_t pitch);
-cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int64_t n, int64_t pitch);
+cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int rows, int64_t n, int64_t pitch);
+cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int rows, int64_t n, int64_t pitch);
+// two-phase mixed precision (hyp_step2_mixed.cu)
+cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
+cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end);
+cudaError_t launch_update2_mixed(hyp_ctx* c, int p, double t_end);
 int setup_mixed_tma(hyp_ctx* c);
 cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q);
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot);

@@ -1,0 +1,256 @@
+// hyp_physics_mph_mixed.cuh -- the two-phase physics of hyp_physics_mph.cuh in
+// FP32 for the mixed-precision two-phase step.
+//
+// Per phase, cons2prim (HyperelasticityMPh.jl:106-133) keeps its cancellation-
+// prone steps in float-float, as the single-phase mixed step does:
+// det(alpha rho A) (with the lo parts of a compensated state through the
+// cofactors), rho_true = sqrt(det(rho A / alpha) / rho0), 1/(alpha rho_true),
+// alpha rho e = alpha rho E - |alpha rho u|^2 / (2 alpha rho_true), and
+// s - 1 = rho_true/rho0 - 1. Everything else -- the Finger tensor, stress,
+// temperature, the non-conservative columns of B (HyperelasticityMPh.jl:178-250),
+// wave speeds, fluxes and the path-conservative HLL / LxF faces
+// (NumFluxes.jl:25-132) -- is FP32, statement for statement as in the FP64 forms.
+#pragma once
+#include "hyp_physics_mixed.cuh"
+#include "hyp_physics_mph.cuh"
+
+namespace hyp {
+
+struct Eos2M {
+  EosMixed m[2];
+};
+
+struct Quad6F {
+  float x[6], w[6];
+};
+
+// One phase of a two-phase cell in FP32.
+struct PrimM2 {
+  float den, true_den;  // alpha rho_true, rho_true
+  float u[3], E, e_int;
+  float A[9];
+  float xm1;
+  float sm1, rho_s;     // rho_true/rho0 - 1, rho0 s
+  KinT<float> k;
+  PowsT<float> w;
+};
+
+// q: [alpha, alpha rho (unused), alpha rho u(3), alpha rho E, alpha rho A(9)]; ql: the lo
+// parts (or nullptr). Returns HYP_CELL_* status.
+__device__ __forceinline__ int cons_to_prim_m2(const EosMixed& em, const float* q, const float* ql, PrimM2& P) {
+  const EosT<float>& e = em.f;
+  const float* m = q + 6;
+  // det(alpha rho A) in float-float, lo parts through the cofactors
+  ff C00 = ff_diff_prod(m[4], m[8], m[7], m[5]);
+  ff C01 = ff_neg(ff_diff_prod(m[1], m[8], m[7], m[2]));
+  ff C02 = ff_diff_prod(m[1], m[5], m[4], m[2]);
+  ff d = ff_add(ff_add(ff_mul_f(C00, m[0]), ff_mul_f(C01, m[3])), ff_mul_f(C02, m[6]));
+  if (ql) {
+    const float* l = ql + 6;
+    float dlo = C00.hi * l[0] + C01.hi * l[3] + C02.hi * l[6];
+    dlo += -(m[3] * m[8] - m[6] * m[5]) * l[1] + (m[0] * m[8] - m[6] * m[2]) * l[4] -
+           (m[0] * m[5] - m[3] * m[2]) * l[7];
+    dlo += (m[3] * m[7] - m[6] * m[4]) * l[2] - (m[0] * m[7] - m[6] * m[1]) * l[5] +
+           (m[0] * m[4] - m[3] * m[1]) * l[8];
+    d = ff_add_f(d, dlo);
+  }
+  int st = d.hi > 0.0f ? HYP_CELL_OK : HYP_CELL_NEG_DET;
+  const ff alpha{q[0], ql ? ql[0] : 0.0f};
+  const ff ia = ff_recip(alpha);
+  // det(rho A / alpha) = det(alpha rho A) / alpha^3
+  const ff dq = ff_mul(ff_mul(ff_mul(d, ia), ia), ia);
+  const ff rho = ff_sqrt(ff_mul(dq, em.inv_rho0));  // rho_true
+  const ff den = ff_mul(alpha, rho);
+  const ff inv_den = ff_recip(den);
+  ff m0{q[2], ql ? ql[2] : 0.0f}, m1{q[3], ql ? ql[3] : 0.0f}, m2{q[4], ql ? ql[4] : 0.0f};
+  const ff k2 = ff_add(ff_add(ff_mul(m0, m0), ff_mul(m1, m1)), ff_mul(m2, m2));
+  const ff rhoe = ff_sub(ff{q[5], ql ? ql[5] : 0.0f}, ff_mul(k2, ff_mul_f(inv_den, 0.5f)));
+  P.e_int = ff_val(ff_mul(rhoe, inv_den));
+  const ff s = ff_mul(rho, em.inv_rho0);  // 1/det A
+  P.sm1 = ff_val(ff_add_f(s, -1.0f));
+  P.true_den = ff_val(rho);
+  P.den = ff_val(den);
+  const float idn = ff_val(inv_den);
+  for (int c = 0; c < 3; ++c) P.u[c] = q[2 + c] * idn;
+  P.E = q[5] * idn;
+  for (int c = 0; c < 9; ++c) P.A[c] = m[c] * idn;
+  const float sf = 1.0f + P.sm1;
+  P.k = kinematics_s<float>(P.A, sf, __frcp_rn(sf));
+  P.w = powers<float>(e, P.k);
+  P.w.Pam1 = e.default_exp ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
+  P.xm1 = entropy_xm1<float>(e, P.e_int, P.k, P.w);
+  P.rho_s = e.rho0 * sf;
+  if (!(P.e_int == P.e_int) || !(P.xm1 == P.xm1) || !isfinite(P.k.p)) st |= HYP_CELL_NONFINITE;
+  return st;
+}
+
+// Flux of one phase after alpha (HyperelasticityMPh.jl:146-175), 14 components.
+__device__ __forceinline__ void phase_flux_m2(const EosT<float>& e, float alpha, const PrimM2& P,
+                                              const StressCT<float>& c, float* f) {
+  float s0[3];
+  stress_row0<float>(P.rho_s, P.k, c, s0);
+  s0[0] *= alpha;
+  s0[1] *= alpha;
+  s0[2] *= alpha;
+  const float du = P.den * P.u[0];
+  f[0] = du;
+  f[1] = du * P.u[0] - s0[0];
+  f[2] = du * P.u[1] - s0[1];
+  f[3] = du * P.u[2] - s0[2];
+  f[4] = du * P.E - (P.u[0] * s0[0] + P.u[1] * s0[1] + P.u[2] * s0[2]);
+  for (int b = 0; b < 3; ++b)
+    for (int a = 0; a < 3; ++a) f[5 + a + 3 * b] = P.den * (P.u[0] * P.A[a + 3 * b] - P.u[a] * P.A[3 * b]);
+}
+
+__device__ __forceinline__ float phase_cmax_m2(const EosT<float>& e, const PrimM2& P, const StressCT<float>& c) {
+  float s0[3], s0r[3], om[9];
+  stress_row0<float>(P.rho_s, P.k, c, s0);
+  const float irs = __frcp_rn(P.rho_s);
+  for (int i = 0; i < 3; ++i) s0r[i] = s0[i] * irs;
+  acoustic_omega<float>(e, P.k, P.w, c, P.xm1, s0r, om);
+  return sqrtf(spectral_radius_fast(om));
+}
+
+// Both phases' flux (30) and wave-speed bounds of a cell from its compensated state.
+__device__ __forceinline__ int cell2_mixed(const Eos2M& E, const float* qh, const float* ql, float* F, float& smin,
+                                           float& smax) {
+  int st = 0;
+  for (int p = 0; p < 2; ++p) {
+    const float* q = qh + 15 * p;
+    PrimM2 P;
+    st |= cons_to_prim_m2(E.m[p], q, ql + 15 * p, P);
+    const StressCT<float> c = stress_coeffs<float>(E.m[p].f, P.k, P.w, P.xm1);
+    F[15 * p] = 0.0f;
+    phase_flux_m2(E.m[p].f, q[0], P, c, F + 15 * p + 1);
+    const float cm = phase_cmax_m2(E.m[p].f, P, c);
+    const float lo = P.u[0] - cm, hi = P.u[0] + cm;
+    if (p == 0 || lo < smin) smin = lo;
+    if (p == 0 || hi > smax) smax = hi;
+  }
+  return st;
+}
+
+__device__ __forceinline__ int speeds2_m(const Eos2M& E, const float* Q, float& smin, float& smax) {
+  int st = 0;
+  for (int p = 0; p < 2; ++p) {
+    PrimM2 P;
+    st |= cons_to_prim_m2(E.m[p], Q + 15 * p, nullptr, P);
+    const StressCT<float> c = stress_coeffs<float>(E.m[p].f, P.k, P.w, P.xm1);
+    const float cm = phase_cmax_m2(E.m[p].f, P, c);
+    const float lo = P.u[0] - cm, hi = P.u[0] + cm;
+    if (p == 0 || lo < smin) smin = lo;
+    if (p == 0 || hi > smax) smax = hi;
+  }
+  return st;
+}
+
+// What B needs from one phase (as phase_b).
+struct PhaseBM {
+  float true_den, u[3], A[9], K0[3], T;
+};
+
+__device__ __forceinline__ int phase_b_m(const EosMixed& em, const float* q, PhaseBM& b) {
+  PrimM2 P;
+  const int st = cons_to_prim_m2(em, q, nullptr, P);
+  const StressCT<float> c = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
+  stress_row0<float>(P.rho_s, P.k, c, b.K0);
+  b.T = em.f.t0 * P.w.Pg * (P.xm1 + 1.0f);
+  b.true_den = P.true_den;
+  for (int a = 0; a < 3; ++a) b.u[a] = P.u[a];
+  for (int k = 0; k < 9; ++k) b.A[k] = P.A[k];
+  return st;
+}
+
+// bcol of B(Q) (noncons_bcol in FP32).
+__device__ __forceinline__ int noncons_bcol_m(const Eos2M& E, const float* Q, float* bcol) {
+  PhaseBM b[2];
+  const int st = phase_b_m(E.m[0], Q, b[0]) | phase_b_m(E.m[1], Q + 15, b[1]);
+  float uI[3], sI[3];
+  for (int a = 0; a < 3; ++a) uI[a] = 0.5f * b[0].u[a] + 0.5f * b[1].u[a];
+  const float iden = __frcp_rn(0.5f * b[0].T + 0.5f * b[1].T);
+  for (int a = 0; a < 3; ++a) sI[a] = ((0.5f * b[1].T) * b[0].K0[a] + (0.5f * b[0].T) * b[1].K0[a]) * iden;
+  for (int p = 0; p < 2; ++p) {
+    float* r = bcol + 15 * p;
+    const PhaseBM& B = b[p];
+    r[0] = uI[0];
+    r[1] = 0.0f;
+    r[2] = sI[0];
+    r[3] = sI[1];
+    r[4] = sI[2];
+    r[5] = (sI[0] * uI[0] + sI[1] * uI[1]) + sI[2] * uI[2];
+    for (int c = 0; c < 3; ++c)
+      for (int a = 0; a < 3; ++a) r[6 + a + 3 * c] = (B.true_den * B.A[3 * c]) * B.u[a];
+    const float dv[3] = {uI[0] - B.u[0], uI[1] - B.u[1], uI[2] - B.u[2]};
+    for (int c = 0; c < 3; ++c)
+      r[6 + 3 * c] += B.true_den * ((B.A[3 * c] * dv[0] + B.A[1 + 3 * c] * dv[1]) + B.A[2 + 3 * c] * dv[2]);
+  }
+  return st;
+}
+
+__device__ __forceinline__ int path_integral_add_m(const Eos2M& E, const Quad6F& qd, const float* Qa, const float* Qb,
+                                                   float* acc) {
+  const float da0 = Qb[0] - Qa[0], da1 = Qb[15] - Qa[15];
+  int st = 0;
+  float u[30], bc[30];
+  for (int i = 0; i < 6; ++i) {
+    const float s = qd.x[i], oms = 1.0f - s;
+    for (int k = 0; k < 30; ++k) u[k] = Qa[k] * oms + Qb[k] * s;
+    st |= noncons_bcol_m(E, u, bc);
+    for (int k = 0; k < 30; ++k) acc[k] += (qd.w[i] * bc[k]) * (k < 15 ? da0 : da1);
+  }
+  return st;
+}
+
+// Path-conservative HLL fluctuations of one face (hll_face2 in FP32).
+__device__ __forceinline__ int hll_face2_m(const Eos2M& E, const Quad6F& qd, const float* QL, const float* QR,
+                                           const float* fl, const float* fr, float sminL, float smaxR, float* dm,
+                                           float* dp) {
+  float Qm[30];
+  for (int k = 0; k < 30; ++k) Qm[k] = 0.5f * (QL[k] + QR[k]);
+  float mmin = 0.0f, mmax = 0.0f;
+  int st = speeds2_m(E, Qm, mmin, mmax);
+  float sl = 0.0f;
+  if (mmin < sl) sl = mmin;
+  if (sminL < sl) sl = sminL;
+  float sr = 0.0f;
+  if (mmax > sr) sr = mmax;
+  if (smaxR > sr) sr = smaxR;
+  const float idsr = 1.0f / (sr - sl);
+  float acc[30], Qh[30];
+  for (int k = 0; k < 30; ++k) acc[k] = 0.0f;
+  st |= path_integral_add_m(E, qd, QL, QR, acc);
+  for (int k = 0; k < 30; ++k) {
+    const float pint = (acc[k] + fr[k]) - fl[k];
+    Qh[k] = ((QR[k] * sr - QL[k] * sl) - pint) * idsr;
+  }
+  float b2[30];
+  for (int k = 0; k < 30; ++k) {
+    acc[k] = 0.0f;
+    b2[k] = 0.0f;
+  }
+  st |= path_integral_add_m(E, qd, QL, Qh, acc);
+  st |= path_integral_add_m(E, qd, Qh, QR, b2);
+  const float cm = (-sl) * idsr, cp = sr * idsr, cq = (sl * sr) * idsr;
+  for (int k = 0; k < 30; ++k) {
+    const float inner = ((fr[k] - fl[k]) + acc[k]) + b2[k];
+    const float jump = QR[k] - QL[k];
+    dm[k] = cm * inner + cq * jump;
+    dp[k] = cp * inner - cq * jump;
+  }
+  return st;
+}
+
+// Path-conservative LxF face (lxf_face2 in FP32).
+__device__ __forceinline__ int lxf_face2_m(const Eos2M& E, const Quad6F& lobatto, const float* QL, const float* QR,
+                                           const float* fl, const float* fr, float lambda, float* F, float* dm,
+                                           float* dp) {
+  const float hl = lambda * 0.5f;
+  for (int k = 0; k < 30; ++k) F[k] = 0.5f * (fl[k] + fr[k]) - hl * (QR[k] - QL[k]);
+  float acc[30];
+  for (int k = 0; k < 30; ++k) acc[k] = 0.0f;
+  const int st = path_integral_add_m(E, lobatto, QL, QR, acc);
+  for (int k = 0; k < 30; ++k) dm[k] = dp[k] = 0.5f * acc[k];
+  return st;
+}
+
+}  // namespace hyp

@@ -202,19 +202,21 @@ unsigned elementwise_grid(int64_t m) {
   return (unsigned)(g > 152 * 64 ? 152 * 64 : (g < 1 ? 1 : g));
 }
 
-cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int64_t n, int64_t pitch) {
-  split_kernel<<<elementwise_grid(14 * n), kBlock, 0, s>>>(q, hi, lo, n, pitch, 14 * n);
+cudaError_t launch_split_n(cudaStream_t s, const double* q, float* hi, float* lo, int rows, int64_t n,
+                           int64_t pitch) {
+  split_kernel<<<elementwise_grid(rows * n), kBlock, 0, s>>>(q, hi, lo, n, pitch, rows * n);
   return cudaGetLastError();
 }
-cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int64_t n, int64_t pitch) {
-  join_kernel<<<elementwise_grid(14 * n), kBlock, 0, s>>>(hi, lo, q, n, pitch, 14 * n);
+cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, double* q, int rows, int64_t n,
+                          int64_t pitch) {
+  join_kernel<<<elementwise_grid(rows * n), kBlock, 0, s>>>(hi, lo, q, n, pitch, rows * n);
   return cudaGetLastError();
 }
 cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo) {
-  return launch_split_n(c->stream, q, hi, lo, c->n, c->mpitch);
+  return launch_split_n(c->stream, q, hi, lo, c->nvar, c->n, c->mpitch);
 }
 cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q) {
-  return launch_join_n(c->stream, hi, lo, q, c->n, c->mpitch);
+  return launch_join_n(c->stream, hi, lo, q, c->nvar, c->n, c->mpitch);
 }
 
 static MixedArrays arrays_of(hyp_ctx* c, int p) {

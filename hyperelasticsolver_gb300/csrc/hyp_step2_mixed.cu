@@ -1,0 +1,193 @@
+// hyp_step2_mixed.cu -- two-phase step in mixed precision: the kernels of
+// hyp_step2.cu with FP32 physics (hyp_physics_mph_mixed.cuh) and the state held
+// as compensated (hi, lo) FP32 pairs of its 30 variables.
+//
+//   cell   : per cell, both phases' flux and wave-speed bounds from the (hi, lo)
+//            state (float-float islands in cons2prim); block max of the wave speed
+//            -> one atomicMax on the step's max-lambda slot (main.jl:204-212);
+//   face   : per face, the path-conservative HLL fluctuations (NumFluxes.jl:85-132)
+//            or the LxF face with D+- from the Gauss-Lobatto path integral
+//            (NumFluxes.jl:25-60), in FP32;
+//   update : dt = cfl dx / max lambda (FP64), t += dt, and per updated cell the
+//            increment -dt/dx ((F_r - F_l) + (D-_{i+1/2} + D+_{i-1/2})) added to
+//            the (hi, lo) pair with a two-sum (main.jl:30-60).
+#include "hyp_internal.cuh"
+#include "hyp_mixed_tile.cuh"
+#include "hyp_physics_mph_mixed.cuh"
+
+namespace hyp {
+
+__device__ __forceinline__ void record_err2m(DevState* S, int code, long long cell) {
+  if (atomicCAS(&S->err_code, 0, code) == 0) S->err_cell = cell;
+}
+
+__global__ void __launch_bounds__(kBlock) cell2_mixed_kernel(const float* __restrict__ Qh,
+                                                             const float* __restrict__ Ql, int64_t pitch, int64_t n,
+                                                             Eos2M E, float* __restrict__ F, int64_t fpitch,
+                                                             float* __restrict__ smin, float* __restrict__ smax,
+                                                             unsigned long long* lam_slot, const double* t_now,
+                                                             double t_end, DevState* S) {
+  if (!(*t_now < t_end)) return;
+  const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  float l = 0.0f;
+  if (i < n) {
+    float qh[30], ql[30], f[30];
+    for (int v = 0; v < 30; ++v) {
+      qh[v] = Qh[v * pitch + i];
+      ql[v] = Ql[v * pitch + i];
+    }
+    float lo = 0.0f, hi = 0.0f;
+    int st = cell2_mixed(E, qh, ql, f, lo, hi);
+    for (int v = 0; v < 30; ++v) F[v * fpitch + i] = f[v];
+    smin[i] = lo;
+    smax[i] = hi;
+    l = fmaxf(fabsf(lo), fabsf(hi));
+    if (!(l <= 3.0e38f)) st |= HYP_CELL_NONFINITE;
+    if (st) record_err2m(S, st, i);
+  }
+  const float m = mixed_block_max<kBlock>(l);
+  if (threadIdx.x == 0) atomicMax(lam_slot, (unsigned long long)__double_as_longlong((double)m));
+}
+
+constexpr int kFaceBlockM = 64;
+
+__device__ __forceinline__ void load_face_states(const float* Qh, int64_t pitch, const float* F, int64_t fpitch,
+                                                 int64_t L, int64_t R, float* QL, float* QR, float* fl, float* fr) {
+  for (int v = 0; v < 30; ++v) {
+    QL[v] = Qh[v * pitch + L];
+    QR[v] = Qh[v * pitch + R];
+    fl[v] = F[v * fpitch + L];
+    fr[v] = F[v * fpitch + R];
+  }
+}
+
+__global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
+    const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, Quad6F qd, const float* __restrict__ F,
+    int64_t fpitch, const float* __restrict__ smin, const float* __restrict__ smax, float* __restrict__ DM,
+    float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
+  if (!(*t_now < t_end)) return;
+  const int64_t f = (int64_t)blockIdx.x * kFaceBlockM + threadIdx.x;  // face between cells f-1 and f
+  if (f > n) return;
+  const int64_t nf = n + 1;
+  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+  float dm[30], dp[30];
+  if (L == R) {  // boundary face with a zero-gradient ghost: no jump, no fluctuation
+    for (int v = 0; v < 30; ++v) dm[v] = dp[v] = 0.0f;
+  } else {
+    float QL[30], QR[30], fl[30], fr[30];
+    load_face_states(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
+    const int st = hll_face2_m(E, qd, QL, QR, fl, fr, smin[L], smax[R], dm, dp);
+    if (st) record_err2m(S, st, R);
+  }
+  for (int v = 0; v < 30; ++v) {
+    DM[v * nf + f] = dm[v];
+    DP[v * nf + f] = dp[v];
+  }
+}
+
+__global__ void __launch_bounds__(kFaceBlockM) face2_lxf_mixed_kernel(
+    const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, Quad6F lobatto, const float* __restrict__ F,
+    int64_t fpitch, const unsigned long long* lam_now, double cfl, double dx, float* __restrict__ FF,
+    float* __restrict__ DM, float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
+  if (!(*t_now < t_end)) return;
+  const int64_t f = (int64_t)blockIdx.x * kFaceBlockM + threadIdx.x;
+  if (f > n) return;
+  const int64_t nf = n + 1;
+  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+  const double lmax = __longlong_as_double((long long)*lam_now);
+  const double dt = (cfl * dx) / lmax;
+  const float lam = (float)(dx / dt);  // lambda = dx/dt (main.jl:223)
+  float QL[30], QR[30], fl[30], fr[30], ff_[30], dm[30], dp[30];
+  load_face_states(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
+  const int st = lxf_face2_m(E, lobatto, QL, QR, fl, fr, lam, ff_, dm, dp);
+  if (st) record_err2m(S, st, R);
+  for (int v = 0; v < 30; ++v) {
+    FF[v * nf + f] = ff_[v];
+    DM[v * nf + f] = dm[v];
+    DP[v * nf + f] = dp[v];
+  }
+}
+
+__global__ void __launch_bounds__(kBlock) update2_mixed_kernel(
+    const float* __restrict__ Qh, const float* __restrict__ Ql, float* __restrict__ Qh_out, float* __restrict__ Ql_out,
+    int64_t pitch, int64_t n, const float* __restrict__ FF, const float* __restrict__ DM, const float* __restrict__ DP,
+    const unsigned long long* lam_in, unsigned long long* lam_next, const double* t_in, double* t_out,
+    long long* steps, double t_end, double cfl, double dx, int bc) {
+  const double tn = *t_in;
+  const bool active = tn < t_end;
+  const double lmax = __longlong_as_double((long long)*lam_in);
+  const double dt = (cfl * dx) / lmax;
+  const float dtdx = (float)(dt / dx);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    *t_out = active ? tn + dt : tn;
+    *lam_next = 0ull;
+    if (active) *steps += 1;
+  }
+  if (!active) return;
+  const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (i >= n) return;
+  const int64_t nf = n + 1;
+  const bool frozen = bc == HYP_BC_FROZEN && (i == 0 || i == n - 1);
+  for (int v = 0; v < 30; ++v) {
+    float h = Qh[v * pitch + i], l = Ql[v * pitch + i];
+    if (!frozen) {
+      const float fr = FF ? FF[v * nf + i + 1] : 0.0f, fl = FF ? FF[v * nf + i] : 0.0f;
+      const float delta = -dtdx * ((fr - fl) + (DM[v * nf + i + 1] + DP[v * nf + i]));
+      const ff q = ff_add_f(ff{h, l}, delta);
+      h = q.hi;
+      l = q.lo;
+    }
+    Qh_out[v * pitch + i] = h;
+    Ql_out[v * pitch + i] = l;
+  }
+}
+
+static inline unsigned grid_m(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
+
+static Quad6F to_f(const Quad6D& q) {
+  Quad6F r;
+  for (int i = 0; i < 6; ++i) {
+    r.x[i] = (float)q.x[i];
+    r.w[i] = (float)q.w[i];
+  }
+  return r;
+}
+
+static Eos2M eos2m(const hyp_ctx* c) {
+  Eos2M E;
+  E.m[0] = make_eos_mixed(c->eos[0]);
+  E.m[1] = make_eos_mixed(c->eos[1]);
+  return E;
+}
+
+cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end) {
+  cell2_mixed_kernel<<<grid_m(c->n, kBlock), kBlock, 0, c->stream>>>(c->Qh[p], c->Ql[p], c->mpitch, c->n, eos2m(c),
+                                                                      c->F32, c->n, c->smin32, c->smax32, lam_slot,
+                                                                      t_now, t_end, c->st);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
+  if (c->cfg.flux == HYP_FLUX_LXF) {
+    const double dx = c->cfg.x_length / (double)c->n;
+    face2_lxf_mixed_kernel<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
+        c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->lobatto), c->F32, c->n, &c->st->lam_bits[p], c->cfg.cfl, dx,
+        c->FF32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
+  } else {
+    face2_hll_mixed_kernel<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
+        c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n, c->smin32, c->smax32, c->DM32, c->DP32,
+        &c->st->t[p], t_end, c->st);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_update2_mixed(hyp_ctx* c, int p, double t_end) {
+  const double dx = c->cfg.x_length / (double)c->n;
+  update2_mixed_kernel<<<grid_m(c->n, kBlock), kBlock, 0, c->stream>>>(
+      c->Qh[p], c->Ql[p], c->Qh[1 - p], c->Ql[1 - p], c->mpitch, c->n, c->FF32, c->DM32, c->DP32,
+      &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p], &c->st->t[1 - p], &c->st->steps, t_end,
+      c->cfg.cfl, dx, c->cfg.bc);
+  return cudaGetLastError();
+}
+
+}  // namespace hyp

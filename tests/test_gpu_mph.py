@@ -125,3 +125,75 @@ def test_twophase_uniform_state_preserved(hyp, orc):
         s.upload(Q0)
         s.step(max_steps=3)
         assert np.array_equal(s.download(), Q0)
+
+
+def phase_densities(Q, rho0=8.93):
+    """rho_true of both phases, sqrt(det(alpha rho A / alpha) / rho0) (HyperelasticityMPh.jl:113-114)."""
+    out = []
+    for p in range(2):
+        a = Q[15 * p]
+        m = Q[15 * p + 6:15 * p + 15] / a
+        det = (m[0] * (m[4] * m[8] - m[5] * m[7]) - m[3] * (m[1] * m[8] - m[7] * m[2])
+               + m[6] * (m[1] * m[5] - m[4] * m[2]))
+        out.append(np.sqrt(det / rho0))
+    return out
+
+
+def l1_linf(a, b):
+    return np.sum(np.abs(a - b)) / np.sum(np.abs(b)), np.max(np.abs(a - b)) / np.max(np.abs(b))
+
+
+@pytest.mark.parametrize("flux", ["hll", "lxf"])
+@pytest.mark.parametrize("testcase", [4, 6, 7])
+def test_mixed_twophase_vs_fp64(hyp, orc, testcase, flux):
+    """Mixed-precision two-phase step (FP32 physics, compensated state, float-float
+    cons2prim islands) against the FP64 two-phase step: relative L1 error of each
+    phase's density <= 1e-6 after 100 steps of the reference's test cases."""
+    from hyperelasticsolver_gb300._cases import mph_case, initial_condition
+    nx, steps = 400, 100
+    pb = oracle_pb(orc, nx=nx, cfl=0.6)
+    Pl, Pr = mph_case(testcase)
+    Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, precision=prec, cfl=0.6) as s:
+            s.upload(Q0)
+            n, t = s.step(max_steps=steps)
+            assert n == steps
+            out[prec] = (s.download(), t)
+    assert abs(out["mixed"][1] - out["fp64"][1]) <= 1e-6 * out["fp64"][1]
+    errs = [l1_linf(a, b) for a, b in zip(phase_densities(out["mixed"][0]), phase_densities(out["fp64"][0]))]
+    print(f"mixed two-phase test case {testcase} ({flux}), {steps} steps: density L1/Linf per phase "
+          + ", ".join(f"{l1:.1e}/{li:.1e}" for l1, li in errs))
+    assert max(e[0] for e in errs) <= 1e-6
+
+
+@pytest.mark.parametrize("flux", ["hll", "lxf"])
+def test_mixed_twophase_smoothed_interface(hyp, orc, flux):
+    from hyperelasticsolver_gb300._cases import mph_interface_prims
+    nx, steps = 2048, 100
+    P = mph_interface_prims(hyp.Barton2009(), nx)
+    Q0 = np.ascontiguousarray(orc.prim2cons(oracle_pb(orc), P).T)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, precision=prec, cfl=0.5) as s:
+            s.upload(Q0)
+            s.step(max_steps=steps)
+            out[prec] = s.download()
+    errs = [l1_linf(a, b) for a, b in zip(phase_densities(out["mixed"]), phase_densities(out["fp64"]))]
+    print(f"mixed two-phase smoothed interface ({flux}), {steps} steps: density L1/Linf per phase "
+          + ", ".join(f"{l1:.1e}/{li:.1e}" for l1, li in errs))
+    assert max(e[0] for e in errs) <= 1e-6
+
+
+def test_mixed_twophase_uniform_state_preserved(hyp, orc):
+    rng = np.random.default_rng(8)
+    q = random_mph(orc, 1, rng)[0]
+    Q0 = np.ascontiguousarray(np.repeat(q[:, None], 1000, axis=1))
+    with hyp.Solver(eos_pair(hyp), 1000, model="multi", flux="hll", precision="mixed", bc="transmissive") as s:
+        s.upload(Q0)
+        Qa = s.download()  # the compensated pair holds the FP64 input to ~48 bits
+        s.step(max_steps=3)
+        Qb = s.download()
+    assert np.max(np.abs(Qa - Q0) / np.maximum(np.abs(Q0), 1e-300)) < 1e-13
+    assert np.array_equal(Qb, Qa)  # and does not move
