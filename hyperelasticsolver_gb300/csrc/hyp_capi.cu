@@ -297,7 +297,7 @@ static int collect_profile(hyp_ctx* c) {
     CK(cudaEventElapsedTime(&b, c->prof_ev[k + 1], c->prof_ev[k + 2]));
     c->timing.ms_cell += a;
     c->timing.n_cell += 1;
-    if (!mixed(c)) {
+    if (!mixed1(c)) {  // the single-phase mixed step is one kernel
       c->timing.ms_update += b;
       c->timing.n_update += 1;
     }

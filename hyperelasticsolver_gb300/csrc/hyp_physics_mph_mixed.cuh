@@ -1,12 +1,14 @@
 // hyp_physics_mph_mixed.cuh -- the two-phase physics of hyp_physics_mph.cuh in
 // FP32 for the mixed-precision two-phase step.
 //
-// Per phase, cons2prim (HyperelasticityMPh.jl:106-133) keeps its cancellation-
-// prone steps in float-float, as the single-phase mixed step does:
+// Per phase, cons2prim (HyperelasticityMPh.jl:106-133) of a cell's state keeps
+// its cancellation-prone steps in float-float, as the single-phase mixed step does:
 // det(alpha rho A) (with the lo parts of a compensated state through the
 // cofactors), rho_true = sqrt(det(rho A / alpha) / rho0), 1/(alpha rho_true),
 // alpha rho e = alpha rho E - |alpha rho u|^2 / (2 alpha rho_true), and
-// s - 1 = rho_true/rho0 - 1. Everything else -- the Finger tensor, stress,
+// s - 1 = rho_true/rho0 - 1. The states a face evaluates between its cells
+// (midpoint, Gauss nodes, Q_hll) are FP32 interpolants and go through a plain FP32
+// cons2prim. Everything else -- the Finger tensor, stress,
 // temperature, the non-conservative columns of B (HyperelasticityMPh.jl:178-250),
 // wave speeds, fluxes and the path-conservative HLL / LxF faces
 // (NumFluxes.jl:25-132) -- is FP32, statement for statement as in the FP64 forms.
@@ -130,11 +132,39 @@ __device__ __forceinline__ int cell2_mixed(const Eos2M& E, const float* qh, cons
   return st;
 }
 
+// cons2prim of one phase in plain FP32, for the states a face evaluates between
+// its two cells (midpoint, path nodes, Q_hll): these are FP32 interpolants, whose
+// own rounding the float-float islands could not undo.
+__device__ __forceinline__ int cons_to_prim_f2(const EosMixed& em, const float* q, PrimM2& P) {
+  const EosT<float>& e = em.f;
+  const float* m = q + 6;
+  const float ia = __frcp_rn(q[0]);
+  const float d = det3(m) * (ia * ia * ia);  // det(alpha rho A / alpha)
+  int st = d > 0.0f ? HYP_CELL_OK : HYP_CELL_NEG_DET;
+  const float rho = sqrtf(d * e.inv_rho0);
+  P.true_den = rho;
+  P.den = q[0] * rho;
+  const float idn = __frcp_rn(P.den);
+  for (int c = 0; c < 3; ++c) P.u[c] = q[2 + c] * idn;
+  P.E = q[5] * idn;
+  P.e_int = P.E - 0.5f * (P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2]);
+  for (int c = 0; c < 9; ++c) P.A[c] = m[c] * idn;
+  const float sf = rho * e.inv_rho0;
+  P.sm1 = sf - 1.0f;
+  P.k = kinematics_s<float>(P.A, sf, __frcp_rn(sf));
+  P.w = powers<float>(e, P.k);
+  P.w.Pam1 = e.default_exp ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
+  P.xm1 = entropy_xm1<float>(e, P.e_int, P.k, P.w);
+  P.rho_s = e.rho0 * sf;
+  if (!(P.e_int == P.e_int) || !(P.xm1 == P.xm1) || !isfinite(P.k.p)) st |= HYP_CELL_NONFINITE;
+  return st;
+}
+
 __device__ __forceinline__ int speeds2_m(const Eos2M& E, const float* Q, float& smin, float& smax) {
   int st = 0;
   for (int p = 0; p < 2; ++p) {
     PrimM2 P;
-    st |= cons_to_prim_m2(E.m[p], Q + 15 * p, nullptr, P);
+    st |= cons_to_prim_f2(E.m[p], Q + 15 * p, P);
     const StressCT<float> c = stress_coeffs<float>(E.m[p].f, P.k, P.w, P.xm1);
     const float cm = phase_cmax_m2(E.m[p].f, P, c);
     const float lo = P.u[0] - cm, hi = P.u[0] + cm;
@@ -151,7 +181,7 @@ struct PhaseBM {
 
 __device__ __forceinline__ int phase_b_m(const EosMixed& em, const float* q, PhaseBM& b) {
   PrimM2 P;
-  const int st = cons_to_prim_m2(em, q, nullptr, P);
+  const int st = cons_to_prim_f2(em, q, P);
   const StressCT<float> c = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
   stress_row0<float>(P.rho_s, P.k, c, b.K0);
   b.T = em.f.t0 * P.w.Pg * (P.xm1 + 1.0f);

@@ -196,4 +196,7 @@ def test_mixed_twophase_uniform_state_preserved(hyp, orc):
         s.step(max_steps=3)
         Qb = s.download()
     assert np.max(np.abs(Qa - Q0) / np.maximum(np.abs(Q0), 1e-300)) < 1e-13
-    assert np.array_equal(Qb, Qa)  # and does not move
+    # With Q_l = Q_r the FP32 Q_hll differs from Q by rounding, so the two path integrals
+    # through it cancel only to rounding: the state stays uniform to that level.
+    scale = np.max(np.abs(Qa), axis=1, keepdims=True)
+    assert np.max(np.abs(Qb - Qa) / np.maximum(scale, 1e-30)) < 1e-9
