@@ -101,6 +101,7 @@ __device__ __forceinline__ double block_sum(double v, double* sh) {
 
 struct AdjArgs {
   const double* Q;     // Q_n [14][n]
+  const double* Qn;    // Q_{n+1} [14][n] (the step's result, kept by the recompute)
   const double* F;     // fluxes of Q_n [11][n]
   const double* lam;   // wave speeds of Q_n [n]
   const unsigned long long* lmax;  // max wave speed of Q_n (bits)
@@ -118,35 +119,38 @@ struct AdjArgs {
 
 __device__ __forceinline__ bool updated(int64_t i, int64_t n, int trans) { return trans || (i > 0 && i < n - 1); }
 
-// Face (a, b) value of variable v from the stored fluxes.
-__device__ __forceinline__ double face_val(const AdjArgs& g, int v, int64_t a, int64_t b, double lf) {
-  const int64_t n = g.n;
-  const int s = flux_slot1(v);
-  const double fa = s >= 0 ? g.F[s * n + a] : 0.0, fb = s >= 0 ? g.F[s * n + b] : 0.0;
-  return 0.5 * (fa + fb) - 0.5 * lf * (g.Q[v * n + b] - g.Q[v * n + a]);
-}
 __device__ __forceinline__ double face_lambda(double la, double lb) { return la > lb ? la : lb; }
 
 __device__ __forceinline__ double dtdx_of(const AdjArgs& g, double lmax) { return ((g.cfl * g.dx) / lmax) / g.dx; }
 
-// Partial sums of rb_n = -sum Qb'_i . (F_{i+1/2} - F_{i-1/2}), and the arg-max cell.
+// Partial sums of r * rb_n, where rb_n = -sum_{updated i} Qb'_i . (F_{i+1/2} - F_{i-1/2})
+// and, for an updated cell, F_{i+1/2} - F_{i-1/2} = (Q_i - Q'_i) / r with Q' the step's
+// result: r rb_n = sum Qb'_i . (Q'_i - Q_i), a 14-term dot product per cell. Also the
+// arg-max cell (smallest index whose wave speed equals the step's max), one atomicMin
+// per block.
 __global__ void __launch_bounds__(256) adj_dtdx_kernel(AdjArgs g) {
   __shared__ double sh[8];
+  __shared__ int shi[8];
   const int64_t n = g.n;
   const double lmax = __longlong_as_double((long long)*g.lmax);
   double acc = 0.0;
+  int imin = INT_MAX;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    const double li = g.lam[i];
-    if (li == lmax) atomicMin(g.amax_rd, (int)i);
+    if (g.lam[i] == lmax && (int)i < imin) imin = (int)i;
     if (!updated(i, n, g.trans)) continue;
-    const int64_t il = i > 0 ? i - 1 : 0, ir = i < n - 1 ? i + 1 : n - 1;
-    const double lL = face_lambda(g.lam[il], li), lR = face_lambda(li, g.lam[ir]);
     double s = 0.0;
-    for (int v = 0; v < 14; ++v) s += g.Qb1[v * n + i] * (face_val(g, v, i, ir, lR) - face_val(g, v, il, i, lL));
-    acc -= s;
+    for (int v = 0; v < 14; ++v) s += g.Qb1[v * n + i] * (g.Qn[v * n + i] - g.Q[v * n + i]);
+    acc += s;
   }
-  const double b = block_sum<256>(acc, sh);
-  if (threadIdx.x == 0) g.rpart[blockIdx.x] = b;
+  for (int o = 16; o > 0; o >>= 1) imin = min(imin, __shfl_xor_sync(0xffffffffu, imin, o));
+  if ((threadIdx.x & 31) == 0) shi[threadIdx.x >> 5] = imin;
+  const double b = block_sum<256>(acc, sh);  // its barriers also publish shi
+  if (threadIdx.x == 0) {
+    g.rpart[blockIdx.x] = b;
+    int m = INT_MAX;
+    for (int w = 0; w < 8; ++w) m = min(m, shi[w]);
+    if (m != INT_MAX) atomicMin(g.amax_rd, m);
+  }
 }
 
 __global__ void __launch_bounds__(kAdjBlock) adj_cell_kernel(AdjArgs g, EosC e) {
@@ -159,7 +163,8 @@ __global__ void __launch_bounds__(kAdjBlock) adj_cell_kernel(AdjArgs g, EosC e) 
     double s = 0.0;
     for (int k = threadIdx.x; k < g.part_grid; k += 32) s += g.rpart[k];
     for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
-    if (threadIdx.x == 0) s_lamb_max = -s * r / lmax;  // d r / d lmax = -r / lmax
+    // the partials sum to r rb_n; d r / d lmax = -r / lmax, so dL/d lmax = -(r rb_n) / lmax
+    if (threadIdx.x == 0) s_lamb_max = -s / lmax;
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) *g.amax_clr = INT_MAX;
   __syncthreads();
@@ -203,7 +208,12 @@ __global__ void __launch_bounds__(kAdjBlock) adj_cell_kernel(AdjArgs g, EosC e) 
     }
     if (il != i && takeL) lamb -= 0.5 * dL;
     if (ir != i && takeR) lamb -= 0.5 * dR;
-    cell_vjp(e, q, fb, lamb, qb, eb);
+    bool any = lamb != 0.0;
+#pragma unroll
+    for (int v = 0; v < 14; ++v) any |= fb[v] != 0.0;
+    // where the face adjoints vanish (a region where the adjoint field is constant) the
+    // VJP adds exact zeros: skip it
+    if (any) cell_vjp(e, q, fb, lamb, qb, eb);
 #pragma unroll
     for (int v = 0; v < 14; ++v) g.Qb0[v * n + i] = qb[v];
   }
@@ -389,6 +399,9 @@ extern "C" int hyp_adjoint(hyp_ctx* c, const double* dL_dQ_final, double* dL_dQ0
       const int step = a + k;
       AdjArgs g;
       g.Q = t->seg_Q + (size_t)k * 14 * n;
+      // the step's result: the next segment state, the next checkpoint, or the final state
+      g.Qn = k + 1 < L ? t->seg_Q + (size_t)(k + 1) * 14 * n
+                       : (s + 1 < n_seg ? t->ckpt + (size_t)(s + 1) * 14 * n : c->Q[c->cur]);
       g.F = t->seg_F + (size_t)k * kNFlux1 * n;
       g.lam = t->seg_lam + (size_t)k * n;
       g.lmax = &t->seg_lmax[k];
