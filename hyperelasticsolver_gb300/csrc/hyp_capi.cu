@@ -40,6 +40,7 @@ static int free_ctx(hyp_ctx* c) {
   cudaSetDevice(c->device);
   if (c->stream) cudaStreamSynchronize(c->stream);
   free_tape(c);
+  free_snap(c);
   for (auto& g : c->graph)
     if (g) cudaGraphExecDestroy(g);
   for (int p = 0; p < 2; ++p) cudaFree(c->Q[p]);

@@ -56,6 +56,7 @@ struct StepTiming {
 
 namespace hyp {
 struct AdjTape;
+struct SnapBuf;
 // Mixed-precision state of one parity: kMixedRows rows of a pitch of floats,
 // rows 0-13 hi parts, 14-27 lo parts, 28 the cell's wave speed, 29-31 its
 // island outputs. The two parities are consecutive blocks of one allocation, so
@@ -122,6 +123,7 @@ struct hyp_ctx {
   std::string err;
   int64_t err_cell = -1;
   hyp::AdjTape* tape = nullptr;  // checkpoints and buffers of the adjoint (hyp_adjoint.cu)
+  hyp::SnapBuf* snap = nullptr;  // snapshot buffers and writer (hyp_snapshot.cu)
 };
 
 // Context helpers shared by the C-ABI files (hyp_capi.cu): record an error
@@ -134,6 +136,8 @@ int ctx_check_cell_error(hyp_ctx* c);
 namespace hyp {
 // adjoint buffers of a context (hyp_adjoint.cu)
 void free_tape(hyp_ctx* c);
+// snapshot buffers of a context (hyp_snapshot.cu)
+void free_snap(hyp_ctx* c);
 // single-phase FP64 step kernels (defined in hyp_step1.cu)
 __global__ void __launch_bounds__(kBlock) cell1_f64_kernel(const double* __restrict__ Q, int64_t n, EosC e,
                                                            double* __restrict__ F, double* __restrict__ lam,

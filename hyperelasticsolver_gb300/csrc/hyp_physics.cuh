@@ -405,6 +405,31 @@ HYP_HD double phase_cmax(const EosC& e, const Prim& P, const StressC& c) {
   return sqrt(spectral_radius(om));
 }
 
+// cons2prim / prim2cons of one phase (HyperelasticityMPh.jl:106-133, 63-90):
+// q[15] = [alpha, alpha rho, alpha rho u(3), alpha rho E, alpha rho A(9)],
+// p[15] = [alpha, rho_true, u(3), S, A(9)].
+HYP_HD void phase_cons2prim(const EosC& e, const double* q, double* p) {
+  Prim P;
+  cons_to_prim(e, q[0], q + 2, q[5], q + 6, P);
+  p[0] = q[0];
+  p[1] = P.true_den;
+  for (int c = 0; c < 3; ++c) p[2 + c] = P.u[c];
+  p[5] = e.cv * log(P.xm1 + 1.0);  // S = cv log x (EquationsOfState.jl:155)
+  for (int c = 0; c < 9; ++c) p[6 + c] = P.A[c];
+}
+HYP_HD void phase_prim2cons(const EosC& e, const double* p, double* q) {
+  double den = p[0] * p[1];
+  Kin k = kinematics(p + 6, det3(p + 6));
+  Pows w = powers(e, k);
+  double eint = e_cold(e, w) + e.cvt0 * w.Pg * (exp(p[5] / e.cv) - 1.0) + e_shear(e, k, w);
+  double ek = 0.5 * (p[2] * p[2] + p[3] * p[3] + p[4] * p[4]);
+  q[0] = p[0];
+  q[1] = den;
+  for (int c = 0; c < 3; ++c) q[2 + c] = den * p[2 + c];
+  q[5] = den * (eint + ek);
+  for (int c = 0; c < 9; ++c) q[6 + c] = den * p[6 + c];
+}
+
 // ---- function-level forms with the reference's signatures -----------------
 
 // stress(eos, ent, F) (EquationsOfState.jl:179-190): full 3x3, column-major.

@@ -1,6 +1,8 @@
 """The explicit time loop of main.jl:202-241 on the GPU (one context = one problem)."""
 import ctypes
+import glob
 import math
+import os
 
 import numpy as np
 
@@ -93,6 +95,31 @@ class Solver:
                                          ctypes.byref(nu)), self._h, "hyp_last_timing")
         return {"ms_total": a.value, "ms_cell": b.value, "n_cell": nc.value, "ms_update": d.value,
                 "n_update": nu.value}
+
+    # ---- snapshots and restart (main.jl:62-95, 174-198, 233-237) ----
+    def snapshot(self):
+        """Primitive states of the current state, (15 or 30, nx): per phase alpha, rho, u(3), S, A(9)."""
+        cols = 15 if self.nvar == 14 else 30
+        P = np.empty((cols, self.nx))
+        L.check(L.load().hyp_snapshot(self._h, L.ptr(P)), self._h, "hyp_snapshot")
+        return P
+
+    def save_snapshot(self, path):
+        """Write the current state as the reference's save_data file (tab-separated prims)."""
+        L.check(L.load().hyp_save_snapshot(self._h, os.fsencode(path)), self._h, "hyp_save_snapshot")
+
+    def load_snapshot(self, path, t0=0.0):
+        """Make a save_data file's state the current state at time t0 (read_data + prim2cons)."""
+        L.check(L.load().hyp_load_snapshot(self._h, os.fsencode(path), float(t0)), self._h, "hyp_load_snapshot")
+
+    def run_logged(self, directory, t_end=math.inf, max_steps=0, log_freq=100, first_step=0):
+        """The main.jl loop with logging: writes directory/sol_%06i.csv for the current state and
+        after every step whose number is a multiple of log_freq. Returns (steps taken, t)."""
+        sd = ctypes.c_int(0)
+        t = ctypes.c_double(0.0)
+        L.check(L.load().hyp_run_logged(self._h, float(t_end), int(max_steps), int(log_freq), os.fsencode(directory),
+                                        int(first_step), ctypes.byref(sd), ctypes.byref(t)), self._h, "hyp_run_logged")
+        return sd.value, t.value
 
     # ---- adjoint (single-phase FP64 Rusanov) ----
     def record(self, n_steps, ckpt_every=50):
@@ -215,3 +242,13 @@ class Batch:
     def problem(self, Q, p):
         """Columns of problem p in a SoA batch state."""
         return Q[:, self.offsets[p]:self.offsets[p + 1]]
+
+
+def last_snapshot(directory, dt):
+    """The restart point of main.jl:181-187: the last sol_*.csv in `directory`, its step
+    number and the time step_number * dt. Returns (path, step, t) or None if there is none."""
+    files = sorted(glob.glob(os.path.join(directory, "sol_*.csv")))
+    if not files:
+        return None
+    step = int(os.path.basename(files[-1]).split(".")[0].split("_")[1])
+    return files[-1], step, step * dt

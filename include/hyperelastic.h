@@ -184,6 +184,24 @@ int hyp_adjoint_timing(const hyp_ctx* ctx, double* ms_record, double* ms_recompu
    main.jl:71 writes), and dL/dQ (host [14][n], may be NULL). */
 int hyp_density_misfit(hyp_ctx* ctx, const double* rho_target, double* loss, double* dL_dQ);
 
+/* ---- snapshots and restart (main.jl:62-95, 108, 174-198, 233-237) ---------- */
+/* cons2prim of the current state (per phase [alpha, rho, u(3), S, A(9)]) to host
+   P [cols][n], cols = 15 (single phase, alpha = 1) or 30. */
+int hyp_snapshot(hyp_ctx* ctx, double* P);
+/* The reference's save_data file of the current state: tab-separated header
+   a1 r1 u11 u21 u31 S1 F111 ... F331 [a2 ... F332], one row per cell, shortest
+   round-trip numbers in Julia's layout. */
+int hyp_save_snapshot(hyp_ctx* ctx, const char* path);
+/* read_data + prim2cons (main.jl:79-95, 186-191): the file's prims become the
+   current state at time t0 (the reference restarts at t = step * dt). */
+int hyp_load_snapshot(hyp_ctx* ctx, const char* path, double t0);
+/* The main.jl time loop with logging: saves dir/sol_%06i.csv for the current
+   state (step number first_step) and after every step whose number is a multiple
+   of log_freq, until t >= t_end or max_steps steps (either may be unbounded,
+   not both). Copies and file writing overlap the following steps. */
+int hyp_run_logged(hyp_ctx* ctx, double t_end, int max_steps, int log_freq, const char* dir, int64_t first_step,
+                   int* steps_done, double* t_out);
+
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);
 int hyp_host_free(void* p);
