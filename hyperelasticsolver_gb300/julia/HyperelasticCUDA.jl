@@ -82,16 +82,28 @@ module HyperelasticityMPh
 end
 
 module NumFluxes
-  import ..libhyp, ..check, ..config, ..ConfigC, ..HYP_MODEL_SINGLE
-  "lxf(eos, Q_l, Q_r, lambda) for single-phase cells (NumFluxes.jl:25-60): (cons, D-, D+)"
+  import ..libhyp, ..check, ..config, ..ConfigC, ..HYP_MODEL_SINGLE, ..HYP_MODEL_MULTI, ..HYP_FLUX_LXF, ..HYP_FLUX_HLL
+  """lxf(eos, Q_l, Q_r, lambda) (NumFluxes.jl:25-60): (cons, D-, D+). `eos` one Barton2009C:
+  single-phase cells (n, 14); a pair: two-phase cells (n, 30) with the Gauss-Lobatto D+-."""
   function lxf(eos, Ql::Matrix{Float64}, Qr::Matrix{Float64}, lam::Vector{Float64})
     n = size(Ql, 1)
     cons, dm, dp = similar(Ql), similar(Ql), similar(Ql)
-    cfg = Ref(config(eos, HYP_MODEL_SINGLE))
+    cfg = Ref(eos isa Tuple ? config(eos, HYP_MODEL_MULTI; flux=HYP_FLUX_LXF) : config(eos, HYP_MODEL_SINGLE))
     check(ccall((:hyp_eval_lxf, libhyp), Cint,
                 (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
                 cfg, Ql, Qr, lam, cons, dm, dp, n), "lxf")
     cons, dm, dp
+  end
+  """hll(eos, Q_l, Q_r, eigvals) for two-phase cells (n, 30) (NumFluxes.jl:70-132): (zeros, D-, D+).
+  The speed bounds come from Q_l and Q_r as main.jl:225 passes them; `eigvals` is not used."""
+  function hll(eos::Tuple, Ql::Matrix{Float64}, Qr::Matrix{Float64}, eigvals=nothing)
+    n = size(Ql, 1)
+    dm, dp = similar(Ql), similar(Ql)
+    cfg = Ref(config(eos, HYP_MODEL_MULTI; flux=HYP_FLUX_HLL))
+    check(ccall((:hyp_eval_hll, libhyp), Cint,
+                (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64), cfg, Ql, Qr, dm, dp, n),
+          "hll")
+    zeros(size(Ql)), dm, dp
   end
 end
 
@@ -122,6 +134,80 @@ function step!(s::Solver; max_steps::Integer=0, T::Float64=Inf)
   check(ccall((:hyp_step, libhyp), Cint, (Ptr{Cvoid}, Cint, Float64, Ref{Cint}, Ref{Float64}), s.h, max_steps, T, n, t),
         "hyp_step", s.h)
   (n[], t[])
+end
+
+# ---- snapshots and restart (main.jl:62-95, 108, 174-198, 233-237) ----
+"save_data(s, fname): the reference's save_data file of the current state (device cons2prim)"
+save_data(s::Solver, fname::AbstractString) =
+  check(ccall((:hyp_save_snapshot, libhyp), Cint, (Ptr{Cvoid}, Cstring), s.h, fname), "hyp_save_snapshot", s.h)
+"read_data!(s, fname, t0): read_data + prim2cons; the file's state becomes current at t0 (main.jl:186-191)"
+read_data!(s::Solver, fname::AbstractString, t0::Float64) =
+  check(ccall((:hyp_load_snapshot, libhyp), Cint, (Ptr{Cvoid}, Cstring, Float64), s.h, fname, t0),
+        "hyp_load_snapshot", s.h)
+"run_logged!(s, dir; T, max_steps, log_freq, step_num): main.jl:196-241 with sol_%06i.csv every log_freq steps"
+function run_logged!(s::Solver, dir::AbstractString; T::Float64=Inf, max_steps::Integer=0, log_freq::Integer=100,
+                     step_num::Integer=0)
+  n, t = Ref{Cint}(0), Ref{Float64}(0.0)
+  check(ccall((:hyp_run_logged, libhyp), Cint,
+              (Ptr{Cvoid}, Float64, Cint, Cint, Cstring, Int64, Ref{Cint}, Ref{Float64}),
+              s.h, T, max_steps, log_freq, dir, step_num, n, t), "hyp_run_logged", s.h)
+  (n[], t[])
+end
+
+# ---- batches of independent single-phase problems ----
+"Many independent single-phase problems of uneven size stepped in lockstep (one CUDA graph per call)."
+mutable struct Batch
+  h::Ptr{Cvoid}
+  total::Int64
+  function Batch(cfg::ConfigC, offsets::Vector{Int64})
+    r = Ref{Ptr{Cvoid}}(C_NULL)
+    rc = ccall((:hyp_batch_create, libhyp), Cint, (Ref{ConfigC}, Ptr{Int64}, Cint, Ref{Ptr{Cvoid}}),
+               Ref(cfg), offsets, length(offsets) - 1, r)
+    rc == 0 || throw(HypError(rc, "hyp_batch_create"))
+    b = new(r[], offsets[end])
+    finalizer(x -> ccall((:hyp_batch_destroy, libhyp), Cint, (Ptr{Cvoid},), x.h), b)
+  end
+end
+bcheck(rc, b::Batch, what) = rc == 0 ? nothing :
+  throw(HypError(rc, what * ": " * unsafe_string(ccall((:hyp_batch_last_error, libhyp), Cstring, (Ptr{Cvoid},), b.h))))
+upload!(b::Batch, Q::Matrix{Float64}, t0=0.0) =
+  bcheck(ccall((:hyp_batch_upload, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Float64), b.h, Q, t0), b, "hyp_batch_upload")
+function download(b::Batch)
+  Q = Matrix{Float64}(undef, b.total, 14)
+  bcheck(ccall((:hyp_batch_download, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}), b.h, Q), b, "hyp_batch_download")
+  Q
+end
+step!(b::Batch, n_steps::Integer; T::Float64=Inf) =
+  bcheck(ccall((:hyp_batch_step, libhyp), Cint, (Ptr{Cvoid}, Cint, Float64), b.h, n_steps, T), b, "hyp_batch_step")
+function autotune!(b::Batch; trial_steps::Integer=10)
+  chosen, ms = Ref{Cint}(-1), zeros(6)
+  bcheck(ccall((:hyp_batch_autotune, libhyp), Cint, (Ptr{Cvoid}, Cint, Ref{Cint}, Ptr{Float64}), b.h, trial_steps,
+               chosen, ms), b, "hyp_batch_autotune")
+  (chosen[], ms)
+end
+
+# ---- the adjoint of a single-phase FP64 Rusanov run ----
+"record!(s, n_steps; K): n_steps steps that keep a checkpoint every K steps (the rrule's forward pass)"
+function record!(s::Solver, n_steps::Integer; K::Integer=50)
+  t = Ref{Float64}(0.0)
+  check(ccall((:hyp_adjoint_record, libhyp), Cint, (Ptr{Cvoid}, Cint, Cint, Ref{Float64}), s.h, n_steps, K, t),
+        "hyp_adjoint_record", s.h)
+  t[]
+end
+"adjoint(s, dQ): (dL/dQ0, (dL/db0sq, dL/dk0)) of the recorded run from dL/dQ of its final state"
+function adjoint(s::Solver, dQ::Matrix{Float64})
+  dQ0 = similar(dQ)
+  de = zeros(2)
+  check(ccall((:hyp_adjoint, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}), s.h, dQ, dQ0, de),
+        "hyp_adjoint", s.h)
+  dQ0, (de[1], de[2])
+end
+"evolve(cfg, Q0, n_steps; K): the final state of n_steps FP64 steps from Q0 (differentiable, see rrule.jl)"
+function evolve(cfg::ConfigC, Q0::Matrix{Float64}, n_steps::Integer; K::Integer=50)
+  s = Solver(cfg)
+  upload!(s, Q0)
+  step!(s; max_steps=n_steps)
+  download(s)
 end
 
 end # module HyperelasticCUDA
