@@ -46,7 +46,9 @@ def noncons_flux(eos, Q):
 
 
 def initial_states(eos, testcase):
-    """Left/right conservative states of the Riemann test cases (HyperelasticityMPh.jl:275-426)."""
-    from ._cases import mph_case
-    Pl, Pr = mph_case(testcase)
-    return prim2cons_mph(eos, Pl), prim2cons_mph(eos, Pr)
+    """Left/right conservative states of the Riemann test cases 1-7 and 10
+    (HyperelasticityMPh.jl:275-426), built by hyp_initial_states."""
+    Ql, Qr = np.empty(30), np.empty(30)
+    L.check(L.load().hyp_initial_states(_cfg(eos), int(testcase), L.ptr(Ql), L.ptr(Qr)),
+            what=f"initial_states({testcase})")
+    return Ql, Qr

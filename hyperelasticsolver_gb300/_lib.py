@@ -108,6 +108,9 @@ _SIGS = {
     "hyp_load_snapshot": ([ctypes.c_void_p, ctypes.c_char_p, ctypes.c_double], ctypes.c_int),
     "hyp_run_logged": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int, ctypes.c_char_p, _i64,
                         ctypes.POINTER(ctypes.c_int), _dp], ctypes.c_int),
+    "hyp_initial_states": ([ctypes.POINTER(ConfigC), ctypes.c_int, _dp, _dp], ctypes.c_int),
+    "hyp_init_riemann": ([ctypes.c_void_p, _dp, _dp], ctypes.c_int),
+    "hyp_init_tanh": ([ctypes.c_void_p, _dp, _dp, ctypes.c_double], ctypes.c_int),
     "hyp_host_alloc": ([ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "hyp_host_free": ([ctypes.c_void_p], ctypes.c_int),
     "hyp_eval_finger": ([_dp, _dp, _i64], ctypes.c_int),

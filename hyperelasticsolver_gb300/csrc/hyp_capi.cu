@@ -204,20 +204,18 @@ static int check_cell_error(hyp_ctx* c) {
   return set_err(c, HYP_ERR_NONFINITE, buf);
 }
 
-extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_vars, double t0) {
-  if (!c || !Q) return HYP_ERR_INVALID;
-  if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_upload: size mismatch");
-  CK(cudaSetDevice(c->device));
-  const size_t bytes = (size_t)n_vars * n_cells * sizeof(double);
+// Where an FP64 state [nvar][n] goes before ctx_finish_install makes it current:
+// the FP64 buffer of parity 0, or the mixed contexts' staging block.
+double* ctx_install_target(hyp_ctx* c) { return mixed(c) ? (double*)c->Qh[1] : c->Q[0]; }
+
+// Makes the FP64 state at ctx_install_target the current state at time t0 (splits
+// it into (hi, lo) pairs for mixed precision) and resets the loop control.
+int ctx_finish_install(hyp_ctx* c, double t0) {
   std::memset(c->st_host, 0, sizeof(DevState));
   c->st_host->t[0] = c->st_host->t[1] = t0;
   CK(cudaMemcpyAsync(c->st, c->st_host, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
-  if (!mixed(c)) {
-    CK(cudaMemcpyAsync(c->Q[0], Q, bytes, cudaMemcpyHostToDevice, c->stream));
-  } else {
-    double* stage = (double*)c->Qh[1];
-    CK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, c->stream));
-    CK(launch_split(c, stage, c->Qh[0], c->Ql[0]));
+  if (mixed(c)) {
+    CK(launch_split(c, ctx_install_target(c), c->Qh[0], c->Ql[0]));
     if (mixed1(c)) CK(launch_lam1_mixed(c, 0, &c->st->lam_slots[0]));
   }
   int rc = sync_state(c);
@@ -227,6 +225,15 @@ extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_va
   c->steps_host = 0;
   c->err_cell = -1;
   return check_cell_error(c);
+}
+
+extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_vars, double t0) {
+  if (!c || !Q) return HYP_ERR_INVALID;
+  if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_upload: size mismatch");
+  CK(cudaSetDevice(c->device));
+  const size_t bytes = (size_t)n_vars * n_cells * sizeof(double);
+  CK(cudaMemcpyAsync(ctx_install_target(c), Q, bytes, cudaMemcpyHostToDevice, c->stream));
+  return ctx_finish_install(c, t0);
 }
 
 extern "C" int hyp_download(hyp_ctx* c, double* Q, int64_t n_cells, int n_vars) {

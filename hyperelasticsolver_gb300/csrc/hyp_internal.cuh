@@ -132,6 +132,10 @@ struct hyp_ctx {
 int ctx_set_err(hyp_ctx* c, int code, const std::string& msg);
 int ctx_sync_state(hyp_ctx* c);
 int ctx_check_cell_error(hyp_ctx* c);
+// Installing a state generated on the device (hyp_capi.cu): write it, FP64 [nvar][n],
+// to ctx_install_target(c), then call ctx_finish_install(c, t0).
+double* ctx_install_target(hyp_ctx* c);
+int ctx_finish_install(hyp_ctx* c, double t0);
 
 namespace hyp {
 // adjoint buffers of a context (hyp_adjoint.cu)

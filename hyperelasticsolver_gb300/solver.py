@@ -96,6 +96,23 @@ class Solver:
         return {"ms_total": a.value, "ms_cell": b.value, "n_cell": nc.value, "ms_update": d.value,
                 "n_update": nu.value}
 
+    # ---- initial conditions on the device (main.jl:99-123) ----
+    def init_riemann(self, Ql, Qr):
+        """initial_condition(Ql, Qr, nx) (main.jl:99-106) built on the device as the state at t = 0."""
+        ql = np.ascontiguousarray(Ql, dtype=np.float64)
+        qr = np.ascontiguousarray(Qr, dtype=np.float64)
+        if ql.shape != (self.nvar,) or qr.shape != (self.nvar,):
+            raise ValueError(f"states must have {self.nvar} values")
+        L.check(L.load().hyp_init_riemann(self._h, L.ptr(ql), L.ptr(qr)), self._h, "hyp_init_riemann")
+
+    def init_tanh(self, Ql, Qr, eps=0.2):
+        """initial_condition_tanh(eos, Ql, Qr, nx, eps) (main.jl:110-123), two phases, on the device."""
+        ql = np.ascontiguousarray(Ql, dtype=np.float64)
+        qr = np.ascontiguousarray(Qr, dtype=np.float64)
+        if ql.shape != (30,) or qr.shape != (30,):
+            raise ValueError("two-phase states have 30 values")
+        L.check(L.load().hyp_init_tanh(self._h, L.ptr(ql), L.ptr(qr), float(eps)), self._h, "hyp_init_tanh")
+
     # ---- snapshots and restart (main.jl:62-95, 174-198, 233-237) ----
     def snapshot(self):
         """Primitive states of the current state, (15 or 30, nx): per phase alpha, rho, u(3), S, A(9)."""

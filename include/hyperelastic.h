@@ -202,6 +202,19 @@ int hyp_load_snapshot(hyp_ctx* ctx, const char* path, double t0);
 int hyp_run_logged(hyp_ctx* ctx, double t_end, int max_steps, int log_freq, const char* dir, int64_t first_step,
                    int* steps_done, double* t_out);
 
+/* ---- initial conditions built on the device --------------------------------- */
+/* HyperelasticityMPh.initial_states(eos, testcase) (HyperelasticityMPh.jl:275-426):
+   the conservative left and right 30-vectors of test case 1-7 or 10 for the two
+   phases of cfg (two-phase config). */
+int hyp_initial_states(const hyp_config* cfg, int testcase, double* Ql, double* Qr);
+/* initial_condition(Ql, Qr, nx) (main.jl:99-106) generated on the device as the
+   current state at t = 0: cells (i - 1) < nx/2 (1-based) take Ql (nvar values). */
+int hyp_init_riemann(hyp_ctx* ctx, const double* Ql, const double* Qr);
+/* initial_condition_tanh(eos, Ql, Qr, nx, eps) (main.jl:110-123), two phases: per
+   cell the primitive state of its side with alpha1 = 0.1 (tanh(4 (x - 1/2)/eps) + 1)
+   + 0.4 and alpha2 = 1 - alpha1, x = (i - 1/2)/nx. */
+int hyp_init_tanh(hyp_ctx* ctx, const double* Ql, const double* Qr, double eps);
+
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);
 int hyp_host_free(void* p);
