@@ -25,6 +25,20 @@ class Barton2009:
                 f"alpha={self.alpha}, beta={self.beta}, gamma={self.gamma})")
 
 
+class Hank2016:
+    """Hank2016 EOS parameters (EquationsOfState.jl:305-326), same names and defaults.
+    The reference defines energy, pressure and stress for it; its time step uses Barton2009."""
+
+    def __init__(self, rho0=2.7, mu=26e9, gamma=3.4, pres_inf=21.5e9, a=0.5):
+        self.rho0, self.mu, self.gamma, self.pres_inf, self.a = (float(v) for v in (rho0, mu, gamma, pres_inf, a))
+
+    def c(self):
+        return L.Hank2016C(self.rho0, self.mu, self.gamma, self.pres_inf, self.a)
+
+    def __repr__(self):
+        return f"Hank2016(rho0={self.rho0}, mu={self.mu}, gamma={self.gamma}, pres_inf={self.pres_inf}, a={self.a})"
+
+
 EoS = Barton2009
 
 
@@ -43,9 +57,31 @@ def _eval(fname, eos, s, M, k_out):
     return L.unsoa(out, single)
 
 
-def energy(eos, S, G):
-    """Internal energy e(S, G) (EquationsOfState.jl:118-137)."""
+def _eval_hank(fname, eos, x, y, M, k_in, k_out):
+    m, n, single = L.soa(M, k_in)
+    x, y = _scalar_vec(x, n), _scalar_vec(y, n)
+    out = np.empty((k_out, n))
+    L.check(getattr(L.load(), fname)(eos.c(), L.ptr(x), L.ptr(y), L.ptr(m), L.ptr(out), n), what=fname)
+    if k_out == 1:
+        return out[0, 0] if single else out[0]
+    return L.unsoa(out, single)
+
+
+def energy(eos, *args):
+    """Internal energy: energy(eos::Barton2009, S, G) (EquationsOfState.jl:118-137) or
+    energy(eos::Hank2016, den, pres, G) (EquationsOfState.jl:321-336)."""
+    if isinstance(eos, Hank2016):
+        den, pres, G = args
+        return _eval_hank("hyp_eval_hank2016_energy", eos, den, pres, G, 9, 1)
+    S, G = args
     return _eval("hyp_eval_energy", eos, S, G, 1)
+
+
+def pressure(eos, den, e_int, i):
+    """pressure(eos::Hank2016, den, e_int, i) (EquationsOfState.jl:338-352); i: invariants (3,) or (n, 3)."""
+    if not isinstance(eos, Hank2016):
+        raise NotImplementedError("the reference defines pressure for Hank2016 only")
+    return _eval_hank("hyp_eval_hank2016_pressure", eos, den, e_int, i, 3, 1)
 
 
 def entropy(eos, e_int, G):
@@ -53,8 +89,14 @@ def entropy(eos, e_int, G):
     return _eval("hyp_eval_entropy", eos, e_int, G, 1)
 
 
-def stress(eos, ent, F):
-    """Cauchy stress -2 rho G dE/dG, rho = rho0/det F (EquationsOfState.jl:179-190); column-major 9-vector."""
+def stress(eos, *args):
+    """Cauchy stress: stress(eos::Barton2009, ent, F) = -2 rho G dE/dG, rho = rho0/det F
+    (EquationsOfState.jl:179-190), or stress(eos::Hank2016, den, pressure, distortion)
+    = -2 den G dE/dG with G = finger(inv(F)) (EquationsOfState.jl:354-361); column-major."""
+    if isinstance(eos, Hank2016):
+        den, pres, F = args
+        return _eval_hank("hyp_eval_hank2016_stress", eos, den, pres, F, 9, 9)
+    ent, F = args
     return _eval("hyp_eval_stress", eos, ent, F, 9)
 
 

@@ -57,6 +57,10 @@ class Barton2009C(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("rho0", "c0", "cv", "t0", "b0", "alpha", "beta", "gamma")]
 
 
+class Hank2016C(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("rho0", "mu", "gamma", "pres_inf", "a")]
+
+
 class ConfigC(ctypes.Structure):
     _fields_ = [
         ("n_cells", ctypes.c_int64),
@@ -119,6 +123,9 @@ _SIGS = {
     "hyp_eval_entropy": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_stress": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_acoustic": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_hank2016_energy": ([ctypes.POINTER(Hank2016C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_hank2016_pressure": ([ctypes.POINTER(Hank2016C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_hank2016_stress": ([ctypes.POINTER(Hank2016C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_cons2prim": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_prim2cons": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_prim2cons_vjp": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),

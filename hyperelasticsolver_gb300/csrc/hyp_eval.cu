@@ -5,6 +5,7 @@
 #include <cmath>
 #include <vector>
 #include "hyp_internal.cuh"
+#include "hyp_hank.cuh"
 
 using namespace hyp;
 
@@ -232,6 +233,61 @@ extern "C" int hyp_eval_acoustic(const hyp_barton2009* eos, const double* S, con
              },
              &ec);
 }
+// ---- Hank2016 (EquationsOfState.jl:305-366) ----------------------------------
+namespace {
+__global__ void k_hank_energy(Hank h, const double* den, const double* pres, const double* G, double* out,
+                              int64_t n) {
+  IDX double g[9];
+  LD(g, G, 9);
+  out[i] = hank_energy(h, den[i], pres[i], g);
+}
+__global__ void k_hank_pressure(Hank h, const double* den, const double* e, const double* I3, double* out,
+                                int64_t n) {
+  IDX double v[3];
+  LD(v, I3, 3);
+  out[i] = hank_pressure(h, den[i], e[i], v);
+}
+__global__ void k_hank_stress(Hank h, const double* den, const double* pres, const double* F, double* out,
+                              int64_t n) {
+  IDX double f[9], s[9];
+  LD(f, F, 9);
+  hank_stress(h, den[i], pres[i], f, s);
+  ST(out, s, 9);
+}
+Hank hank_of(const hyp_hank2016* e) { return Hank{e->rho0, e->mu, e->gamma, e->pres_inf, e->a}; }
+}  // namespace
+
+extern "C" int hyp_eval_hank2016_energy(const hyp_hank2016* eos, const double* den, const double* pres,
+                                        const double* G, double* e, int64_t n) {
+  if (!eos) return HYP_ERR_INVALID;
+  const Hank h = hank_of(eos);
+  return run(n, {{den, nullptr, 1}, {pres, nullptr, 1}, {G, nullptr, 9}, {nullptr, e, 1}},
+             [](int64_t n, double** d, const void* a) {
+               k_hank_energy<<<grid(n), kBlock>>>(*(const Hank*)a, d[0], d[1], d[2], d[3], n);
+             },
+             &h);
+}
+extern "C" int hyp_eval_hank2016_pressure(const hyp_hank2016* eos, const double* den, const double* e_int,
+                                          const double* inv, double* pres, int64_t n) {
+  if (!eos) return HYP_ERR_INVALID;
+  const Hank h = hank_of(eos);
+  return run(n, {{den, nullptr, 1}, {e_int, nullptr, 1}, {inv, nullptr, 3}, {nullptr, pres, 1}},
+             [](int64_t n, double** d, const void* a) {
+               k_hank_pressure<<<grid(n), kBlock>>>(*(const Hank*)a, d[0], d[1], d[2], d[3], n);
+             },
+             &h);
+}
+extern "C" int hyp_eval_hank2016_stress(const hyp_hank2016* eos, const double* den, const double* pres,
+                                        const double* F, double* sigma, int64_t n) {
+  if (!eos) return HYP_ERR_INVALID;
+  const Hank h = hank_of(eos);
+  return run(n, {{den, nullptr, 1}, {pres, nullptr, 1}, {F, nullptr, 9}, {nullptr, sigma, 9}},
+             [](int64_t n, double** d, const void* a) {
+               k_hank_stress<<<grid(n), kBlock>>>(*(const Hank*)a, d[0], d[1], d[2], d[3], n);
+             },
+             &h);
+}
+
 extern "C" int hyp_eval_cons2prim(const hyp_config* cfg, const double* Q, double* P, int64_t n) {
   if (!model_ok(cfg)) return HYP_ERR_INVALID;
   ModelArg m = model_arg(cfg);

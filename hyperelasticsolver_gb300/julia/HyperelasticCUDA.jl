@@ -18,6 +18,12 @@ end
 Barton2009C(; _rho0=8.93, _c0=4.6, _cv=3.9e-4, _t0=300, _b0=2.1, _alpha=1, _beta=3, _gamma=2) =
   Barton2009C(_rho0, _c0, _cv, _t0, _b0, _alpha, _beta, _gamma)
 
+"Hank2016 parameters (EquationsOfState.jl:305-326); function-level evaluators only."
+struct Hank2016C
+  rho0::Float64; mu::Float64; gamma::Float64; pres_inf::Float64; a::Float64
+end
+Hank2016C() = Hank2016C(2.7, 26e9, 3.4, 21.5e9, 0.5)
+
 struct ConfigC
   n_cells::Int64; model::Cint; flux::Cint; bc::Cint; precision::Cint
   x_length::Float64; cfl::Float64; eos1::Barton2009C; eos2::Barton2009C
@@ -63,6 +69,22 @@ module EquationsOfState
       check(ccall(($(QuoteNode(c)), libhyp), Cint, (Ref{Barton2009C}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
                   e, s, M, out, size(M, 1)), $(string(jl)))
       $k == 1 ? vec(out) : out
+    end
+  end
+end
+
+module Hank
+  import ..libhyp, ..check, ..Hank2016C
+  # energy(eos, den, pres, G), pressure(eos, den, e_int, i), stress(eos, den, pres, F) over n cells
+  for (jl, c, k_in, k_out) in ((:energy, :hyp_eval_hank2016_energy, 9, 1),
+                               (:pressure, :hyp_eval_hank2016_pressure, 3, 1),
+                               (:stress, :hyp_eval_hank2016_stress, 9, 9))
+    @eval function $jl(eos::Hank2016C, x::Vector{Float64}, y::Vector{Float64}, M::Matrix{Float64})
+      out = Matrix{Float64}(undef, size(M, 1), $k_out)
+      check(ccall(($(QuoteNode(c)), libhyp), Cint,
+                  (Ref{Hank2016C}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                  Ref(eos), x, y, M, out, size(M, 1)), $(string(jl)))
+      $k_out == 1 ? vec(out) : out
     end
   end
 end

@@ -235,6 +235,22 @@ int hyp_eval_stress(const hyp_barton2009* eos, const double* S, const double* F,
 /* EquationsOfState.acoustic(eos, ent, F, [1,0,0]) (EquationsOfState.jl:223-246).  [9][n] */
 int hyp_eval_acoustic(const hyp_barton2009* eos, const double* S, const double* F, double* ac, int64_t n);
 
+/* Hank2016 (EquationsOfState.jl:305-366), which the reference defines at function
+   level only (its time step uses Barton2009). Defaults: rho0 2.7, mu 26e9, gamma 3.4,
+   pres_inf 21.5e9, a 0.5. */
+typedef struct {
+  double rho0, mu, gamma, pres_inf, a;
+} hyp_hank2016;
+/* energy(eos, den, pres, G) (:321-336).  den, pres, e: [n]; G: [9][n] */
+int hyp_eval_hank2016_energy(const hyp_hank2016* eos, const double* den, const double* pres, const double* G,
+                             double* e, int64_t n);
+/* pressure(eos, den, e_int, i) (:338-352).  inv: [3][n] invariants of G */
+int hyp_eval_hank2016_pressure(const hyp_hank2016* eos, const double* den, const double* e_int, const double* inv,
+                               double* pres, int64_t n);
+/* stress(eos, den, pressure, distortion) (:354-361): -2 den G dE/dG with G = finger(inv(F)).  F, sigma: [9][n] */
+int hyp_eval_hank2016_stress(const hyp_hank2016* eos, const double* den, const double* pres, const double* F,
+                             double* sigma, int64_t n);
+
 /* Model-level functions; cfg selects model and EOS (n_cells etc. ignored).
    cons2prim / prim2cons (HyperelasticityMPh.jl:99-133, 63-90): per phase
    [alpha, rho_true, u(3), S, A(9)] (single phase: alpha dropped). [nvar][n] */

@@ -201,6 +201,46 @@ template <class T, class S, class PM> void acoustic(const BartonT<PM>& e, const 
 }
 
 // ---------------------------------------------------------------------------
+// EquationsOfState.jl:305-366  Hank2016: energy(eos, den, pres, G), pressure(eos,
+// den, e_int, i), stress(eos, den, pres, distortion) = -2 den G dE/dG with
+// G = finger(inv(F)) and the gradient by forward-mode duals (ForwardDiff.gradient).
+struct Hank2016 {
+  double rho0, mu, gamma, pres_inf, a;
+};
+template <class T> T hank_e_el(const Hank2016& h, const T* i) {
+  T j1 = i[0] / pow(i[2], 1.0 / 3.0);
+  T j2 = (ipow2(i[0]) - 2.0 * i[1]) / pow(i[2], 2.0 / 3.0);
+  return h.mu / (4.0 * h.rho0) * (((1.0 - 2.0 * h.a) / 3.0 * ipow2(j1) + h.a * j2) + 3.0 * (h.a - 1.0));
+}
+template <class T> T hank_energy(const Hank2016& h, double den, double pres, const T* G) {
+  T i[3];
+  invariants(G, i);
+  T e_el = hank_e_el(h, i);
+  double e_h = (pres + h.gamma * h.pres_inf) / (den * (h.gamma - 1.0));
+  return e_el + e_h;
+}
+inline double hank_pressure(const Hank2016& h, double den, double e_int, const double* i) {
+  double e_h = e_int - hank_e_el(h, i);
+  return e_h * (h.gamma - 1.0) * den - h.gamma * h.pres_inf;
+}
+inline void hank_stress(const Hank2016& h, double den, double pres, const double* F, double* sig) {
+  double Fi[9], G[9];
+  inv_(F, Fi);
+  finger(Fi, G);
+  using D = Dual<double, 9>;
+  D g[9];
+  for (int k = 0; k < 9; ++k) {
+    g[k] = D(G[k]);
+    g[k].d[k] = 1.0;
+  }
+  D e = hank_energy(h, den, pres, g);
+  double dedG[9], a[9];
+  for (int k = 0; k < 9; ++k) dedG[k] = e.d[k];
+  for (int k = 0; k < 9; ++k) a[k] = (-2.0 * den) * G[k];
+  matmul3(a, dedG, sig);
+}
+
+// ---------------------------------------------------------------------------
 // Eigenvalue moduli of a real 3x3 matrix (the reference calls LAPACK
 // `eigvals`, HyperelasticityMPh.jl:263, and consumes only sqrt(abs(.))).
 // Characteristic polynomial mu^3 - c2 mu^2 + c1 mu - c0; closed-form

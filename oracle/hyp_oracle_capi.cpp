@@ -95,6 +95,35 @@ int hyo_acoustic(const hyo_eos* eos, const double* S, const double* F, double* a
   }
   return 0;
 }
+typedef struct { double rho0, mu, gamma, pres_inf, a; } hyo_hank;
+int hyo_hank_energy(const hyo_hank* p, const double* den, const double* pres, const double* G, double* e, int64_t n) {
+  Hank2016 h{p->rho0, p->mu, p->gamma, p->pres_inf, p->a};
+  for (int64_t i = 0; i < n; ++i) {
+    double g[9];
+    GATHER(g, G, 9, n, i);
+    e[i] = hank_energy(h, den[i], pres[i], g);
+  }
+  return 0;
+}
+int hyo_hank_pressure(const hyo_hank* p, const double* den, const double* e, const double* I, double* pr, int64_t n) {
+  Hank2016 h{p->rho0, p->mu, p->gamma, p->pres_inf, p->a};
+  for (int64_t i = 0; i < n; ++i) {
+    double v[3];
+    GATHER(v, I, 3, n, i);
+    pr[i] = hank_pressure(h, den[i], e[i], v);
+  }
+  return 0;
+}
+int hyo_hank_stress(const hyo_hank* p, const double* den, const double* pres, const double* F, double* sig, int64_t n) {
+  Hank2016 h{p->rho0, p->mu, p->gamma, p->pres_inf, p->a};
+  for (int64_t i = 0; i < n; ++i) {
+    double f[9], s[9];
+    GATHER(f, F, 9, n, i);
+    hank_stress(h, den[i], pres[i], f, s);
+    SCATTER(sig, s, 9, n, i);
+  }
+  return 0;
+}
 int hyo_eig3_moduli(const double* a, double* mods, int64_t n) {
   for (int64_t i = 0; i < n; ++i) {
     double m[9], r[3];

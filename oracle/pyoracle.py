@@ -23,6 +23,34 @@ class Eos(ctypes.Structure):
     _fields_ = [(n, ctypes.c_double) for n in ("rho0", "c0", "cv", "t0", "b0", "alpha", "beta", "gamma")]
 
 
+class Hank(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_double) for n in ("rho0", "mu", "gamma", "pres_inf", "a")]
+
+
+def hank2016(rho0=2.7, mu=26e9, gamma=3.4, pres_inf=21.5e9, a=0.5):
+    return Hank(rho0, mu, gamma, pres_inf, a)
+
+
+def _hank(fname, h, x, y, M, k_in, k_out):
+    m, n, single = _soa(M, k_in)
+    x, y = _vec(x, n), _vec(y, n)
+    out = np.empty((k_out, n))
+    getattr(lib(), fname)(ctypes.byref(h), _ptr(x), _ptr(y), _ptr(m), _ptr(out), n)
+    return (out[0, 0] if single else out[0]) if k_out == 1 else _out(out, single)
+
+
+def hank_energy(h, den, pres, G):
+    return _hank("hyo_hank_energy", h, den, pres, G, 9, 1)
+
+
+def hank_pressure(h, den, e_int, inv):
+    return _hank("hyo_hank_pressure", h, den, e_int, inv, 3, 1)
+
+
+def hank_stress(h, den, pres, F):
+    return _hank("hyo_hank_stress", h, den, pres, F, 9, 9)
+
+
 def barton2009(rho0=8.93, c0=4.6, cv=3.9e-4, t0=300.0, b0=2.1, alpha=1.0, beta=3.0, gamma=2.0):
     """Default arguments as the reference constructor (EquationsOfState.jl:90)."""
     return Eos(rho0, c0, cv, t0, b0, alpha, beta, gamma)
@@ -98,6 +126,10 @@ def lib():
         L.hyo_quadrature.restype = None
         L.hyo_max_speed.argtypes = [pp, dp, ctypes.c_int]
         L.hyo_max_speed.restype = ctypes.c_double
+        hp = ctypes.POINTER(Hank)
+        for name in ("hyo_hank_energy", "hyo_hank_pressure", "hyo_hank_stress"):
+            getattr(L, name).argtypes = [hp, dp, dp, dp, dp, ctypes.c_int64]
+            getattr(L, name).restype = ctypes.c_int
         L.hyo_misfit_grad_dual.argtypes = [pp, dp, dp, ctypes.c_int, dp, ctypes.c_int, dp, dp]
         L.hyo_misfit_grad_dual.restype = ctypes.c_int
         _lib = L

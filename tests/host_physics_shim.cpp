@@ -3,6 +3,7 @@
 // GPU. Compiled by tests/test_physics_host.py into a temporary shared library.
 #include "../hyperelasticsolver_gb300/csrc/hyp_physics.cuh"
 #include "../hyperelasticsolver_gb300/csrc/hyp_adjoint.cuh"
+#include "../hyperelasticsolver_gb300/csrc/hyp_hank.cuh"
 
 using namespace hyp;
 
@@ -72,5 +73,13 @@ void hs_prim2cons1_vjp(const double* ep, const double* p, const double* qb, doub
   prim2cons_vjp(e, p, qb, pb, b);
   eb[0] = b.b0sq;
   eb[1] = b.k0;
+}
+
+// Hank2016: h = [rho0, mu, gamma, pres_inf, a]
+double hs_hank_energy(const double* h, double den, double pres, const double* G) {
+  return hank_energy(Hank{h[0], h[1], h[2], h[3], h[4]}, den, pres, G);
+}
+void hs_hank_stress(const double* h, double den, double pres, const double* F, double* sig) {
+  hank_stress(Hank{h[0], h[1], h[2], h[3], h[4]}, den, pres, F, sig);
 }
 }

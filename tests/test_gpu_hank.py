@@ -1,0 +1,38 @@
+"""Hank2016 EOS (EquationsOfState.jl:305-366) on the device against the oracle's
+restatement (stress by forward-mode dual numbers, as ForwardDiff.gradient)."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+
+def states(n, rng):
+    F = np.eye(3)[None] + 0.05 * rng.standard_normal((n, 3, 3))
+    return F.transpose(0, 2, 1).reshape(n, 9)  # column-major 9-vectors
+
+
+def test_hank2016_matches_oracle(hyp, orc):
+    from hyperelasticsolver_gb300 import EquationsOfState as E, Strains
+    rng = np.random.default_rng(11)
+    n = 200
+    F = states(n, rng)
+    den = 2.7 * rng.uniform(0.9, 1.1, n)
+    pres = rng.uniform(-1e9, 5e9, n)
+    eos, ho = E.Hank2016(), orc.hank2016()
+    G = Strains.finger(F)
+    e = E.energy(eos, den, pres, G)
+    np.testing.assert_allclose(e, orc.hank_energy(ho, den, pres, G), rtol=1e-13)
+    inv = Strains.invariants(G)
+    p = E.pressure(eos, den, e, inv)
+    np.testing.assert_allclose(p, orc.hank_pressure(ho, den, e, inv), rtol=1e-10, atol=1e-3)
+    np.testing.assert_allclose(p, pres, rtol=1e-9, atol=1e-2)  # pressure inverts energy at fixed G
+    s = E.stress(eos, den, pres, F)
+    so = orc.hank_stress(ho, den, pres, F)
+    scale = np.max(np.abs(so), axis=1, keepdims=True)
+    assert np.max(np.abs(s - so) / scale) < 1e-12
+
+
+def test_hank2016_stress_free_reference_state(hyp):
+    from hyperelasticsolver_gb300 import EquationsOfState as E
+    s = E.stress(E.Hank2016(), 2.7, 1e5, np.eye(3).reshape(-1))
+    assert np.max(np.abs(s)) < 1e-3  # mu = 26e9: zero to rounding

@@ -25,6 +25,7 @@ def shim():
     for n in ("hs_energy", "hs_entropy", "hs_spectral_radius"):
         getattr(L, n).restype = ctypes.c_double
     L.hs_cell1_vjp.restype = ctypes.c_int
+    L.hs_hank_energy.restype = ctypes.c_double
     return L
 
 
@@ -160,3 +161,21 @@ def test_prim2cons_vjp_matches_central_differences(shim):
                        (phi(p, _ep_moduli(EOS[0], dk0=1e-5)) - phi(p, _ep_moduli(EOS[0], dk0=-1e-5))) / 2e-5])
         assert np.max(np.abs(pb - fd)) <= 1e-7 * np.max(np.abs(fd)), (trial, pb, fd)
         assert np.max(np.abs(eb - fe)) <= 1e-7 * np.max(np.abs(fe)), (trial, eb, fe)
+
+
+def test_hank2016_closed_form_matches_dual_numbers(shim, orc):
+    """Hank2016 stress in closed form (hyp_hank.cuh) against the oracle's dual-number
+    gradient (EquationsOfState.jl:354-361), and the energy."""
+    h = np.array([2.7, 26e9, 3.4, 21.5e9, 0.5])
+    ho = orc.hank2016()
+    rng = np.random.default_rng(12)
+    for _ in range(20):
+        F = (np.eye(3) + 0.05 * rng.standard_normal((3, 3))).reshape(-1, order="F")
+        den, pres = 2.7 * rng.uniform(0.9, 1.1), rng.uniform(-1e9, 5e9)
+        sig = np.zeros(9)
+        shim.hs_hank_stress(P(h), ctypes.c_double(den), ctypes.c_double(pres), P(F), P(sig))
+        ref = orc.hank_stress(ho, den, pres, F)
+        assert np.max(np.abs(sig - ref)) <= 1e-12 * np.max(np.abs(ref))
+        G = orc.finger(F)
+        e = shim.hs_hank_energy(P(h), ctypes.c_double(den), ctypes.c_double(pres), P(G))
+        assert abs(e - orc.hank_energy(ho, den, pres, G)) <= 1e-13 * abs(e)
