@@ -64,6 +64,14 @@ __global__ void __launch_bounds__(kBlock) cell1_f64_kernel(const double* __restr
   if (threadIdx.x == 0) atomicMax(lam_slot, (unsigned long long)__double_as_longlong(m));
 }
 
+// The Rusanov face flux 0.5 (f_a + f_b) - h (q_b - q_a) with one fixed rounding
+// sequence: both cells that share a face evaluate it, and with explicit intrinsics
+// (no compiler contraction) they get the same value, so the update conserves
+// exactly and the step commutes with x -> -x.
+__device__ __forceinline__ double face_flux(double fa, double fb, double h, double qa, double qb) {
+  return __fma_rn(-h, __dsub_rn(qb, qa), __dmul_rn(0.5, __dadd_rn(fa, fb)));
+}
+
 __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __restrict__ Q, double* __restrict__ Qn,
                                                              int64_t n, const double* __restrict__ F,
                                                              const double* __restrict__ lam,
@@ -112,9 +120,9 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
       fc = F[sl * n + i];
       fr = F[sl * n + ir];
     }
-    const double FL = 0.5 * (fl + fc) - hl * (qc - ql);
-    const double FR = 0.5 * (fc + fr) - hr * (qr - qc);
-    Qn[v * n + i] = qc - dtdx * (FR - FL);
+    const double FL = face_flux(fl, fc, hl, ql, qc);
+    const double FR = face_flux(fc, fr, hr, qc, qr);
+    Qn[v * n + i] = __fma_rn(-dtdx, __dsub_rn(FR, FL), qc);
   }
 }
 
