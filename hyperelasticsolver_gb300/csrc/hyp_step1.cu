@@ -65,13 +65,37 @@ __global__ void __launch_bounds__(kBlock) cell1_f64_kernel(const double* __restr
 }
 
 // The Rusanov face flux 0.5 (f_a + f_b) - h (q_b - q_a) with one fixed rounding
-// sequence: both cells that share a face evaluate it, and with explicit intrinsics
-// (no compiler contraction) they get the same value, so the update conserves
-// exactly and the step commutes with x -> -x.
+// sequence (explicit intrinsics, no compiler contraction), so the step commutes
+// with x -> -x.
 __device__ __forceinline__ double face_flux(double fa, double fb, double h, double qa, double qb) {
   return __fma_rn(-h, __dsub_rn(qb, qa), __dmul_rn(0.5, __dadd_rn(fa, fb)));
 }
 
+// Face f of the block (between cells f - 1 and f, a zero-gradient ghost past either
+// end) into slot k of the block's face table: its 14 flux components.
+__device__ __forceinline__ void rusanov_face(const double* __restrict__ Q, const double* __restrict__ F,
+                                             const double* __restrict__ lam, int64_t n, int64_t f, bool lxf,
+                                             double lam_lxf, double (*sF)[kBlock + 1], int k) {
+  const int64_t a = f > 0 ? f - 1 : 0, b = f < n ? f : n - 1;
+  double lf;
+  if (lxf) {
+    lf = lam_lxf;
+  } else {
+    const double la = lam[a], lb = lam[b];
+    lf = la > lb ? la : lb;  // max(lambda_L, lambda_R) (main.jl:45-48)
+  }
+  const double h = lf * 0.5;
+#pragma unroll
+  for (int v = 0; v < 14; ++v) {
+    const int sl = flux_slot1(v);
+    const double fa = sl >= 0 ? F[sl * n + a] : 0.0, fb = sl >= 0 ? F[sl * n + b] : 0.0;
+    sF[v][k] = face_flux(fa, fb, h, Q[v * n + a], Q[v * n + b]);
+  }
+}
+
+// Each face is evaluated once, by the block that owns the cell on its right (the
+// block's last cell also evaluates its right face), into shared memory; both cells
+// of a face read the same value, so the update conserves exactly.
 __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __restrict__ Q, double* __restrict__ Qn,
                                                              int64_t n, const double* __restrict__ F,
                                                              const double* __restrict__ lam,
@@ -79,6 +103,7 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
                                                              unsigned long long* lam_next, const double* t_in,
                                                              double* t_out, long long* steps, double t_end,
                                                              double cfl, double dx, int flux, int bc) {
+  __shared__ double sF[14][kBlock + 1];  // face k of the block = left face of cell i0 + k
   const double tn = *t_in;
   const bool active = tn < t_end;
   const double lmax = __longlong_as_double((long long)*lam_in);
@@ -91,38 +116,21 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
     *lam_next = 0ull;
     if (active) *steps += 1;
   }
-  if (!active) return;
-  int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  if (!active) return;  // the same for every block
+  const int64_t i0 = (int64_t)blockIdx.x * kBlock;
+  const int64_t i = i0 + threadIdx.x;
+  const bool lxf = flux == HYP_FLUX_LXF;
+  if (i < n) {
+    rusanov_face(Q, F, lam, n, i, lxf, lam_lxf, sF, threadIdx.x);
+    if (threadIdx.x == kBlock - 1 || i == n - 1) rusanov_face(Q, F, lam, n, i + 1, lxf, lam_lxf, sF, threadIdx.x + 1);
+  }
+  __syncthreads();
   if (i >= n) return;
-  if (bc == HYP_BC_FROZEN && (i == 0 || i == n - 1)) {
-#pragma unroll
-    for (int v = 0; v < 14; ++v) Qn[v * n + i] = Q[v * n + i];
-    return;
-  }
-  const int64_t il = i > 0 ? i - 1 : 0, ir = i < n - 1 ? i + 1 : n - 1;
-  double lc = lam[i];
-  double lamL, lamR;
-  if (flux == HYP_FLUX_LXF) {
-    lamL = lamR = lam_lxf;
-  } else {
-    double ll = lam[il], lr = lam[ir];
-    lamL = ll > lc ? ll : lc;
-    lamR = lc > lr ? lc : lr;
-  }
-  const double hl = lamL * 0.5, hr = lamR * 0.5;
+  const bool frozen = bc == HYP_BC_FROZEN && (i == 0 || i == n - 1);
 #pragma unroll
   for (int v = 0; v < 14; ++v) {
-    const double qc = Q[v * n + i], ql = Q[v * n + il], qr = Q[v * n + ir];
-    const int sl = flux_slot1(v);
-    double fl = 0.0, fc = 0.0, fr = 0.0;
-    if (sl >= 0) {
-      fl = F[sl * n + il];
-      fc = F[sl * n + i];
-      fr = F[sl * n + ir];
-    }
-    const double FL = face_flux(fl, fc, hl, ql, qc);
-    const double FR = face_flux(fc, fr, hr, qc, qr);
-    Qn[v * n + i] = __fma_rn(-dtdx, __dsub_rn(FR, FL), qc);
+    const double qc = Q[v * n + i];
+    Qn[v * n + i] = frozen ? qc : __fma_rn(-dtdx, __dsub_rn(sF[v][threadIdx.x + 1], sF[v][threadIdx.x]), qc);
   }
 }
 
