@@ -65,7 +65,7 @@ HYP_HD double powers_vjp(const EosC& e, const Kin& k, const Pows& w, const PowsB
 HYP_HD double kinematics_vjp(const double* A, const Kin& k, Sym Gb, Sym Hb, double i1b, double psib, double pb,
                              double* Ab) {
   // psi = i1^2/3 - i2, i2 = (i1^2 - tr H)/2  ->  psi = -i1^2/6 + tr H / 2
-  i1b -= psib * k.i1 / 3.0;
+  i1b -= psib * k.i1 * (1.0 / 3.0);
   Hb.a00 += 0.5 * psib;
   Hb.a11 += 0.5 * psib;
   Hb.a22 += 0.5 * psib;
@@ -146,7 +146,7 @@ HYP_HD void stress_coeffs_vjp(const EosC& e, const Kin& k, const Pows& w, double
   const double E1b = cb.cG;
   const double E2b = -cb.cGG + cb.cG * k.i1;
   i1b += cb.cG * E2;
-  eb.b0sq += E1b * w.Pb * k.i1 / 3.0;
+  eb.b0sq += E1b * w.Pb * k.i1 * (1.0 / 3.0);
   wb.Pb += E1b * e.b0sq_3 * k.i1;
   i1b += E1b * e.b0sq_3 * w.Pb;
   eb.b0sq -= 0.5 * E2b * w.Pb;
@@ -238,7 +238,7 @@ HYP_HD void acoustic_omega_vjp(const EosC& e, const Kin& k, const Pows& w, const
       eb.b0sq += 0.5 * dcGGb * dPb;
       double dPbb = 0.5 * e.b0sq * dcGGb;
       // dcG = -b0sq/6 (dPb i1 + Pb di1)
-      eb.b0sq -= dcGb * (dPb * k.i1 + w.Pb * di1) / 6.0;
+      eb.b0sq -= dcGb * (dPb * k.i1 + w.Pb * di1) * (1.0 / 6.0);
       dPbb -= bs6 * dcGb * k.i1;
       i1b -= bs6 * dcGb * dPb;
       wb.Pb -= bs6 * dcGb * di1;
@@ -263,7 +263,7 @@ HYP_HD void acoustic_omega_vjp(const EosC& e, const Kin& k, const Pows& w, const
       eb.b0sq += dE3b * w.Pb1 * dpsi * e.beta / 4.0;
       wb.Pb1 += dE3b * e.kE3b * dpsi;
       dpsib += dE3b * e.kE3b * w.Pb1;
-      eb.b0sq -= dcGb * w.Pb * di1 / 6.0;
+      eb.b0sq -= dcGb * w.Pb * di1 * (1.0 / 6.0);
       wb.Pb -= bs6 * dcGb * di1;
       di1b -= bs6 * dcGb * w.Pb;
     }
@@ -358,14 +358,15 @@ HYP_HD int cell_vjp(const EosC& e, const double* q, const double* fb, double lb,
   if (lb != 0.0) {
     ub[0] += P.u[0] > 0.0 ? lb : (P.u[0] < 0.0 ? -lb : 0.0);
     double s0r[3], om[9], omb[9], s0rb[3] = {0.0, 0.0, 0.0};
-    for (int i = 0; i < 3; ++i) s0r[i] = F.s0[i] / F.rho_s;
+    const double irs = k.inv_s * e.inv_rho0;  // 1/rho_s = det A / rho0
+    for (int i = 0; i < 3; ++i) s0r[i] = F.s0[i] * irs;
     acoustic_omega(e, k, w, F.c, P.xm1, s0r, om);
     const double mu = spectral_radius(om);
     eig_top_vjp(om, mu, lb * 0.5 / sqrt(mu), omb);
     acoustic_omega_vjp(e, k, w, F.c, P.xm1, omb, Gb, Hb, i1b, pb, psib, wb, cb, xm1b, s0rb, eb);
     for (int i = 0; i < 3; ++i) {
-      s0b[i] += s0rb[i] / F.rho_s;
-      rhosb -= s0rb[i] * s0r[i] / F.rho_s;
+      s0b[i] += s0rb[i] * irs;
+      rhosb -= s0rb[i] * s0r[i] * irs;
     }
   }
   // ---- stress row 1: s0 = -2 rho_s (cG G0. + cGG H0. + cI e0) ----
@@ -393,7 +394,7 @@ HYP_HD int cell_vjp(const EosC& e, const double* q, const double* fb, double lb,
   double sb = kinematics_vjp(P.A, k, Gb, Hb, i1b, psib, pb, Ab);
   sb += e.rho0 * rhosb;  // rho_s = rho0 s
   // ---- cons2prim (alpha = 1): s = rho/rho0 (through det A = rho0/rho) ----
-  rhob += sb / e.rho0;
+  rhob += sb * e.inv_rho0;
   Eb += eintb;  // e_int = E - |u|^2/2
   for (int a = 0; a < 3; ++a) ub[a] -= eintb * P.u[a];
   const double irho = P.inv_den;
@@ -409,7 +410,7 @@ HYP_HD int cell_vjp(const EosC& e, const double* q, const double* fb, double lb,
   }
   rhob -= irhob * irho * irho;
   // rho = sqrt(det(rho A) / rho0)
-  const double db = rhob * e.inv_rho0 / (2.0 * rho);
+  const double db = rhob * e.inv_rho0 * (0.5 * P.inv_den);
   const double* m = q + 5;
   qb[5] += db * (m[4] * m[8] - m[5] * m[7]);
   qb[6] += db * (m[5] * m[6] - m[3] * m[8]);

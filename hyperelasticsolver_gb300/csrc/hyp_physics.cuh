@@ -370,9 +370,10 @@ HYP_HD int cons_to_prim(const EosC& e, double alpha, const double* m, double rho
   P.E = rhoE * P.inv_den;
   P.e_int = P.E - 0.5 * (P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2]);
   for (int c = 0; c < 9; ++c) P.A[c] = rA[c] * P.inv_den;
-  // det A = det(rA/den) = d alpha^3 / den^3 = rho0 / true_den  ->  1/det A = true_den / rho0
-  double detA = e.rho0 / P.true_den;
-  P.k = kinematics(P.A, detA);
+  // det A = det(rA/den) = d alpha^3 / den^3 = rho0 / true_den = rho0 alpha / den,
+  // 1/det A = true_den / rho0
+  const double detA = (e.rho0 * alpha) * P.inv_den;
+  P.k = kinematics_s(P.A, P.true_den * e.inv_rho0, detA);
   P.w = powers(e, P.k);
   P.xm1 = entropy_xm1(e, P.e_int, P.k, P.w);
   if (!(P.e_int == P.e_int) || !(P.xm1 == P.xm1) || !isfinite(P.k.p)) st |= HYP_CELL_NONFINITE;
@@ -400,7 +401,8 @@ HYP_HD double phase_cmax(const EosC& e, const Prim& P, const StressC& c) {
   double rho_s = e.rho0 * P.k.s;
   double s0[3], s0r[3], om[9];
   stress_row0(rho_s, P.k, c, s0);
-  for (int i = 0; i < 3; ++i) s0r[i] = s0[i] / rho_s;
+  const double irs = P.k.inv_s * e.inv_rho0;  // 1/rho_s = det A / rho0
+  for (int i = 0; i < 3; ++i) s0r[i] = s0[i] * irs;
   acoustic_omega(e, P.k, P.w, c, P.xm1, s0r, om);
   return sqrt(spectral_radius(om));
 }

@@ -44,8 +44,8 @@ HYP_HD int noncons_bcol(const EosC* eos, const double* Q, double* bcol) {
   int st = phase_b(eos[0], Q, b[0]) | phase_b(eos[1], Q + 15, b[1]);
   double uI[3], sI[3];
   for (int a = 0; a < 3; ++a) uI[a] = 0.5 * b[0].u[a] + 0.5 * b[1].u[a];
-  const double den = 0.5 * b[0].T + 0.5 * b[1].T;
-  for (int a = 0; a < 3; ++a) sI[a] = ((0.5 * b[1].T) * b[0].K0[a] + (0.5 * b[0].T) * b[1].K0[a]) / den;
+  const double iden = 1.0 / (0.5 * b[0].T + 0.5 * b[1].T);
+  for (int a = 0; a < 3; ++a) sI[a] = ((0.5 * b[1].T) * b[0].K0[a] + (0.5 * b[0].T) * b[1].K0[a]) * iden;
   for (int p = 0; p < 2; ++p) {
     double* r = bcol + 15 * p;
     const PhaseB& B = b[p];
@@ -125,13 +125,13 @@ HYP_HD int hll_face2(const EosC* eos, const Quad6D& qd, const double* QL, const 
   double sr = 0.0;
   if (mmax > sr) sr = mmax;
   if (smaxR > sr) sr = smaxR;
-  const double dsr = sr - sl;
+  const double idsr = 1.0 / (sr - sl);
   double acc[30], Qh[30];
   for (int k = 0; k < 30; ++k) acc[k] = 0.0;
   st |= path_integral_add(eos, qd, QL, QR, acc);  // B_int(Q_l, Q_r)
   for (int k = 0; k < 30; ++k) {
     const double pint = (acc[k] + fr[k]) - fl[k];
-    Qh[k] = ((QR[k] * sr - QL[k] * sl) - pint) / dsr;
+    Qh[k] = ((QR[k] * sr - QL[k] * sl) - pint) * idsr;
   }
   // inner = ((f_r - f_l) + B_int(Q_l, Q_hll)) + B_int(Q_hll, Q_r), each integral summed first
   double b2[30];
@@ -141,7 +141,7 @@ HYP_HD int hll_face2(const EosC* eos, const Quad6D& qd, const double* QL, const 
   }
   st |= path_integral_add(eos, qd, QL, Qh, acc);
   st |= path_integral_add(eos, qd, Qh, QR, b2);
-  const double cm = (-sl) / dsr, cp = sr / dsr, cq = (sl * sr) / dsr;
+  const double cm = (-sl) * idsr, cp = sr * idsr, cq = (sl * sr) * idsr;
   for (int k = 0; k < 30; ++k) {
     const double inner = ((fr[k] - fl[k]) + acc[k]) + b2[k];
     const double jump = QR[k] - QL[k];
