@@ -43,9 +43,12 @@ def test_library_loads_without_gpu(hyp):
 def test_invalid_arguments_rejected_before_any_device_work(hyp):
     import ctypes
     L = hyp._lib.load()
-    cfg = hyp._model.config(hyp.Barton2009(), hyp._lib.HYP_MODEL_SINGLE, n_cells=2)  # n < 3
     h = ctypes.c_void_p()
-    assert L.hyp_create(cfg, ctypes.byref(h)) == hyp._lib.HYP_ERR_INVALID
+    for model, eos in ((hyp._lib.HYP_MODEL_SINGLE, hyp.Barton2009()),
+                       (hyp._lib.HYP_MODEL_MULTI, (hyp.Barton2009(), hyp.Barton2009()))):
+        for n in (0, 1, 2):  # fewer than the reference's two frozen ends and one interior cell
+            cfg = hyp._model.config(eos, model, n_cells=n)
+            assert L.hyp_create(cfg, ctypes.byref(h)) == hyp._lib.HYP_ERR_INVALID
     cfg = hyp._model.config(hyp.Barton2009(), 5, n_cells=100)  # bad model
     assert L.hyp_create(cfg, ctypes.byref(h)) == hyp._lib.HYP_ERR_INVALID
     assert L.hyp_create(None, ctypes.byref(h)) == hyp._lib.HYP_ERR_INVALID
