@@ -275,16 +275,35 @@ HYP_HD void acoustic_omega(const EosT<R>& e, const KinT<R>& k, const PowsT<R>& w
 // (trigonometric for three real roots, Cardano otherwise), three Newton steps
 // in R on the seed of largest modulus (a real root r), and deflation to the
 // quadratic mu^2 - (c2 - r) mu + c0/r for the other two (a complex pair has
-// modulus sqrt(c0/r)). Returns |r| and the two other moduli.
-template <class R> HYP_HD void eig_core(const R* a, R* mods) {
-  R c2 = a[0] + a[4] + a[8];
-  R c1 = (a[0] * a[4] - a[3] * a[1]) + (a[0] * a[8] - a[6] * a[2]) + (a[4] * a[8] - a[7] * a[5]);
-  R c0 = det3(a);
+// modulus sqrt(c0/r)).
+template <class R> struct CubicTop {
+  R c2, c1, c0;
+  R r;          // Newton-refined real root of largest seed modulus
+  float other;  // single-precision estimate of the larger other modulus (-1: unknown)
+};
+
+// FP32 reciprocal of a Newton step's slope: the step's own error is then ~1e-7 of
+// the (shrinking) correction, so three steps still reach the root to the last bit.
+template <class R> HYP_HD R newton_recip(R fp) {
+  const float f = (float)fp;
+#ifdef __CUDA_ARCH__
+  const float inv = __frcp_rn(f);
+#else
+  const float inv = 1.0f / f;
+#endif
+  return (fabsf(f) > 1e-30f && fabsf(f) < 1e30f) ? R(inv) : R(1) / fp;
+}
+
+template <class R> HYP_HD CubicTop<R> cubic_top(const R* a) {
+  CubicTop<R> t;
+  const R c2 = a[0] + a[4] + a[8];
+  const R c1 = (a[0] * a[4] - a[3] * a[1]) + (a[0] * a[8] - a[6] * a[2]) + (a[4] * a[8] - a[7] * a[5]);
+  const R c0 = det3(a);
   float C2 = (float)c2, C1 = (float)c1, C0 = (float)c0;
   float p = C1 - C2 * C2 * (1.0f / 3.0f);
   float q = -2.0f / 27.0f * C2 * C2 * C2 + C2 * C1 * (1.0f / 3.0f) - C0;
   float disc = 0.25f * q * q + p * p * p * (1.0f / 27.0f);
-  float seed;
+  float seed, other = -1.0f;
   if (disc < 0.0f && p < 0.0f) {
     float m = 2.0f * sqrtf(-p * (1.0f / 3.0f));
     float cc = fminf(1.0f, fmaxf(-1.0f, 3.0f * q / (p * m)));
@@ -293,42 +312,125 @@ template <class R> HYP_HD void eig_core(const R* a, R* mods) {
     float y1 = m * cosf(th - 2.0943951f) + C2 * (1.0f / 3.0f);
     float y2 = m * cosf(th - 4.1887902f) + C2 * (1.0f / 3.0f);
     seed = y0;
-    if (fabsf(y1) > fabsf(seed)) seed = y1;
-    if (fabsf(y2) > fabsf(seed)) seed = y2;
+    float o1 = y1, o2 = y2;
+    if (fabsf(y1) > fabsf(seed)) { o1 = seed; seed = y1; }
+    if (fabsf(y2) > fabsf(seed)) { o2 = seed; seed = y2; }
+    other = fmaxf(fabsf(o1), fabsf(o2));
   } else {
     float sd = sqrtf(fmaxf(disc, 0.0f));
     seed = cbrtf(-0.5f * q + sd) + cbrtf(-0.5f * q - sd) + C2 * (1.0f / 3.0f);
+    if (seed != 0.0f) other = sqrtf(fabsf(C0 / seed));  // modulus of the complex pair
   }
   R r = (R)seed;
   for (int it = 0; it < 3; ++it) {
     R f = ((r - c2) * r + c1) * r - c0;
     R fp = (R(3) * r - R(2) * c2) * r + c1;
-    r = (fp != R(0)) ? r - f / fp : r;
+    r = (fp != R(0)) ? r - f * newton_recip(fp) : r;
   }
+  t.c2 = c2;
+  t.c1 = c1;
+  t.c0 = c0;
+  t.r = r;
+  t.other = (other == other && seed == seed) ? other : -1.0f;
+  return t;
+}
+
+// Moduli of the two roots other than t.r (deflation).
+template <class R> HYP_HD void cubic_rest(const CubicTop<R>& t, R* m1, R* m2) {
   R s, qq;
-  if (r != R(0)) {
-    s = c2 - r;
-    qq = c0 / r;
+  if (t.r != R(0)) {
+    s = t.c2 - t.r;
+    qq = t.c0 / t.r;
   } else {  // singular: the other roots solve mu^2 - c2 mu + c1
-    s = c2;
-    qq = c1;
+    s = t.c2;
+    qq = t.c1;
   }
   R dsc = s * s - R(4) * qq;
-  mods[0] = fabs(r);
   if (dsc < R(0)) {
-    mods[1] = mods[2] = sqrt(fabs(qq));
+    *m1 = *m2 = sqrt(fabs(qq));
   } else {
     R sq = sqrt(dsc);
     R ra = s >= R(0) ? R(0.5) * (s + sq) : R(0.5) * (s - sq);
-    mods[1] = fabs(ra);
-    mods[2] = ra != R(0) ? fabs(qq / ra) : fabs(s - ra);
+    *m1 = fabs(ra);
+    *m2 = ra != R(0) ? fabs(qq / ra) : fabs(s - ra);
   }
 }
-// Largest eigenvalue modulus (what the step consumes).
+
+// Eigenvalues of the symmetric part of a 3x3 (column-major) by cyclic Jacobi
+// rotations (Jacobi 1846, with Rutishauser's rotation formulas): accurate to a few
+// ulps of the largest modulus whatever the gaps between eigenvalues, where the
+// characteristic polynomial loses half the digits of a repeated root. At theta = 0
+// the rotation's sign follows a_pq, so a matrix and its mirror S A S (S a signature
+// matrix) give the same diagonal bit for bit.
+template <class R> HYP_HD void sym_eig_jacobi(const R* a, R* d) {
+  R m[3][3];
+  for (int j = 0; j < 3; ++j)
+    for (int i = 0; i < 3; ++i) m[i][j] = R(0.5) * (a[i + 3 * j] + a[j + 3 * i]);
+  for (int sweep = 0; sweep < 12; ++sweep) {
+    const R off = fabs(m[0][1]) + fabs(m[0][2]) + fabs(m[1][2]);
+    const R dg = fabs(m[0][0]) + fabs(m[1][1]) + fabs(m[2][2]);
+    if (!(off > R(1e-20) * dg)) break;
+    for (int p = 0; p < 2; ++p)
+      for (int q = p + 1; q < 3; ++q) {
+        const R apq = m[p][q];
+        if (apq == R(0)) continue;
+        const R theta = (m[q][q] - m[p][p]) / (R(2) * apq);
+        const R sg = theta > R(0) ? R(1) : (theta < R(0) ? R(-1) : (apq > R(0) ? R(1) : R(-1)));
+        const R at = fabs(theta);
+        const R t = sg / (at < R(1e150) ? at + sqrt(R(1) + at * at) : R(2) * at);
+        const R c = R(1) / sqrt(R(1) + t * t), sn = t * c;
+        m[p][p] -= t * apq;
+        m[q][q] += t * apq;
+        m[p][q] = m[q][p] = R(0);
+        const int r = 3 - p - q;
+        const R arp = m[r][p], arq = m[r][q];
+        m[r][p] = m[p][r] = c * arp - sn * arq;
+        m[r][q] = m[q][r] = sn * arp + c * arq;
+      }
+  }
+  d[0] = m[0][0];
+  d[1] = m[1][1];
+  d[2] = m[2][2];
+}
+
+// True when a (column-major 3x3) is symmetric to rounding, as the acoustic tensor
+// of a hyperelastic material is.
+template <class R> HYP_HD bool symmetric_to_rounding(const R* a) {
+  R mx = R(0);
+  for (int k = 0; k < 9; ++k) mx = fmax(mx, fabs(a[k]));
+  const R tol = R(64) * R(sizeof(R) == 8 ? 1.1102230246251565e-16 : 5.9604645e-8) * mx;
+  return fabs(a[3] - a[1]) <= tol && fabs(a[6] - a[2]) <= tol && fabs(a[7] - a[5]) <= tol;
+}
+
+// All three moduli: Jacobi for a symmetric matrix, else |r| and the deflated pair.
+template <class R> HYP_HD void eig_core(const R* a, R* mods) {
+  if (symmetric_to_rounding(a)) {
+    sym_eig_jacobi(a, mods);
+    for (int k = 0; k < 3; ++k) mods[k] = fabs(mods[k]);
+    return;
+  }
+  const CubicTop<R> t = cubic_top(a);
+  mods[0] = fabs(t.r);
+  cubic_rest(t, mods + 1, mods + 2);
+}
+
+// Largest eigenvalue modulus (what the step consumes). When the single-precision
+// roots put the other two moduli below 0.9 |r|, the maximum is |r| itself (seed
+// errors are ~1e-6 relative, far inside that margin): the Newton root, accurate to
+// the last bits for a root that separated. Otherwise a symmetric matrix goes to
+// Jacobi and a general one compares |r| with the deflated pair.
 template <class R> HYP_HD R spectral_radius(const R* a) {
-  R m[3];
-  eig_core(a, m);
-  return fmax(m[0], fmax(m[1], m[2]));
+  const CubicTop<R> t = cubic_top(a);
+  const R top = fabs(t.r);
+  if (t.other >= 0.0f && R(t.other) < R(0.9) * top) return top;
+  R m1, m2;
+  if (symmetric_to_rounding(a)) {
+    R d[3];
+    sym_eig_jacobi(a, d);
+    return fmax(fabs(d[0]), fmax(fabs(d[1]), fabs(d[2])));
+  }
+  cubic_rest(t, &m1, &m2);
+  return fmax(top, fmax(m1, m2));
 }
 // All three moduli, descending (the function-level get_eigvals).
 HYP_HD void eig_moduli3(const double* a, double* mods) {

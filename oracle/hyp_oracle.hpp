@@ -27,6 +27,7 @@
 #include <cstring>
 #include <vector>
 #include <algorithm>
+#include <type_traits>
 #include "dual.hpp"
 
 namespace hyp_oracle {
@@ -246,7 +247,61 @@ inline void hank_stress(const Hank2016& h, double den, double pres, const double
 // Characteristic polynomial mu^3 - c2 mu^2 + c1 mu - c0; closed-form
 // (trigonometric / Cardano) seeds, Newton polishing of the real root of
 // largest modulus, and deflation to a quadratic for the other two.
+// A symmetric matrix (the acoustic tensor of a hyperelastic material is one, to
+// rounding) takes classical Jacobi rotations instead, in plain double: LAPACK's
+// eigenvalues of such a matrix are accurate to a few ulps even for a repeated pair
+// (the rest state's b0^2, b0^2), which a deflated quadratic resolves only to about
+// the square root of the rounding.
+inline bool eig3_symmetric(const double* a) {
+  double mx = 0.0;
+  for (int k = 0; k < 9; ++k) mx = std::max(mx, std::fabs(a[k]));
+  const double tol = 64.0 * 2.220446049250313e-16 * 0.5 * mx;
+  return std::fabs(M3(a, 0, 1) - M3(a, 1, 0)) <= tol && std::fabs(M3(a, 0, 2) - M3(a, 2, 0)) <= tol &&
+         std::fabs(M3(a, 1, 2) - M3(a, 2, 1)) <= tol;
+}
+
+// Classical Jacobi (largest off-diagonal entry first) on the symmetric part.
+inline void eig3_jacobi(const double* a, double* ev) {
+  double m[3][3];
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) m[i][j] = 0.5 * (M3(a, i, j) + M3(a, j, i));
+  for (int it = 0; it < 100; ++it) {
+    int p = 0, q = 1;
+    if (std::fabs(m[0][2]) > std::fabs(m[p][q])) { p = 0; q = 2; }
+    if (std::fabs(m[1][2]) > std::fabs(m[p][q])) { p = 1; q = 2; }
+    const double apq = m[p][q];
+    const double scale = std::fabs(m[0][0]) + std::fabs(m[1][1]) + std::fabs(m[2][2]);
+    if (apq == 0.0 || std::fabs(apq) <= 1e-22 * scale) break;
+    const double phi = 0.5 * std::atan2(2.0 * apq, m[q][q] - m[p][p]);
+    const double c = std::cos(phi), sn = std::sin(phi);
+    // rows/columns p, q of R^T m R with R the rotation in the (p, q) plane
+    double np[3], nq[3];
+    for (int k = 0; k < 3; ++k) {
+      np[k] = c * m[p][k] - sn * m[q][k];
+      nq[k] = sn * m[p][k] + c * m[q][k];
+    }
+    for (int k = 0; k < 3; ++k) {
+      m[p][k] = np[k];
+      m[q][k] = nq[k];
+    }
+    for (int k = 0; k < 3; ++k) {
+      const double kp = c * m[k][p] - sn * m[k][q], kq = sn * m[k][p] + c * m[k][q];
+      m[k][p] = kp;
+      m[k][q] = kq;
+    }
+    m[p][q] = m[q][p] = 0.0;
+  }
+  for (int k = 0; k < 3; ++k) ev[k] = m[k][k];
+}
+
 template <class T> void eig3_moduli(const T* a, T* mods) {
+  if constexpr (std::is_same<T, double>::value) {
+    if (eig3_symmetric(a)) {
+      eig3_jacobi(a, mods);
+      for (int k = 0; k < 3; ++k) mods[k] = std::fabs(mods[k]);
+      return;
+    }
+  }
   T c2 = (M3(a, 0, 0) + M3(a, 1, 1)) + M3(a, 2, 2);
   T c1 = ((M3(a, 0, 0) * M3(a, 1, 1) - M3(a, 0, 1) * M3(a, 1, 0)) +
           (M3(a, 0, 0) * M3(a, 2, 2) - M3(a, 0, 2) * M3(a, 2, 0))) +

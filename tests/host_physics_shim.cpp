@@ -18,6 +18,7 @@ double hs_entropy(const double* ep, double e, const double* G) { return entropy_
 void hs_stress(const double* ep, double S, const double* F, double* sig) { stress_SF(mk(ep), S, F, sig); }
 void hs_acoustic(const double* ep, double S, const double* F, double* om) { acoustic_SF(mk(ep), S, F, om); }
 double hs_spectral_radius(const double* a) { return spectral_radius(a); }
+void hs_eig_moduli3(const double* a, double* m) { eig_moduli3(a, m); }
 
 // one phase of a cell: q = [alpha, alpha*rho, alpha*rho*u(3), alpha*rho*E, alpha*rho*A(9)]
 // out: [flux(14 after alpha), u1, cmax, S, status]

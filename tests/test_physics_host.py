@@ -179,3 +179,55 @@ def test_hank2016_closed_form_matches_dual_numbers(shim, orc):
         G = orc.finger(F)
         e = shim.hs_hank_energy(P(h), ctypes.c_double(den), ctypes.c_double(pres), P(G))
         assert abs(e - orc.hank_energy(ho, den, pres, G)) <= 1e-13 * abs(e)
+
+
+def test_spectral_radius_on_hard_spectra(shim):
+    """The spectral radius (FP32 seeds and three Newton steps when the top root
+    separates by 10 %, Jacobi rotations for a symmetric matrix otherwise, deflation
+    for a general one) against numpy: symmetric matrices with well separated,
+    nearly equal (relative gaps 1e-3 ... 1e-12) and repeated top eigenvalues,
+    negative dominant eigenvalues, and general matrices whose complex pair is the
+    larger or the smaller in modulus."""
+    rng = np.random.default_rng(40)
+    worst = 0.0
+
+    def check(m, tol):
+        nonlocal worst
+        a = np.ascontiguousarray(m.reshape(-1, order="F"))
+        ref = np.max(np.abs(np.linalg.eigvals(m)))
+        err = abs(shim.hs_spectral_radius(P(a)) - ref) / ref
+        worst = max(worst, err)
+        assert err < tol, (m, err)
+
+    for gap in [0.5, 1e-1, 1e-3, 1e-6, 1e-9, 1e-12, 0.0]:
+        for sign in (1.0, -1.0):
+            for _ in range(20):
+                Qm, _r = np.linalg.qr(rng.standard_normal((3, 3)))
+                top = rng.uniform(1, 50)
+                lam = sign * np.array([top, top * (1 - gap), rng.uniform(-0.5, 0.5) * top])
+                check(Qm @ np.diag(lam) @ Qm.T, 1e-13)
+    for _ in range(200):  # general real matrices: a real root and a complex pair
+        th = rng.uniform(0.1, 3.0)
+        rad, r = rng.uniform(0.5, 5.0), rng.uniform(-5.0, 5.0)
+        B = np.array([[rad * np.cos(th), -rad * np.sin(th), 0], [rad * np.sin(th), rad * np.cos(th), 0], [0, 0, r]])
+        S = rng.standard_normal((3, 3)) + 3 * np.eye(3)
+        check(S @ B @ np.linalg.inv(S), 1e-11)
+    print(f"spectral radius worst relative error {worst:.1e}")
+
+
+def test_eigen_moduli_with_repeated_roots(shim):
+    """All three moduli (the function-level get_eigvals): symmetric matrices with a
+    repeated pair -- the acoustic tensor at rest has c0^2 once and b0^2 twice --
+    agree with numpy to a few ulps of the largest."""
+    rng = np.random.default_rng(41)
+    worst = 0.0
+    out = np.zeros(3)
+    for lam in ([4.6 ** 2, 2.1 ** 2, 2.1 ** 2], [3.0, 3.0, 3.0], [5.0, 5.0, -1.0], [1.0, 1.0 + 1e-9, 0.2]):
+        for _ in range(30):
+            Qm, _r = np.linalg.qr(rng.standard_normal((3, 3)))
+            m = Qm @ np.diag(lam) @ Qm.T
+            a = np.ascontiguousarray(m.reshape(-1, order="F"))
+            shim.hs_eig_moduli3(P(a), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double)))
+            ref = np.sort(np.abs(np.linalg.eigvalsh(m)))[::-1]
+            worst = max(worst, np.max(np.abs(out - ref)) / ref[0])
+    assert worst < 1e-14, worst
