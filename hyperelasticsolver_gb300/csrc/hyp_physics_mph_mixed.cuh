@@ -233,8 +233,7 @@ __device__ __forceinline__ int path_integral_add_m(const Eos2M& E, const Quad6F&
 
 // Path-conservative HLL fluctuations of one face (hll_face2 in FP32).
 __device__ __forceinline__ int hll_face2_m(const Eos2M& E, const Quad6F& qd, const float* QL, const float* QR,
-                                           const float* fl, const float* fr, float sminL, float smaxR, float* dm,
-                                           float* dp) {
+                                           const float* dF, float sminL, float smaxR, float* dm, float* dp) {
   float Qm[30];
   for (int k = 0; k < 30; ++k) Qm[k] = 0.5f * (QL[k] + QR[k]);
   float mmin = 0.0f, mmax = 0.0f;
@@ -250,19 +249,15 @@ __device__ __forceinline__ int hll_face2_m(const Eos2M& E, const Quad6F& qd, con
   for (int k = 0; k < 30; ++k) acc[k] = 0.0f;
   st |= path_integral_add_m(E, qd, QL, QR, acc);
   for (int k = 0; k < 30; ++k) {
-    const float pint = (acc[k] + fr[k]) - fl[k];
-    Qh[k] = ((QR[k] * sr - QL[k] * sl) - pint) * idsr;
-  }
-  float b2[30];
-  for (int k = 0; k < 30; ++k) {
+    Qh[k] = ((QR[k] * sr - QL[k] * sl) - (acc[k] + dF[k])) * idsr;
     acc[k] = 0.0f;
-    b2[k] = 0.0f;
   }
+  // B_int(Q_l, Q_hll) + B_int(Q_hll, Q_r) in one accumulator
   st |= path_integral_add_m(E, qd, QL, Qh, acc);
-  st |= path_integral_add_m(E, qd, Qh, QR, b2);
+  st |= path_integral_add_m(E, qd, Qh, QR, acc);
   const float cm = (-sl) * idsr, cp = sr * idsr, cq = (sl * sr) * idsr;
   for (int k = 0; k < 30; ++k) {
-    const float inner = ((fr[k] - fl[k]) + acc[k]) + b2[k];
+    const float inner = dF[k] + acc[k];
     const float jump = QR[k] - QL[k];
     dm[k] = cm * inner + cq * jump;
     dp[k] = cp * inner - cq * jump;

@@ -76,7 +76,8 @@ __global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
   } else {
     float QL[30], QR[30], fl[30], fr[30];
     load_face_states(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
-    const int st = hll_face2_m(E, qd, QL, QR, fl, fr, smin[L], smax[R], dm, dp);
+    for (int v = 0; v < 30; ++v) fr[v] -= fl[v];  // f(Q_r) - f(Q_l)
+    const int st = hll_face2_m(E, qd, QL, QR, fr, smin[L], smax[R], dm, dp);
     if (st) record_err2m(S, st, R);
   }
   for (int v = 0; v < 30; ++v) {
@@ -85,7 +86,10 @@ __global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
   }
 }
 
-__global__ void __launch_bounds__(kFaceBlockM) face2_lxf_mixed_kernel(
+// 128 registers (8 blocks of 64 per SM) with a small spill: 2.00 ms per step at 2^22
+// cells against 2.36 ms at its natural 197 registers. The HLL face kernel, with three
+// path integrals live, spills heavily under the same cap and stays uncapped.
+__global__ void __launch_bounds__(kFaceBlockM, 8) face2_lxf_mixed_kernel(
     const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, Quad6F lobatto, const float* __restrict__ F,
     int64_t fpitch, const unsigned long long* lam_now, double cfl, double dx, float* __restrict__ FF,
     float* __restrict__ DM, float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
