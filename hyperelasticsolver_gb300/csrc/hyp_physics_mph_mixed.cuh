@@ -223,10 +223,12 @@ __device__ __forceinline__ int path_integral_add_m(const Eos2M& E, const Quad6F&
   int st = 0;
   float u[30], bc[30];
   for (int i = 0; i < 6; ++i) {
-    const float s = qd.x[i], oms = 1.0f - s;
-    for (int k = 0; k < 30; ++k) u[k] = Qa[k] * oms + Qb[k] * s;
+    const float s = qd.x[i];
+    for (int k = 0; k < 30; ++k) u[k] = fmaf(s, Qb[k] - Qa[k], Qa[k]);  // Qa + s (Qb - Qa)
     st |= noncons_bcol_m(E, u, bc);
-    for (int k = 0; k < 30; ++k) acc[k] += (qd.w[i] * bc[k]) * (k < 15 ? da0 : da1);
+    const float wd0 = qd.w[i] * da0, wd1 = qd.w[i] * da1;
+    for (int k = 0; k < 30; ++k)
+      if (k != 1 && k != 16) acc[k] = fmaf(bc[k], k < 15 ? wd0 : wd1, acc[k]);  // rows 1 and 16 of B are 0
   }
   return st;
 }
