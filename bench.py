@@ -401,7 +401,7 @@ def run_mph(args):
     res = {}
     clocks = None
     for prec in ("mixed", "fp64"):
-        with h.Solver(eos, n, model="multi", flux="hll", precision=prec, cfl=0.5) as s:
+        with h.Solver(eos, n, model="multi", flux=args.flux, precision=prec, cfl=0.5) as s:
             s.upload(Q0)
             s.step(max_steps=W)
             s.set_profiling(True)
@@ -423,7 +423,7 @@ def run_mph(args):
     line = {"metric": METRIC, "value": n * K / (tm["ms_total"] / 1e3), "unit": METRIC, "n_gpus": 1, "steps": K,
             "warmup": W, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
             "dtype": "f32", "data": "synthetic",
-            "config": {"workload": f"two-phase HLL path-conservative step, {n} cells, alpha1 1-1e-6 -> 1e-6 over "
+            "config": {"workload": f"two-phase {args.flux.upper()} path-conservative step, {n} cells, alpha1 1-1e-6 -> 1e-6 over "
                                    "8 cells, phase 2 shear modulus x0.1", "l2": "inputs larger than L2"},
             "precision": "FP32 two-phase physics and fluxes, compensated hi/lo FP32 state, float-float cons2prim "
                          "islands per phase", "clocks": clocks,
@@ -502,6 +502,84 @@ def run_adjoint(args):
     return 0
 
 
+def run_evaluators(args):
+    """Function-level API workload: each evaluator that a per-cell function of the
+    reference maps to (Strains, EquationsOfState, Hyperelasticity, HyperelasticityMPh,
+    NumFluxes; Barton2009 and Hank2016), called on n seeded cells with host arrays in and
+    out, so the timed call holds the device allocation, both copies and the kernel.
+    Per evaluator: cells/s of the whole call (median of --steps calls after --warmup
+    untimed ones)."""
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300 import Strains as St, EquationsOfState as E, Hyperelasticity as H
+    from hyperelasticsolver_gb300 import HyperelasticityMPh as HM, NumFluxes as NF
+    from hyperelasticsolver_gb300._cases import mph_interface_prims
+    h.build_library()
+    n = args.n_cells
+    rng = np.random.default_rng(20261204)
+    eos, hank = h.Barton2009(), E.Hank2016()
+    eos2 = (h.Barton2009(), h.Barton2009(_b0=2.1 * np.sqrt(0.1)))
+    A = np.tile(np.eye(3).reshape(1, 9, order="F"), (n, 1)) + 0.03 * rng.standard_normal((n, 9))
+    S = rng.uniform(0.0, 1e-3, n)
+    P = np.empty((n, 14))
+    P[:, 0] = 8.93 * rng.uniform(0.95, 1.05, n)
+    P[:, 1:4] = rng.uniform(-0.5, 0.5, (n, 3))
+    P[:, 4] = S
+    P[:, 5:] = A
+    Q = H.prim2cons(eos, P)
+    P2 = mph_interface_prims(eos2[0], n)
+    Q2 = HM.prim2cons_mph(eos2, P2)
+    G = St.finger(A)
+    inv = St.invariants(G)
+    e_int = E.energy(eos, S, G)
+    den = 2.7 * rng.uniform(0.95, 1.05, n)
+    pres = rng.uniform(0.0, 1e9, n)
+    lam = np.max(np.abs(H.get_eigvals(eos, Q)), axis=1)
+    calls = {
+        "Strains.finger": lambda: St.finger(A),
+        "Strains.invariants": lambda: St.invariants(G),
+        "EquationsOfState.energy": lambda: E.energy(eos, S, G),
+        "EquationsOfState.entropy": lambda: E.entropy(eos, e_int, G),
+        "EquationsOfState.stress": lambda: E.stress(eos, S, A),
+        "EquationsOfState.acoustic": lambda: E.acoustic(eos, S, A),
+        "Hyperelasticity.prim2cons": lambda: H.prim2cons(eos, P),
+        "Hyperelasticity.cons2prim": lambda: H.cons2prim(eos, Q),
+        "Hyperelasticity.flux": lambda: H.flux(eos, Q),
+        "Hyperelasticity.get_eigvals": lambda: H.get_eigvals(eos, Q),
+        "NumFluxes.lxf (one phase)": lambda: NF.lxf(eos, Q[:-1], Q[1:], lam[1:]),
+        "HyperelasticityMPh.prim2cons_mph": lambda: HM.prim2cons_mph(eos2, P2),
+        "HyperelasticityMPh.cons2prim_mph": lambda: HM.cons2prim_mph(eos2, Q2),
+        "HyperelasticityMPh.flux_mph": lambda: HM.flux_mph(eos2, Q2),
+        "HyperelasticityMPh.get_eigvals": lambda: HM.get_eigvals(eos2, Q2),
+        "HyperelasticityMPh.noncons_flux": lambda: HM.noncons_flux(eos2, Q2),
+        "NumFluxes.hll (two phases)": lambda: NF.hll(eos2, Q2[:-1], Q2[1:]),
+        "NumFluxes.lxf (two phases)": lambda: NF.lxf(eos2, Q2[:-1], Q2[1:], 10.0),
+        "Hank2016 energy": lambda: E.energy(hank, den, pres, G),
+        "Hank2016 pressure": lambda: E.pressure(hank, den, e_int, inv),
+        "Hank2016 stress": lambda: E.stress(hank, den, pres, A),
+    }
+    rates, total_s = {}, 0.0
+    for name, f in calls.items():
+        for _ in range(args.warmup):
+            f()
+        ts = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            f()
+            ts.append(time.perf_counter() - t0)
+        t = sorted(ts)[len(ts) // 2]
+        total_s += t
+        rates[name] = n / t
+    unit = "cell evaluations/s"
+    line = {"metric": "function-level evaluations/s (host arrays in and out)", "value": len(calls) * n / total_s,
+            "unit": unit, "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total_s / len(calls),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"every function-level evaluator on {n} seeded cells, one call each, host arrays "
+                                   "(allocation, copies and kernel timed)", "n_cells": n},
+            "per_evaluator": rates}
+    print(json.dumps(line))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -515,16 +593,17 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
-    ap.add_argument("--workload", choices=["single", "batch", "mph", "adjoint"], default="single",
+    ap.add_argument("--workload", choices=["single", "batch", "mph", "adjoint", "evaluators"], default="single",
                     help="single: the headline single-phase step; batch: 4096 ragged problems; mph: two-phase HLL; "
-                         "adjoint: gradient of a 1000-step run")
+                         "adjoint: gradient of a 1000-step run; evaluators: the function-level API")
+    ap.add_argument("--flux", choices=["hll", "lxf"], default="hll", help="two-phase workload's face flux")
     ap.add_argument("--ckpt-every", type=int, default=50)
     ap.add_argument("--problems", type=int, default=4096)
     args = ap.parse_args()
     if args.warmup < 1:
         ap.error("--warmup must be >= 1")
-    steps = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000}
-    cells = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536}
+    steps = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000, "evaluators": 3}
+    cells = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536, "evaluators": 1 << 20}
     wl = "single" if args.impl == "reference" else args.workload
     if args.steps is None:
         args.steps = steps[wl]
@@ -532,7 +611,8 @@ def main():
         args.n_cells = cells[wl]
     if args.impl == "reference":
         return run_reference(args)
-    runner = {"batch": run_batch, "adjoint": run_adjoint, "mph": run_mph}.get(args.workload, run_ours)
+    runner = {"batch": run_batch, "adjoint": run_adjoint, "mph": run_mph,
+              "evaluators": run_evaluators}.get(args.workload, run_ours)
     return runner(args)
 
 
