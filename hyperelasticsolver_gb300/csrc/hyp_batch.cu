@@ -164,13 +164,17 @@ __global__ void __launch_bounds__(kBlock) batch_f64_cell_kernel(const double* __
   }
 }
 
+// One tile of kBlock cells per block iteration (tile_cells == kBlock for the FP64
+// batch); each face of the tile once into shared memory, as update1_f64_kernel.
 __global__ void __launch_bounds__(kBlock) batch_f64_update_kernel(const double* __restrict__ Q, double* __restrict__ Qn,
                                                                   int64_t n, const double* __restrict__ F,
                                                                   const double* __restrict__ lam,
                                                                   const TileDesc* __restrict__ tiles, int ntiles,
                                                                   int tile_cells, BatchDev b, int par, double t_end,
                                                                   double cfl, int flux, int bc) {
+  __shared__ double sF[14][kBlock + 1];  // face k of the tile = left face of cell first + k
   const int P = b.P;
+  const bool lxf = flux == HYP_FLUX_LXF;
   for (int tix = blockIdx.x; tix < ntiles; tix += gridDim.x) {
     const TileDesc d = tiles[tix];
     const int p = d.problem;
@@ -180,49 +184,34 @@ __global__ void __launch_bounds__(kBlock) batch_f64_update_kernel(const double* 
     const double dx = b.dx[p];
     const double dt = (cfl * dx) / lmax;
     const double lam_lxf = dx / dt;
-    const double dtdx = flux == HYP_FLUX_LXF ? 1.0 / lam_lxf : dt / dx;
+    const double dtdx = lxf ? 1.0 / lam_lxf : dt / dx;
     if (d.lead && threadIdx.x == 0) {
       b.t[(1 - par) * P + p] = active ? tn + dt : tn;
       b.slots[(1 - par) * P + p] = 0ull;
       if (active) b.steps[p] += 1;
     }
-    if (!active) {  // a finished problem's cells go to the other buffer unchanged
-      for (int64_t i = d.first + threadIdx.x; i < d.first + tile_cells && i < d.hi; i += kBlock)
+    const int64_t i = d.first + threadIdx.x;
+    const bool own = (int)threadIdx.x < tile_cells && i < d.hi;
+    if (!active) {  // a finished problem's cells go to the other buffer unchanged (uniform per tile)
+      if (own)
         for (int v = 0; v < 14; ++v) Qn[v * n + i] = Q[v * n + i];
       continue;
     }
-    for (int64_t i = d.first + threadIdx.x; i < d.first + tile_cells && i < d.hi; i += kBlock) {
-      if (bc == HYP_BC_FROZEN && (i == d.lo || i == d.hi - 1)) {
-#pragma unroll
-        for (int v = 0; v < 14; ++v) Qn[v * n + i] = Q[v * n + i];
-        continue;
-      }
-      const int64_t il = i > d.lo ? i - 1 : d.lo, ir = i < d.hi - 1 ? i + 1 : d.hi - 1;
-      const double lc = lam[i];
-      double lamL, lamR;
-      if (flux == HYP_FLUX_LXF) {
-        lamL = lamR = lam_lxf;
-      } else {
-        const double ll = lam[il], lr = lam[ir];
-        lamL = ll > lc ? ll : lc;
-        lamR = lc > lr ? lc : lr;
-      }
-      const double hl = lamL * 0.5, hr = lamR * 0.5;
+    if (own) {
+      rusanov_face<kBlock + 1>(Q, F, lam, n, d.lo, d.hi, i, lxf, lam_lxf, sF, threadIdx.x);
+      if ((int)threadIdx.x == tile_cells - 1 || i == d.hi - 1)
+        rusanov_face<kBlock + 1>(Q, F, lam, n, d.lo, d.hi, i + 1, lxf, lam_lxf, sF, threadIdx.x + 1);
+    }
+    __syncthreads();
+    if (own) {
+      const bool frozen = bc == HYP_BC_FROZEN && (i == d.lo || i == d.hi - 1);
 #pragma unroll
       for (int v = 0; v < 14; ++v) {
-        const double qc = Q[v * n + i], ql = Q[v * n + il], qr = Q[v * n + ir];
-        const int sl = flux_slot1(v);
-        double fl = 0.0, fc = 0.0, fr = 0.0;
-        if (sl >= 0) {
-          fl = F[sl * n + il];
-          fc = F[sl * n + i];
-          fr = F[sl * n + ir];
-        }
-        const double FL = 0.5 * (fl + fc) - hl * (qc - ql);
-        const double FR = 0.5 * (fc + fr) - hr * (qr - qc);
-        Qn[v * n + i] = qc - dtdx * (FR - FL);
+        const double qc = Q[v * n + i];
+        Qn[v * n + i] = frozen ? qc : __fma_rn(-dtdx, __dsub_rn(sF[v][threadIdx.x + 1], sF[v][threadIdx.x]), qc);
       }
     }
+    __syncthreads();  // the next tile rewrites the face table
   }
 }
 

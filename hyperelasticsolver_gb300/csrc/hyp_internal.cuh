@@ -42,6 +42,36 @@ __host__ __device__ __forceinline__ int flux_slot1(int v) {
   return 5 + 2 * b + (a - 1);
 }
 
+// The Rusanov face flux 0.5 (f_a + f_b) - h (q_b - q_a), h = max(lambda_a, lambda_b)/2
+// (NumFluxes.jl:25-33, main.jl:45-48), with one fixed rounding sequence (explicit
+// intrinsics, no compiler contraction), so the step commutes with x -> -x.
+__device__ __forceinline__ double face_flux(double fa, double fb, double h, double qa, double qb) {
+  return __fma_rn(-h, __dsub_rn(qb, qa), __dmul_rn(0.5, __dadd_rn(fa, fb)));
+}
+
+// Face f of a block's face table (between cells f - 1 and f of the problem [lo, hi),
+// a zero-gradient ghost past either end) into slot k: its 14 flux components.
+template <int kSlots>
+__device__ __forceinline__ void rusanov_face(const double* __restrict__ Q, const double* __restrict__ F,
+                                             const double* __restrict__ lam, int64_t n, int64_t lo, int64_t hi,
+                                             int64_t f, bool lxf, double lam_lxf, double (*sF)[kSlots], int k) {
+  const int64_t a = f > lo ? f - 1 : lo, b = f < hi ? f : hi - 1;
+  double lf;
+  if (lxf) {
+    lf = lam_lxf;
+  } else {
+    const double la = lam[a], lb = lam[b];
+    lf = la > lb ? la : lb;  // max(lambda_L, lambda_R) (main.jl:45-48)
+  }
+  const double h = lf * 0.5;
+#pragma unroll
+  for (int v = 0; v < 14; ++v) {
+    const int sl = flux_slot1(v);
+    const double fa = sl >= 0 ? F[sl * n + a] : 0.0, fb = sl >= 0 ? F[sl * n + b] : 0.0;
+    sF[v][k] = face_flux(fa, fb, h, Q[v * n + a], Q[v * n + b]);
+  }
+}
+
 // The two phases' EOS, passed to the two-phase kernels by value.
 struct Eos2 {
   EosC e[2];

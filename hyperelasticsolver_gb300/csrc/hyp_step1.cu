@@ -64,35 +64,6 @@ __global__ void __launch_bounds__(kBlock) cell1_f64_kernel(const double* __restr
   if (threadIdx.x == 0) atomicMax(lam_slot, (unsigned long long)__double_as_longlong(m));
 }
 
-// The Rusanov face flux 0.5 (f_a + f_b) - h (q_b - q_a) with one fixed rounding
-// sequence (explicit intrinsics, no compiler contraction), so the step commutes
-// with x -> -x.
-__device__ __forceinline__ double face_flux(double fa, double fb, double h, double qa, double qb) {
-  return __fma_rn(-h, __dsub_rn(qb, qa), __dmul_rn(0.5, __dadd_rn(fa, fb)));
-}
-
-// Face f of the block (between cells f - 1 and f, a zero-gradient ghost past either
-// end) into slot k of the block's face table: its 14 flux components.
-__device__ __forceinline__ void rusanov_face(const double* __restrict__ Q, const double* __restrict__ F,
-                                             const double* __restrict__ lam, int64_t n, int64_t f, bool lxf,
-                                             double lam_lxf, double (*sF)[kBlock + 1], int k) {
-  const int64_t a = f > 0 ? f - 1 : 0, b = f < n ? f : n - 1;
-  double lf;
-  if (lxf) {
-    lf = lam_lxf;
-  } else {
-    const double la = lam[a], lb = lam[b];
-    lf = la > lb ? la : lb;  // max(lambda_L, lambda_R) (main.jl:45-48)
-  }
-  const double h = lf * 0.5;
-#pragma unroll
-  for (int v = 0; v < 14; ++v) {
-    const int sl = flux_slot1(v);
-    const double fa = sl >= 0 ? F[sl * n + a] : 0.0, fb = sl >= 0 ? F[sl * n + b] : 0.0;
-    sF[v][k] = face_flux(fa, fb, h, Q[v * n + a], Q[v * n + b]);
-  }
-}
-
 // Each face is evaluated once, by the block that owns the cell on its right (the
 // block's last cell also evaluates its right face), into shared memory; both cells
 // of a face read the same value, so the update conserves exactly.
@@ -121,8 +92,9 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
   const int64_t i = i0 + threadIdx.x;
   const bool lxf = flux == HYP_FLUX_LXF;
   if (i < n) {
-    rusanov_face(Q, F, lam, n, i, lxf, lam_lxf, sF, threadIdx.x);
-    if (threadIdx.x == kBlock - 1 || i == n - 1) rusanov_face(Q, F, lam, n, i + 1, lxf, lam_lxf, sF, threadIdx.x + 1);
+    rusanov_face<kBlock + 1>(Q, F, lam, n, 0, n, i, lxf, lam_lxf, sF, threadIdx.x);
+    if (threadIdx.x == kBlock - 1 || i == n - 1)
+      rusanov_face<kBlock + 1>(Q, F, lam, n, 0, n, i + 1, lxf, lam_lxf, sF, threadIdx.x + 1);
   }
   __syncthreads();
   if (i >= n) return;
