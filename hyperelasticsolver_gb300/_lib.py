@@ -90,6 +90,7 @@ _SIGS = {
     "hyp_last_timing": ([ctypes.c_void_p, _dp, _dp, ctypes.POINTER(ctypes.c_int), _dp, ctypes.POINTER(ctypes.c_int)],
                         ctypes.c_int),
     "hyp_set_mixed_kernel": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "hyp_set_wait_limit": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "hyp_step_noalloc_f64": ([ctypes.POINTER(ConfigC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_double, ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "hyp_batch_create": ([ctypes.POINTER(ConfigC), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,

@@ -408,6 +408,18 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
   return check_cell_error(c);
 }
 
+extern "C" int hyp_set_wait_limit(hyp_ctx* c, int tries) {
+  if (!c || tries < 0) return HYP_ERR_INVALID;
+  c->wait_tries = tries;
+  for (auto& g : c->graph)  // graphs hold the previous kernel arguments
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  c->graph_steps = 0;
+  return HYP_OK;
+}
+
 extern "C" int hyp_set_mixed_kernel(hyp_ctx* c, int tma) {
   if (!c) return HYP_ERR_INVALID;
   if (!mixed(c) || c->cfg.model != HYP_MODEL_SINGLE)

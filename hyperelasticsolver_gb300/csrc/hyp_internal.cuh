@@ -116,6 +116,7 @@ struct hyp_ctx {
   int64_t mpitch = 0;                   // row pitch (floats, a multiple of 4)
   CUtensorMap tmap;                     // TMA map over mixed_base (both parities)
   int mixed_tma = 0;                    // step with the TMA-prefetched persistent kernel
+  int wait_tries = hyp::kWaitTries;     // poll budget of the TMA kernel's barrier waits
   int tma_grid = 0;
   hyp::EosMixed eos_mixed;
   // two-phase (FP64): cell fluxes F [30][n], wave-speed bounds, face fluctuations [30][n+1]

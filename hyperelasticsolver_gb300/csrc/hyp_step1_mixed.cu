@@ -128,7 +128,8 @@ __device__ __forceinline__ int64_t stage_x0(int64_t first) { return (first - 1) 
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB)
     step1_mixed_tma_kernel(const __grid_constant__ CUtensorMap map, MixedArrays a, EosMixed em, MixedSlots sl,
-                           DevState* S, double t_end, double cfl, double dx, int flux, int bc, int ntiles) {
+                           DevState* S, double t_end, double cfl, double dx, int flux, int bc, int ntiles,
+                           int wait_tries) {
   extern __shared__ __align__(128) float stage_raw[];
   __shared__ __align__(8) uint64_t bar;
   float dtdx;
@@ -151,9 +152,12 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   unsigned phase = 0;
   float m = 0.0f;
   for (; tile < ntiles; tile += gridDim.x) {
-    const bool ok = mbar_wait_bounded(&bar, phase);
+    const bool ok = mbar_wait_bounded(&bar, phase, wait_tries);
     if (__syncthreads_or(!ok)) {
       if (threadIdx.x == 0) mixed_record_err(S, HYP_CELL_TIMEOUT, tile * kT);
+      // the awaited box copy is the block's only one in flight: let it land (again a
+      // bounded wait) before the block's shared memory goes away
+      mbar_wait_bounded(&bar, phase, kDrainTries);
       return;
     }
     phase ^= 1u;
@@ -273,7 +277,8 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   if (c->mixed_tma) {
     const int ntiles = (int)((c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2));
     step1_mixed_tma_kernel<kTmaBlock, kTmaMinB><<<c->tma_grid, kTmaBlock, TmaTile<kTmaBlock>::kSmem, c->stream>>>(
-        c->tmap, arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc, ntiles);
+        c->tmap, arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc, ntiles,
+        c->wait_tries);
   } else {
     const unsigned grid = (unsigned)((c->n + kTileM - 1) / kTileM);
     step1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl,

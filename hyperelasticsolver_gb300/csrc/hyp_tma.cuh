@@ -48,7 +48,9 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
 // Waits for the completion of the barrier phase with the given parity; false
 // if it has not completed after `tries` polls (each try_wait may itself block
 // for a bounded, implementation-defined time).
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int tries = 1 << 20) {
+constexpr int kWaitTries = 1 << 20;   // default poll budget of a device wait
+constexpr int kDrainTries = 1 << 20;  // budget for letting an in-flight copy land after a timeout
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, int tries = kWaitTries) {
   for (int k = 0; k < tries; ++k)
     if (mbar_try_wait(bar, parity)) return true;
   return false;

@@ -85,6 +85,10 @@ class Solver:
             raise ValueError("kernel must be 'tma' or 'tile'")
         L.check(L.load().hyp_set_mixed_kernel(self._h, int(kernel == "tma")), self._h, "hyp_set_mixed_kernel")
 
+    def set_wait_limit(self, tries):
+        """Poll budget of the TMA kernel's device waits; 0 makes each wait time out at once."""
+        L.check(L.load().hyp_set_wait_limit(self._h, int(tries)), self._h, "hyp_set_wait_limit")
+
     def set_profiling(self, on):
         L.check(L.load().hyp_set_profiling(self._h, int(bool(on))), self._h, "hyp_set_profiling")
 

@@ -129,6 +129,13 @@ int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_
    (tma = 0, the default, faster on GB300). Both run the same tile arithmetic. */
 int hyp_set_mixed_kernel(hyp_ctx* ctx, int tma);
 
+/* Poll budget of the TMA kernel's device-side barrier waits (default 2^20). A wait
+   that runs out records HYP_CELL_TIMEOUT, lets its in-flight copy land and ends the
+   block, and the step returns HYP_ERR_TIMEOUT; the context stays usable (upload a
+   state again). A budget of 0 makes every wait run out at once: the timeout path
+   exercised without a fault. */
+int hyp_set_wait_limit(hyp_ctx* ctx, int tries);
+
 /* ---- batches of independent single-phase problems -------------------------- */
 /* The reference advances one problem per main.jl run (main.jl:202-241). A batch
    advances n_problems independent problems of uneven size in lockstep, each with

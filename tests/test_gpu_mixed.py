@@ -154,3 +154,33 @@ def test_tma_and_tile_kernels_agree(hyp, orc, nx, bc):
     (ta, sa), (tb, sb) = out[0][1], out[1][1]
     assert sa == sb and abs(ta - tb) <= 1e-6 * tb
     assert abs(out[0][2] - out[1][2]) <= 1e-6 * out[1][2]
+
+
+def test_tma_wait_timeout_is_reported_and_recoverable(hyp, orc):
+    """The TMA kernel's barrier waits are bounded. With a poll budget of 0 every wait
+    runs out at once: each block records the timeout, lets its in-flight box copy land
+    and ends, and the step reports HYP_ERR_TIMEOUT (no fault, no hang). With the
+    budget restored the same context steps a fresh upload as the tile kernel does."""
+    from hyperelasticsolver_gb300._cases import segment_states, segment_fill
+    eos = hyp.Barton2009()
+    seg = orc.prim2cons(orc.problem(cfl=0.5), segment_states(eos, 8))
+    nx = 4097
+    Q0 = segment_fill(seg, nx)
+    with hyp.Solver(eos, nx, precision="mixed") as s:
+        s.set_mixed_kernel("tma")
+        s.upload(Q0)
+        s.set_wait_limit(0)
+        with pytest.raises(hyp._lib.HypError) as err:
+            s.step(max_steps=3)
+        assert err.value.code == hyp._lib.HYP_ERR_TIMEOUT
+        s.set_wait_limit(1 << 20)
+        s.upload(Q0)
+        n, _ = s.step(max_steps=20)
+        assert n == 20
+        Qa = s.download()
+    with hyp.Solver(eos, nx, precision="mixed") as t:
+        t.upload(Q0)
+        t.step(max_steps=20)
+        Qb = t.download()
+    scale = np.maximum(np.max(np.abs(Qb), axis=1, keepdims=True), 1e-30)
+    assert np.max(np.abs(Qa - Qb) / scale) <= 1e-6
