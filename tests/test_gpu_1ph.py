@@ -272,3 +272,32 @@ def test_profiling_counts_launches(hyp, orc):
         tm = s.timing()
         assert tm["n_cell"] == 20 and tm["n_update"] == 20
         assert 0 < tm["ms_cell"] <= tm["ms_total"] and math.isfinite(tm["ms_update"])
+
+
+def test_contexts_on_concurrent_host_threads(hyp, orc):
+    """One context per host thread: two threads stepping their own contexts at the
+    same time (the ctypes calls release the GIL) get the bits each context gets alone."""
+    import threading
+    from hyperelasticsolver_gb300._cases import segment_states, segment_fill
+    eos = hyp.Barton2009()
+    seg = orc.prim2cons(orc.problem(cfl=0.5), segment_states(eos, 8))
+    jobs = [("fp64", segment_fill(seg, 3001)), ("mixed", segment_fill(seg[::-1].copy(), 5003))]
+
+    def run(prec, Q0, out, k):
+        with hyp.Solver(eos, Q0.shape[1], precision=prec) as s:
+            s.upload(Q0)
+            for _ in range(5):
+                s.step(max_steps=8)
+            out[k] = (s.download(), s.time())
+
+    alone = {}
+    for k, (prec, Q0) in enumerate(jobs):
+        run(prec, Q0, alone, k)
+    together = {}
+    threads = [threading.Thread(target=run, args=(prec, Q0, together, k)) for k, (prec, Q0) in enumerate(jobs)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    for k in range(len(jobs)):
+        assert np.array_equal(alone[k][0], together[k][0]) and alone[k][1] == together[k][1]
