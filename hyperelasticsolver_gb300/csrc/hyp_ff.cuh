@@ -16,9 +16,7 @@ struct ff {
   float hi, lo;
 };
 
-__device__ __forceinline__ ff ff_make(float h) { return ff{h, 0.0f}; }
 __device__ __forceinline__ float ff_val(ff a) { return __fadd_rn(a.hi, a.lo); }
-__device__ __forceinline__ double ff_to_double(ff a) { return (double)a.hi + (double)a.lo; }
 
 // s + e == a + b exactly
 __device__ __forceinline__ ff two_sum(float a, float b) {
@@ -88,14 +86,6 @@ __device__ __forceinline__ ff ff_diff_prod(float a, float b, float c, float d) {
   ff p = two_prod(a, b);
   ff q = two_prod(c, d);
   return ff_sub(p, q);
-}
-
-// Compensated accumulation of an FP32 increment into a stored (hi, lo) pair.
-__device__ __forceinline__ void ff_accumulate(float& hi, float& lo, float delta) {
-  ff s = two_sum(hi, __fadd_rn(lo, delta));
-  ff r = fast_two_sum(s.hi, s.lo);
-  hi = r.hi;
-  lo = r.lo;
 }
 
 }  // namespace hyp
