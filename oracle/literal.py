@@ -359,6 +359,55 @@ def hll(eos, Ql, Qr, spdL, spdR):  # NumFluxes.jl:70-132
     return dm, dp
 
 
+def gauss_lobatto6():
+    """Six-point Gauss-Lobatto rule on [0, 1] (FastGaussQuadrature's gausslobatto(6),
+    NumFluxes.jl:36-37): the end points and the roots of P5', weights
+    2 / (n (n - 1) P5(x)^2) on [-1, 1]."""
+    d5 = lambda t: mp.diff(lambda y: mp.legendre(5, y), t)  # noqa: E731
+    inner = sorted(mp.re(r) for r in mp.polyroots(mp.taylor(d5, 0, 4)[::-1], maxsteps=200, extraprec=200))
+    x = [mp.mpf(-1)] + inner + [mp.mpf(1)]
+    w = [mp.mpf(2) / (30 * mp.legendre(5, t) ** 2) for t in x]
+    return [(xi + 1) / 2 for xi in x], [wi / 2 for wi in w]
+
+
+def lxf2(eos, Ql, Qr, lam):  # NumFluxes.jl:25-60, two phases
+    fl = flux(eos[0], Ql[:15]) + flux(eos[1], Ql[15:])
+    fr = flux(eos[0], Qr[:15]) + flux(eos[1], Qr[15:])
+    cons = [mp.mpf("0.5") * (fl[k] + fr[k]) - mp.mpf("0.5") * lam * (Qr[k] - Ql[k]) for k in range(30)]
+    x, w = gauss_lobatto6()
+    fp = path_integral(eos, x, w, Ql, Qr)
+    half = [fp[k] / 2 for k in range(30)]
+    return cons, half, list(half)
+
+
+# --- Hank2016 (EquationsOfState.jl:305-366) ---
+class Hank:
+    def __init__(self, rho0=2.7, mu=26e9, gamma=3.4, pres_inf=21.5e9, a=0.5):
+        self.rho0, self.mu, self.gamma = mp.mpf(rho0), mp.mpf(mu), mp.mpf(gamma)
+        self.pres_inf, self.a = mp.mpf(pres_inf), mp.mpf(a)
+
+
+def _hank_e_el(h, i):
+    j1 = i[0] / i[2] ** (mp.mpf(1) / 3)
+    j2 = (i[0] ** 2 - 2 * i[1]) / i[2] ** (mp.mpf(2) / 3)
+    return h.mu / (4 * h.rho0) * ((1 - 2 * h.a) / 3 * j1 ** 2 + h.a * j2 + 3 * (h.a - 1))
+
+
+def hank_energy(h, den, pres, G):  # :321-336
+    return _hank_e_el(h, invariants(G)) + (pres + h.gamma * h.pres_inf) / (den * (h.gamma - 1))
+
+
+def hank_pressure(h, den, e_int, i):  # :338-352
+    return (e_int - _hank_e_el(h, i)) * (h.gamma - 1) * den - h.gamma * h.pres_inf
+
+
+def hank_stress(h, den, pres, F):  # :354-361
+    G = finger(inv_(F))
+    dedG = gradient(lambda g: hank_energy(h, den, pres, g), G)
+    a = [-2 * den * g for g in G]
+    return [_mm(a, dedG, i, j) for j in range(3) for i in range(3)]
+
+
 # --- single-phase (alpha == 1) Rusanov step of main.jl:202-227 on a small grid ---
 def rusanov_step(e, Q, cfl, X=1, frozen=True):
     """Q: list of 14-vectors. Returns (new Q, dt)."""

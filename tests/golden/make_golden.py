@@ -24,7 +24,7 @@ def main():
     e = L.Barton()
     e2 = L.Barton(b0=2.1 * np.sqrt(0.1))
     g = {"eos": [8.93, 4.6, 3.9e-4, 300, 2.1, 1, 3, 2], "eos2_b0": 2.1 * float(np.sqrt(0.1)), "tensors": [],
-         "cells": [], "noncons": [], "hll": [], "rusanov": {}}
+         "cells": [], "noncons": [], "hll": [], "rusanov": {}, "lxf2": [], "hank": []}
     # tensor-level functions
     for k in range(6):
         F = np.eye(3) + 0.08 * rng.standard_normal((3, 3))
@@ -93,6 +93,27 @@ def main():
         dts.append(float(dt))
     g["rusanov"]["Q2"] = [[float(x) for x in c] for c in Q]
     g["rusanov"]["dt"] = dts
+    # the two-phase LxF face (Gauss-Lobatto path integral) on the test case 6 states
+    lam = mp.mpf(12)
+    cons, dm, dp = L.lxf2(eos, Ql, Qr, lam)
+    g["lxf2"] = [{"Ql": [float(x) for x in Ql], "Qr": [float(x) for x in Qr], "lam": float(lam),
+                  "cons": [f(x) for x in cons], "dm": [f(x) for x in dm], "dp": [f(x) for x in dp]}]
+    # Hank2016 energy / pressure / stress at seeded states
+    h = L.Hank()
+    g["hank"] = []
+    for k in range(3):
+        F = np.eye(3) + 0.05 * rng.standard_normal((3, 3))
+        Fv = [float(x) for x in F.reshape(-1, order="F")]
+        den = float(2.7 * rng.uniform(0.95, 1.05))
+        pres = float(rng.uniform(0.0, 2e9))
+        Fm = [mp.mpf(x) for x in Fv]
+        G = L.finger(Fm)
+        inv = L.invariants(G)
+        e_int = L.hank_energy(h, mp.mpf(den), mp.mpf(pres), G)
+        g["hank"].append({"F": Fv, "den": den, "pres": pres, "G": [f(x) for x in G],
+                          "energy": f(e_int), "invariants": [f(x) for x in inv],
+                          "pressure": f(L.hank_pressure(h, mp.mpf(den), e_int, inv)),
+                          "stress": [f(x) for x in L.hank_stress(h, mp.mpf(den), mp.mpf(pres), Fm)]})
     with open(OUT, "w") as fh:
         json.dump(g, fh, indent=1)
     print("wrote", OUT)

@@ -36,3 +36,20 @@ def test_hank2016_stress_free_reference_state(hyp):
     from hyperelasticsolver_gb300 import EquationsOfState as E
     s = E.stress(E.Hank2016(), 2.7, 1e5, np.eye(3).reshape(-1))
     assert np.max(np.abs(s)) < 1e-3  # mu = 26e9: zero to rounding
+
+
+def test_hank2016_golden_vectors(hyp):
+    """Against the 40-digit transliteration's values (tests/golden)."""
+    import json
+    import os
+    from hyperelasticsolver_gb300 import EquationsOfState as E
+    with open(os.path.join(os.path.dirname(__file__), "golden", "golden_literal.json")) as fh:
+        g = json.load(fh)
+    eos = E.Hank2016()
+    for c in g["hank"]:
+        e = E.energy(eos, c["den"], c["pres"], np.array(c["G"]))
+        assert abs(e - c["energy"]) <= 1e-13 * abs(c["energy"])
+        p = E.pressure(eos, c["den"], c["energy"], np.array(c["invariants"]))
+        assert abs(p - c["pressure"]) <= 1e-13 * max(abs(c["pressure"]), 1e9)  # cancellation against gamma p_inf
+        s = E.stress(eos, c["den"], c["pres"], np.array(c["F"]))
+        assert np.max(np.abs(s - np.array(c["stress"]))) <= 1e-12 * np.max(np.abs(c["stress"]))

@@ -76,6 +76,11 @@ def test_golden_hll_face_on_gpu(hyp):
         _, dm, dp = NF.hll(eos, np.array(h["Ql"]), np.array(h["Qr"]))
         assert_close(dm, h["dm"], 1e-11, "golden hll D-")
         assert_close(dp, h["dp"], 1e-11, "golden hll D+")
+    for c in g["lxf2"]:
+        cons, dm, dp = NF.lxf(eos, np.array(c["Ql"]), np.array(c["Qr"]), c["lam"])
+        assert_close(cons, c["cons"], RTOL_FP64, "golden lxf flux")
+        assert_close(dm, c["dm"], 1e-11, "golden lxf D-")
+        assert_close(dp, c["dp"], 1e-11, "golden lxf D+")
 
 
 @pytest.mark.parametrize("flux", ["hll", "lxf"])

@@ -111,6 +111,30 @@ def test_golden_twophase_noncons_and_hll(orc, golden):
         assert rel_err(dp, h["dp"]) < 1e-12
 
 
+def test_golden_twophase_lxf(orc, golden):
+    """The two-phase LxF face (NumFluxes.jl:25-60): flux and D+- = half the
+    Gauss-Lobatto path integral, against the 40-digit transliteration."""
+    eos = (orc.barton2009(), orc.barton2009(b0=golden["eos2_b0"]))
+    pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_LXF, eos=eos)
+    for c in golden["lxf2"]:
+        cons, dm, dp = orc.lxf(pb, np.array(c["Ql"]), np.array(c["Qr"]), c["lam"])
+        assert rel_err(cons, c["cons"]) < 1e-13
+        assert rel_err(dm, c["dm"]) < 1e-12
+        assert rel_err(dp, c["dp"]) < 1e-12
+
+
+def test_golden_hank2016(orc, golden):
+    """Hank2016 energy, pressure and stress (EquationsOfState.jl:305-366) against the
+    40-digit transliteration (its own dual numbers for the stress)."""
+    h = orc.hank2016()
+    for c in golden["hank"]:
+        G = np.array(c["G"])
+        assert abs(orc.hank_energy(h, c["den"], c["pres"], G) - c["energy"]) <= 1e-13 * abs(c["energy"])
+        p = orc.hank_pressure(h, c["den"], c["energy"], np.array(c["invariants"]))
+        assert abs(p - c["pressure"]) <= 1e-13 * max(abs(c["pressure"]), 1e9)  # cancellation against gamma p_inf
+        assert rel_err(orc.hank_stress(h, c["den"], c["pres"], np.array(c["F"])), c["stress"]) < 1e-12
+
+
 def test_golden_rusanov_steps(orc, golden):
     g = golden["rusanov"]
     Q0 = np.array(g["Q0"]).T.copy()
