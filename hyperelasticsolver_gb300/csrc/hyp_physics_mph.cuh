@@ -106,7 +106,10 @@ HYP_HD int path_integral_add(const EosC* eos, const Quad6D& qd, const double* Qa
     const double s = qd.x[i], oms = 1.0 - s;
     for (int k = 0; k < 30; ++k) u[k] = Qa[k] * oms + Qb[k] * s;
     st |= noncons_bcol(eos, u, bc);
-    for (int k = 0; k < 30; ++k) acc[k] += (qd.w[i] * bc[k]) * (k < 15 ? da0 : da1);
+    // w B dQ = bcol (w d alpha): one multiply-add per row; rows 1 and 16 of B are 0
+    const double wd0 = qd.w[i] * da0, wd1 = qd.w[i] * da1;
+    for (int k = 0; k < 30; ++k)
+      if (k != 1 && k != 16) acc[k] = fma(bc[k], k < 15 ? wd0 : wd1, acc[k]);
   }
   return st;
 }
