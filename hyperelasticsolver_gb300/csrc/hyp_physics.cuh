@@ -458,6 +458,15 @@ struct Prim {
   Pows w;
 };
 
+// 1/sqrt(x): CUDA's rsqrt on the device (1 ulp), the quotient on the host.
+HYP_HD double rsqrt_d(double x) {
+#ifdef __CUDA_ARCH__
+  return rsqrt(x);
+#else
+  return 1.0 / std::sqrt(x);
+#endif
+}
+
 // HyperelasticityMPh.jl:106-133. Returns HYP_CELL_* status.
 HYP_HD int cons_to_prim(const EosC& e, double alpha, const double* m, double rhoE, const double* rA, Prim& P) {
   double FQ[9];
@@ -465,9 +474,12 @@ HYP_HD int cons_to_prim(const EosC& e, double alpha, const double* m, double rho
   for (int c = 0; c < 9; ++c) FQ[c] = rA[c] * ia;
   double d = det3(FQ);
   int st = d > 0.0 ? HYP_CELL_OK : HYP_CELL_NEG_DET;
-  P.true_den = sqrt(d * e.inv_rho0);
+  // rho_true = sqrt(x) and 1/(alpha rho_true) from one reciprocal square root
+  // (within an ulp or two of the sqrt and the division it replaces)
+  const double x = d * e.inv_rho0, r = rsqrt_d(x);
+  P.true_den = x * r;
   P.den = alpha * P.true_den;
-  P.inv_den = 1.0 / P.den;
+  P.inv_den = r * ia;
   for (int c = 0; c < 3; ++c) P.u[c] = m[c] * P.inv_den;
   P.E = rhoE * P.inv_den;
   P.e_int = P.E - 0.5 * (P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2]);
