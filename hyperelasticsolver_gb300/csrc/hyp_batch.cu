@@ -98,7 +98,8 @@ __global__ void __launch_bounds__(BLOCK, MINB)
       }
       continue;
     }
-    const float l = mixed_tile_run<BLOCK>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
+    // faces from shared memory: the batch variants at 64 registers spill more otherwise
+    const float l = mixed_tile_run<BLOCK, false>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
     const float m = mixed_block_max<BLOCK>(l);
     if (threadIdx.x == 0) atomicMax(&slots_wr[d.problem], (unsigned long long)__float_as_uint(m));
     __syncthreads();  // the block-max scratch is reused by the next tile

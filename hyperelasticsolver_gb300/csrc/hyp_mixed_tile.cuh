@@ -102,7 +102,10 @@ __device__ __forceinline__ void mixed_tile_load(int64_t first, int64_t lo, int64
                                                 MixedCellIn& c) {
   load((int)threadIdx.x, tile_cell(first, lo, hi), c);
 }
-template <int BLOCK, class Loader>
+// kOwnRegs: a face reads its left cell (this thread's) and an update its right face
+// (this thread's) from registers instead of shared memory -- 39 fewer shared loads
+// per cell, at 11 more registers live across a barrier (the same values either way).
+template <int BLOCK, bool kOwnRegs = true, class Loader>
 __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
                                                 int64_t hi, float dtdx, int flux, int bc, DevState* S,
                                                 const Loader& load, MixedCellIn& c) {
@@ -112,11 +115,11 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
   const int j = threadIdx.x;
   const int64_t i = first - 1 + j;
   const int64_t ic = tile_cell(first, lo, hi);
+  float f11[kNFlux1];  // this cell's flux: its own face reads it from registers
   {
     PrimM P;
     int st = prim_from_islands(em, c.qh, c.ql, c.I0, P);
     StressCT<float> sc = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
-    float f11[kNFlux1];
     flux_mixed(em, c.qh, P, sc, f11);
 #pragma unroll
     for (int s = 0; s < kNFlux1; ++s) sFF[s][j] = f11[s];
@@ -125,17 +128,17 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
     if (st && i == ic && j > 0 && j < BLOCK - 1) mixed_record_err(S, st, i);
   }
   __syncthreads();
-  // face j + 1/2 between local cells j and j + 1
+  // face j + 1/2 between local cells j (this thread: registers) and j + 1 (shared memory)
   float fv[14];
   if (j < BLOCK - 1) {
-    const float lf = flux == HYP_FLUX_LXF ? 1.0f / dtdx : fmaxf(sL[j], sL[j + 1]);
+    const float lf = flux == HYP_FLUX_LXF ? 1.0f / dtdx : fmaxf(kOwnRegs ? c.li : sL[j], sL[j + 1]);
     const float hl = 0.5f * lf;
     const int64_t i1 = i + 1, ic1 = i1 < lo ? lo : (i1 >= hi ? hi - 1 : i1);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
       const int s = flux_slot1(v);
-      const float fl = s >= 0 ? sFF[s][j] : 0.0f, fr = s >= 0 ? sFF[s][j + 1] : 0.0f;
-      fv[v] = 0.5f * (fl + fr) - hl * (load.face_q(v, j + 1, ic1) - load.face_q(v, j, ic));
+      const float fl = s >= 0 ? (kOwnRegs ? f11[s] : sFF[s][j]) : 0.0f, fr = s >= 0 ? sFF[s][j + 1] : 0.0f;
+      fv[v] = 0.5f * (fl + fr) - hl * (load.face_q(v, j + 1, ic1) - (kOwnRegs ? c.qh[v] : load.face_q(v, j, ic)));
     }
   }
   __syncthreads();
@@ -155,7 +158,7 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
     } else {
 #pragma unroll
       for (int v = 0; v < 14; ++v) {
-        const float delta = -dtdx * (sFF[v][j] - sFF[v][j - 1]);
+        const float delta = -dtdx * ((kOwnRegs ? fv[v] : sFF[v][j]) - sFF[v][j - 1]);  // F_{j+1/2} - F_{j-1/2}
         ff q = ff_add_f(ff{c.qh[v], c.ql[v]}, delta);
         c.qh[v] = q.hi;
         c.ql[v] = q.lo;
