@@ -158,7 +158,9 @@ static int write_tsv(const char* path, const double* P, int64_t n, int cols) {
   return ok ? HYP_OK : HYP_ERR_INVALID;
 }
 
-// Reads the reference's TSV (header line, then n rows of `cols` numbers) into P [cols][n].
+// Reads the reference's TSV (header line, then n rows of `cols` numbers) into P [cols][n];
+// HYP_ERR_INVALID for a missing file, a row with fewer or more numbers, or a row count
+// other than n.
 static int read_tsv(const char* path, double* P, int64_t n, int cols) {
   std::FILE* f = std::fopen(path, "rb");
   if (!f) return HYP_ERR_INVALID;
@@ -187,6 +189,11 @@ static int read_tsv(const char* path, double* P, int64_t n, int cols) {
       }
       P[(int64_t)c * n + row] = v;
       p = end;
+    }
+    while (*p == ' ' || *p == '\t' || *p == '\r') ++p;
+    if (*p != '\0') {  // more columns than the context's model has
+      rc = HYP_ERR_INVALID;
+      return;
     }
     ++row;
   };

@@ -116,3 +116,33 @@ def test_twophase_snapshot_and_logged_t_end(hyp, orc, tmp_path):
     assert head.split("\t")[15] == "a2" and P0.shape == (30, 200)
     np.testing.assert_allclose(P0, orc.cons2prim(pb, Q0.T).T, rtol=RTOL_FP64, atol=1e-15)
     assert P.shape == (30, 200) and np.all(np.isfinite(P))
+
+
+def test_load_snapshot_rejects_malformed_files(hyp, tmp_path):
+    """A missing file, a short or long file, and rows with too few or too many
+    columns are refused (HYP_ERR_INVALID) and leave the context usable."""
+    eos, Q0 = riemann_Q0(hyp, 64)
+    good = str(tmp_path / "good.csv")
+    with hyp.Solver(eos, 64) as s:
+        s.upload(Q0)
+        s.save_snapshot(good)
+        head, P = read_tsv(good)
+        lines = open(good).read().splitlines()
+        bad = {
+            "missing": None,
+            "short": lines[:-1],
+            "long": lines + [lines[-1]],
+            "few columns": lines[:5] + ["\t".join(lines[5].split("\t")[:-1])] + lines[6:],
+            "many columns": lines[:5] + [lines[5] + "\t1.0"] + lines[6:],
+        }
+        for name, content in bad.items():
+            path = str(tmp_path / f"bad_{name.replace(' ', '_')}.csv")
+            if content is not None:
+                with open(path, "w") as fh:
+                    fh.write("\n".join(content) + "\n")
+            with pytest.raises(hyp._lib.HypError) as err:
+                s.load_snapshot(path)
+            assert err.value.code == hyp._lib.HYP_ERR_INVALID, name
+        s.load_snapshot(good)
+        n, _ = s.step(max_steps=3)
+        assert n == 3
