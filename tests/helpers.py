@@ -1,7 +1,7 @@
 """Shared tolerances and comparisons for the parity tests."""
 import numpy as np
 
-# FP64 GPU vs FP64 CPU oracle: the benchmark spec's tolerance. Bit equality is not
+# FP64 GPU vs FP64 CPU oracle: the required parity tolerance. Bit equality is not
 # expected (FMA contraction, closed-form derivatives vs dual numbers, cofactor
 # vs LU determinant), 1e-12 relative is.
 RTOL_FP64 = 1e-12
