@@ -4,7 +4,8 @@ and the entries of rho A with exactly one index along x), so the run of the
 mirrored state is the mirror of the run, bitwise: IEEE negation, fused
 multiply-add and round-to-nearest are sign-symmetric, each face is evaluated with
 one rounding sequence, and the max picks the same value. Checked on the 64-segment
-workload up to 2^24 cells, FP64 and mixed precision, frozen and transmissive ends."""
+workload up to 2^24 cells, FP64 and mixed precision, frozen and transmissive ends;
+the two-phase step at 2^22 cells to rounding."""
 import numpy as np
 import pytest
 
@@ -38,3 +39,41 @@ def test_mirrored_run_is_the_mirror_of_the_run(hyp, precision, bc, n):
     scale = np.maximum(np.max(np.abs(Qa), axis=1, keepdims=True), 1e-30)
     print(f"mirror {precision} {bc} {n}: max rel {np.max(d / scale):.1e}, bitwise {np.array_equal(mirror(Qa), Qb)}")
     assert np.array_equal(mirror(Qa), Qb)
+
+
+FLIP2 = [2, 7, 8, 9, 12]  # per phase: alpha rho u1; alpha rho A (1,0), (2,0), (0,1), (0,2)
+
+
+def mirror2(Q):
+    M = Q[:, ::-1].copy()
+    M[FLIP2 + [k + 15 for k in FLIP2]] *= -1.0
+    return np.ascontiguousarray(M)
+
+
+# observed: FP64 3.4e-15; mixed 1.7e-7 (HLL) and 6.8e-7 (LxF) of each variable's scale
+@pytest.mark.parametrize("precision,flux,tol", [("fp64", "hll", 1e-13), ("mixed", "hll", 5e-6),
+                                                ("mixed", "lxf", 5e-6)])
+def test_twophase_mirrored_run_at_full_size(hyp, precision, flux, tol):
+    """The two-phase step at the 2^22-cell interface workload also commutes with
+    x -> -x, to rounding rather than bitwise: the HLL state Q_hll = (s_R Q_R - s_L Q_L
+    - ...)/(s_R - s_L) and the path integrals evaluate their mirrored operands in a
+    different order, so multiply-add contraction can differ in the last bit."""
+    from hyperelasticsolver_gb300 import HyperelasticityMPh as HM
+    from hyperelasticsolver_gb300._cases import mph_interface_prims
+    eos = (hyp.Barton2009(), hyp.Barton2009(_b0=2.1 * np.sqrt(0.1)))
+    n = 1 << 22
+    Q0 = np.ascontiguousarray(HM.prim2cons_mph(eos, mph_interface_prims(eos[0], n)).T)
+    out = []
+    for q in (Q0, mirror2(Q0)):
+        with hyp.Solver(eos, n, model="multi", flux=flux, precision=precision) as s:
+            s.upload(q)
+            k, t = s.step(max_steps=40)
+            assert k == 40
+            out.append((s.download(), t))
+    (Qa, ta), (Qb, tb) = out
+    # mixed: each step's dt comes from an FP32 max wave speed, itself mirrored only to rounding
+    assert abs(ta - tb) <= (1e-14 if precision == "fp64" else 1e-6) * ta
+    scale = np.maximum(np.max(np.abs(Qa), axis=1, keepdims=True), 1e-30)
+    err = np.max(np.abs(mirror2(Qa) - Qb) / scale)
+    print(f"two-phase mirror {precision} {flux} 2^22: max rel {err:.1e}")
+    assert err <= tol
