@@ -117,6 +117,7 @@ __device__ __forceinline__ float phase_cmax_m2(const EosT<float>& e, const PrimM
 __device__ __forceinline__ int cell2_mixed(const Eos2M& E, const float* qh, const float* ql, float* F, float& smin,
                                            float& smax) {
   int st = 0;
+#pragma unroll  // static indices keep the 90-float arrays in registers, not local memory
   for (int p = 0; p < 2; ++p) {
     const float* q = qh + 15 * p;
     PrimM2 P;
