@@ -415,6 +415,11 @@ extern "C" int hyp_run_logged(hyp_ctx* c, double t_end, int max_steps, int log_f
     }
     if (sd < chunk) break;  // t reached t_end
   }
+  if (rc == HYP_OK && !(t < t_end)) {  // the run reached T: result.csv (main.jl:242-244)
+    std::string d(dir);
+    if (!d.empty() && d.back() != '/') d += '/';
+    if ((rc = enqueue_snapshot(c, slot)) == HYP_OK) start_writer(c, slot, d + "result.csv");
+  }
   const int wrc = finish_writer(c);
   if (rc == HYP_OK) rc = wrc;
   if (steps_done) *steps_done = (int)done;

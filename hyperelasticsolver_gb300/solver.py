@@ -265,10 +265,19 @@ class Batch:
         return Q[:, self.offsets[p]:self.offsets[p + 1]]
 
 
-def last_snapshot(directory, dt):
-    """The restart point of main.jl:181-187: the last sol_*.csv in `directory`, its step
-    number and the time step_number * dt. Returns (path, step, t) or None if there is none."""
+def last_snapshot(directory, dt, clean=False):
+    """The restart point of main.jl:173-187: the last sol_*.csv in `directory`, its step
+    number and the time step_number * dt; (path, step, t). None where the reference
+    starts afresh: an empty directory, or one holding result.csv (a finished run),
+    whose sol_*.csv and result.csv files are then removed if clean is true (the
+    reference removes every file of its data directory)."""
     files = sorted(glob.glob(os.path.join(directory, "sol_*.csv")))
+    result = os.path.join(directory, "result.csv")
+    if os.path.exists(result):
+        if clean:
+            for f in files + [result]:
+                os.remove(f)
+        return None
     if not files:
         return None
     step = int(os.path.basename(files[-1]).split(".")[0].split("_")[1])

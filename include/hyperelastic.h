@@ -205,7 +205,8 @@ int hyp_load_snapshot(hyp_ctx* ctx, const char* path, double t0);
 /* The main.jl time loop with logging: saves dir/sol_%06i.csv for the current
    state (step number first_step) and after every step whose number is a multiple
    of log_freq, until t >= t_end or max_steps steps (either may be unbounded,
-   not both). Copies and file writing overlap the following steps. */
+   not both); a run that reaches t_end also saves dir/result.csv (main.jl:242-244).
+   Copies and file writing overlap the following steps. */
 int hyp_run_logged(hyp_ctx* ctx, double t_end, int max_steps, int log_freq, const char* dir, int64_t first_step,
                    int* steps_done, double* t_out);
 

@@ -76,7 +76,7 @@ def test_run_logged_files_and_restart(hyp, tmp_path):
         n, t = s.run_logged(d, max_steps=250, log_freq=100)
         assert n == 250
         Qlog = s.download()
-    assert sorted(os.listdir(d)) == ["sol_000000.csv", "sol_000100.csv", "sol_000200.csv"]
+    assert sorted(os.listdir(d)) == ["sol_000000.csv", "sol_000100.csv", "sol_000200.csv"]  # T not reached
     with hyp.Solver(eos, 400) as s:
         s.upload(Q0)
         s.step(max_steps=250)
@@ -110,12 +110,20 @@ def test_twophase_snapshot_and_logged_t_end(hyp, orc, tmp_path):
         n, t = s.run_logged(d, t_end=t_end, log_freq=10)
         assert t >= t_end
         P = s.snapshot()
-    files = sorted(os.listdir(d))
+    files = sorted(f for f in os.listdir(d) if f.startswith("sol_"))
     assert files[0] == "sol_000000.csv" and all(int(f[4:10]) % 10 == 0 for f in files)
     head, P0 = read_tsv(os.path.join(d, "sol_000000.csv"))
     assert head.split("\t")[15] == "a2" and P0.shape == (30, 200)
     np.testing.assert_allclose(P0, orc.cons2prim(pb, Q0.T).T, rtol=RTOL_FP64, atol=1e-15)
     assert P.shape == (30, 200) and np.all(np.isfinite(P))
+    # the run reached T: result.csv holds the final state (main.jl:242-244), and the
+    # reference's restart rule then starts afresh (main.jl:173-176)
+    _, Pr = read_tsv(os.path.join(d, "result.csv"))
+    assert np.array_equal(Pr, P)
+    from hyperelasticsolver_gb300.solver import last_snapshot
+    assert last_snapshot(d, dt=1e-6) is None and os.path.exists(os.path.join(d, "result.csv"))
+    assert last_snapshot(d, dt=1e-6, clean=True) is None
+    assert not any(f.startswith("sol_") or f == "result.csv" for f in os.listdir(d))
 
 
 def test_load_snapshot_rejects_malformed_files(hyp, tmp_path):
