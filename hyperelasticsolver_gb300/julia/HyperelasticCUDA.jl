@@ -101,6 +101,41 @@ module HyperelasticityMPh
       out
     end
   end
+  """noncons_flux(eos, Q) (HyperelasticityMPh.jl:178-250): B per cell as an (n, 30, 30) array,
+  whose only non-zero columns are 1 and 16 (the device computes just those two)."""
+  function noncons_flux(eos, Q::Matrix{Float64})
+    n = size(Q, 1)
+    bcol = Matrix{Float64}(undef, n, 30)
+    check(ccall((:hyp_eval_noncons, libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64),
+                Ref(config(eos, HYP_MODEL_MULTI)), Q, bcol, n), "noncons_flux")
+    B = zeros(n, 30, 30)
+    B[:, 1:15, 1] .= bcol[:, 1:15]
+    B[:, 16:30, 16] .= bcol[:, 16:30]
+    B
+  end
+end
+
+module Hyperelasticity
+  import ..libhyp, ..check, ..config, ..ConfigC, ..Barton2009C, ..HYP_MODEL_SINGLE
+  # single-phase cells (n, 14): the per-phase functions of HyperelasticityMPh.jl at alpha = 1
+  for (jl, c, k) in ((:cons2prim, :hyp_eval_cons2prim, 14), (:prim2cons, :hyp_eval_prim2cons, 14),
+                     (:flux, :hyp_eval_flux, 14), (:get_eigvals, :hyp_eval_eigvals, 6))
+    @eval function $jl(eos::Barton2009C, Q::Matrix{Float64})
+      out = Matrix{Float64}(undef, size(Q, 1), $k)
+      cfg = Ref(config(eos, HYP_MODEL_SINGLE))
+      check(ccall(($(QuoteNode(c)), libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64),
+                  cfg, Q, out, size(Q, 1)), $(string(jl)))
+      out
+    end
+  end
+  "prim2cons_vjp(eos, P, Qbar) -> (Pbar, (dL/db0sq, dL/dk0)): the pullback of prim2cons over n cells"
+  function prim2cons_vjp(eos::Barton2009C, P::Matrix{Float64}, Qbar::Matrix{Float64})
+    Pbar, eb = similar(P), zeros(2)
+    check(ccall((:hyp_eval_prim2cons_vjp, libhyp), Cint,
+                (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                Ref(config(eos, HYP_MODEL_SINGLE)), P, Qbar, Pbar, eb, size(P, 1)), "prim2cons_vjp")
+    Pbar, (eb[1], eb[2])
+  end
 end
 
 module NumFluxes
@@ -158,6 +193,83 @@ function step!(s::Solver; max_steps::Integer=0, T::Float64=Inf)
   (n[], t[])
 end
 
+# ---- queries, kernel choices and timing of a context ----
+"error_cell(s): the first cell that raised NEG_DET / NONFINITE in the last call (-1: none)"
+error_cell(s::Solver) = ccall((:hyp_error_cell, libhyp), Int64, (Ptr{Cvoid},), s.h)
+"max_wavespeed(s): max over cells of |u1| + c_max of the current state (main.jl:204-211)"
+function max_wavespeed(s::Solver)
+  v = Ref{Float64}(0.0)
+  check(ccall((:hyp_max_wavespeed, libhyp), Cint, (Ptr{Cvoid}, Ref{Float64}), s.h, v), "hyp_max_wavespeed", s.h)
+  v[]
+end
+"get_time(s) -> (t, steps taken since the upload)"
+function get_time(s::Solver)
+  t, n = Ref{Float64}(0.0), Ref{Int64}(0)
+  check(ccall((:hyp_get_time, libhyp), Cint, (Ptr{Cvoid}, Ref{Float64}, Ref{Int64}), s.h, t, n), "hyp_get_time", s.h)
+  (t[], n[])
+end
+set_profiling!(s::Solver, on::Bool) =
+  check(ccall((:hyp_set_profiling, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, on), "hyp_set_profiling", s.h)
+"last_timing(s): device ms of the last step! call, per-kernel sums when profiling is on"
+function last_timing(s::Solver)
+  tot, mc, mu = Ref{Float64}(0.0), Ref{Float64}(0.0), Ref{Float64}(0.0)
+  nc, nu = Ref{Cint}(0), Ref{Cint}(0)
+  check(ccall((:hyp_last_timing, libhyp), Cint,
+              (Ptr{Cvoid}, Ref{Float64}, Ref{Float64}, Ref{Cint}, Ref{Float64}, Ref{Cint}), s.h, tot, mc, nc, mu, nu),
+        "hyp_last_timing", s.h)
+  (ms_total=tot[], ms_cell=mc[], n_cell=nc[], ms_update=mu[], n_update=nu[])
+end
+"set_mixed_kernel!(s, tma): single-phase mixed precision on the TMA-prefetched persistent kernel (true) or one block per tile"
+set_mixed_kernel!(s::Solver, tma::Bool) =
+  check(ccall((:hyp_set_mixed_kernel, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, tma), "hyp_set_mixed_kernel", s.h)
+"set_wait_limit!(s, tries): poll budget of the persistent kernel's device waits (0: every wait times out)"
+set_wait_limit!(s::Solver, tries::Integer) =
+  check(ccall((:hyp_set_wait_limit, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, tries), "hyp_set_wait_limit", s.h)
+"snapshot(s): cons2prim of the current state, one row per cell ([alpha, rho, u, S, A] per phase)"
+function snapshot(s::Solver)
+  P = Matrix{Float64}(undef, s.n, s.nvar == 14 ? 15 : 30)
+  check(ccall((:hyp_snapshot, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}), s.h, P), "hyp_snapshot", s.h)
+  P
+end
+
+# ---- initial conditions on the device (main.jl:99-123, HyperelasticityMPh.jl:275-426) ----
+"initial_states(eos::Tuple, testcase) -> (Ql, Qr): the conservative 30-vectors of a reference test case"
+function initial_states(eos::Tuple, testcase::Integer)
+  Ql, Qr = zeros(30), zeros(30)
+  check(ccall((:hyp_initial_states, libhyp), Cint, (Ref{ConfigC}, Cint, Ptr{Float64}, Ptr{Float64}),
+              Ref(config(eos, HYP_MODEL_MULTI)), testcase, Ql, Qr), "hyp_initial_states")
+  Ql, Qr
+end
+"initial_condition!(s, Ql, Qr): the two-state fill of main.jl:99-106, made the current state at t = 0"
+initial_condition!(s::Solver, Ql::Vector{Float64}, Qr::Vector{Float64}) =
+  check(ccall((:hyp_init_riemann, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}), s.h, Ql, Qr),
+        "hyp_init_riemann", s.h)
+"initial_condition_tanh!(s, Ql, Qr, eps): the tanh volume-fraction profile of main.jl:110-123"
+initial_condition_tanh!(s::Solver, Ql::Vector{Float64}, Qr::Vector{Float64}, eps::Float64) =
+  check(ccall((:hyp_init_tanh, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64), s.h, Ql, Qr, eps),
+        "hyp_init_tanh", s.h)
+
+# ---- caller-owned device memory and page-locked host memory ----
+"""step_noalloc!(cfg, d_in, d_out, n_steps, t0; stream): single-phase FP64 steps on device
+buffers the caller owns (e.g. pointer(::CuArray)), allocating nothing; returns t"""
+function step_noalloc!(cfg::ConfigC, d_in::Ptr{Float64}, d_out::Ptr{Float64}, n_steps::Integer, t0::Float64;
+                       stream::Ptr{Cvoid}=C_NULL)
+  t, cell = Ref{Float64}(0.0), Ref{Int64}(-1)
+  rc = ccall((:hyp_step_noalloc_f64, libhyp), Cint,
+             (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64, Cint, Float64, Ptr{Cvoid}, Ref{Float64}, Ref{Int64}),
+             Ref(cfg), d_in, d_out, cfg.n_cells, n_steps, t0, stream, t, cell)
+  rc == 0 || throw(HypError(rc, "hyp_step_noalloc_f64 (cell $(cell[]))"))
+  t[]
+end
+"pinned_matrix(n, k): a Matrix{Float64} in page-locked host memory (hyp_host_alloc) for fast copies"
+function pinned_matrix(n::Integer, k::Integer)
+  p = Ref{Ptr{Cvoid}}(C_NULL)
+  check(ccall((:hyp_host_alloc, libhyp), Cint, (Int64, Ref{Ptr{Cvoid}}), Int64(n) * k * 8, p), "hyp_host_alloc")
+  A = unsafe_wrap(Matrix{Float64}, Ptr{Float64}(p[]), (n, k); own=false)
+  finalizer(_ -> ccall((:hyp_host_free, libhyp), Cint, (Ptr{Cvoid},), p[]), A)
+  A
+end
+
 # ---- snapshots and restart (main.jl:62-95, 108, 174-198, 233-237) ----
 "save_data(s, fname): the reference's save_data file of the current state (device cons2prim)"
 save_data(s::Solver, fname::AbstractString) =
@@ -181,12 +293,13 @@ end
 mutable struct Batch
   h::Ptr{Cvoid}
   total::Int64
+  np::Int
   function Batch(cfg::ConfigC, offsets::Vector{Int64})
     r = Ref{Ptr{Cvoid}}(C_NULL)
     rc = ccall((:hyp_batch_create, libhyp), Cint, (Ref{ConfigC}, Ptr{Int64}, Cint, Ref{Ptr{Cvoid}}),
                Ref(cfg), offsets, length(offsets) - 1, r)
     rc == 0 || throw(HypError(rc, "hyp_batch_create"))
-    b = new(r[], offsets[end])
+    b = new(r[], offsets[end], length(offsets) - 1)
     finalizer(x -> ccall((:hyp_batch_destroy, libhyp), Cint, (Ptr{Cvoid},), x.h), b)
   end
 end
@@ -208,7 +321,38 @@ function autotune!(b::Batch; trial_steps::Integer=10)
   (chosen[], ms)
 end
 
+"status(b) -> (t, steps) per problem"
+function status(b::Batch)
+  t, steps = zeros(b.np), zeros(Int64, b.np)
+  bcheck(ccall((:hyp_batch_status, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Int64}), b.h, t, steps), b,
+         "hyp_batch_status")
+  t, steps
+end
+"last_ms(b): device ms of the last step! call"
+function last_ms(b::Batch)
+  ms = Ref{Float64}(0.0)
+  bcheck(ccall((:hyp_batch_last_ms, libhyp), Cint, (Ptr{Cvoid}, Ref{Float64}), b.h, ms), b, "hyp_batch_last_ms")
+  ms[]
+end
+"set_variant!(b, v): the tile kernel variant (0-5, as autotune! numbers them)"
+set_variant!(b::Batch, v::Integer) =
+  bcheck(ccall((:hyp_batch_set_variant, libhyp), Cint, (Ptr{Cvoid}, Cint), b.h, v), b, "hyp_batch_set_variant")
+
 # ---- the adjoint of a single-phase FP64 Rusanov run ----
+"density_misfit(s, rho_target) -> (L, dL/dQ): L = |rho - target|^2 / 2 of the current state"
+function density_misfit(s::Solver, target::Vector{Float64})
+  L, dQ = Ref{Float64}(0.0), Matrix{Float64}(undef, s.n, s.nvar)
+  check(ccall((:hyp_density_misfit, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ref{Float64}, Ptr{Float64}), s.h,
+              target, L, dQ), "hyp_density_misfit", s.h)
+  L[], dQ
+end
+"adjoint_timing(s): device ms of the last record!, and of the recompute and adjoint steps of the last adjoint"
+function adjoint_timing(s::Solver)
+  r, c, a = Ref{Float64}(0.0), Ref{Float64}(0.0), Ref{Float64}(0.0)
+  check(ccall((:hyp_adjoint_timing, libhyp), Cint, (Ptr{Cvoid}, Ref{Float64}, Ref{Float64}, Ref{Float64}), s.h, r, c,
+              a), "hyp_adjoint_timing", s.h)
+  (ms_record=r[], ms_recompute=c[], ms_adjoint=a[])
+end
 "record!(s, n_steps; K): n_steps steps that keep a checkpoint every K steps (the rrule's forward pass)"
 function record!(s::Solver, n_steps::Integer; K::Integer=50)
   t = Ref{Float64}(0.0)

@@ -35,6 +35,15 @@ def test_python_binding_covers_header(hyp):
     assert declared_functions() <= set(hyp._lib.exported_symbols())
 
 
+def test_julia_binding_covers_header():
+    """Every entry point has a ccall in the Julia binding (which cannot run here)."""
+    src = "".join(open(f).read() for f in glob.glob(os.path.join(ROOT, "hyperelasticsolver_gb300", "julia", "*.jl")))
+    called = set(re.findall(r"ccall\(\(\$?\(?QuoteNode\(c\)\)?|ccall\(\(:(hyp_[A-Za-z0-9_]+)", src)) - {""}
+    looped = set(re.findall(r"\(:[a-z_0-9]+, :(hyp_[A-Za-z0-9_]+)", src))  # symbols bound in @eval loops
+    missing = declared_functions() - called - looped
+    assert not missing, f"declared but not bound in Julia: {sorted(missing)}"
+
+
 def test_library_loads_without_gpu(hyp):
     L = hyp._lib.load()
     assert L.hyp_last_error(None) == b"no context"
