@@ -165,9 +165,14 @@ template <class R> HYP_HD R det3(const R* m) {  // column-major, cofactor expans
          m[6] * (m[1] * m[5] - m[4] * m[2]);
 }
 
-template <class R> HYP_HD PowsT<R> powers(const EosT<R>& e, const KinT<R>& k) {
+// kDef: 1 = the reference's default exponents (alpha 1, beta 3, gamma 2) known at
+// compile time, so the general powers' code drops out of a kernel; -1 = decided by
+// e.default_exp at run time.
+template <int kDef, class E> HYP_HD bool default_exponents(const E& e) { return kDef == 1 || (kDef < 0 && e.default_exp); }
+
+template <class R, int kDef = -1> HYP_HD PowsT<R> powers(const EosT<R>& e, const KinT<R>& k) {
   PowsT<R> w;
-  if (e.default_exp) {  // alpha = 1, beta = 3, gamma = 2: p^(n/2) = s^n
+  if (default_exponents<kDef>(e)) {  // alpha = 1, beta = 3, gamma = 2: p^(n/2) = s^n
     R s = k.s, is = k.inv_s, ip = is * is;
     w.Pa = s;         w.Pa1 = is;  w.Pa2 = is * ip;
     w.Pb = s * k.p;   w.Pb1 = s;   w.Pb2 = is;

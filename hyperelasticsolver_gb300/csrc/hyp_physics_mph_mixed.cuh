@@ -39,6 +39,7 @@ struct PrimM2 {
 
 // q: [alpha, alpha rho (unused), alpha rho u(3), alpha rho E, alpha rho A(9)]; ql: the lo
 // parts (or nullptr). Returns HYP_CELL_* status.
+template <int kDef = -1>
 __device__ __forceinline__ int cons_to_prim_m2(const EosMixed& em, const float* q, const float* ql, PrimM2& P) {
   const EosT<float>& e = em.f;
   const float* m = q + 6;
@@ -78,8 +79,8 @@ __device__ __forceinline__ int cons_to_prim_m2(const EosMixed& em, const float* 
   for (int c = 0; c < 9; ++c) P.A[c] = m[c] * idn;
   const float sf = 1.0f + P.sm1;
   P.k = kinematics_s<float>(P.A, sf, __frcp_rn(sf));
-  P.w = powers<float>(e, P.k);
-  P.w.Pam1 = e.default_exp ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
+  P.w = powers<float, kDef>(e, P.k);
+  P.w.Pam1 = default_exponents<kDef>(e) ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
   P.xm1 = entropy_xm1<float>(e, P.e_int, P.k, P.w);
   P.rho_s = e.rho0 * sf;
   if (!(P.e_int == P.e_int) || !(P.xm1 == P.xm1) || !isfinite(P.k.p)) st |= HYP_CELL_NONFINITE;
@@ -114,6 +115,7 @@ __device__ __forceinline__ float phase_cmax_m2(const EosT<float>& e, const PrimM
 }
 
 // Both phases' flux (30) and wave-speed bounds of a cell from its compensated state.
+template <int kDef = -1>
 __device__ __forceinline__ int cell2_mixed(const Eos2M& E, const float* qh, const float* ql, float* F, float& smin,
                                            float& smax) {
   int st = 0;
@@ -121,7 +123,7 @@ __device__ __forceinline__ int cell2_mixed(const Eos2M& E, const float* qh, cons
   for (int p = 0; p < 2; ++p) {
     const float* q = qh + 15 * p;
     PrimM2 P;
-    st |= cons_to_prim_m2(E.m[p], q, ql + 15 * p, P);
+    st |= cons_to_prim_m2<kDef>(E.m[p], q, ql + 15 * p, P);
     const StressCT<float> c = stress_coeffs<float>(E.m[p].f, P.k, P.w, P.xm1);
     F[15 * p] = 0.0f;
     phase_flux_m2(E.m[p].f, q[0], P, c, F + 15 * p + 1);
@@ -136,6 +138,7 @@ __device__ __forceinline__ int cell2_mixed(const Eos2M& E, const float* qh, cons
 // cons2prim of one phase in plain FP32, for the states a face evaluates between
 // its two cells (midpoint, path nodes, Q_hll): these are FP32 interpolants, whose
 // own rounding the float-float islands could not undo.
+template <int kDef = -1>
 __device__ __forceinline__ int cons_to_prim_f2(const EosMixed& em, const float* q, PrimM2& P) {
   const EosT<float>& e = em.f;
   const float* m = q + 6;
@@ -153,19 +156,20 @@ __device__ __forceinline__ int cons_to_prim_f2(const EosMixed& em, const float* 
   const float sf = rho * e.inv_rho0;
   P.sm1 = sf - 1.0f;
   P.k = kinematics_s<float>(P.A, sf, __frcp_rn(sf));
-  P.w = powers<float>(e, P.k);
-  P.w.Pam1 = e.default_exp ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
+  P.w = powers<float, kDef>(e, P.k);
+  P.w.Pam1 = default_exponents<kDef>(e) ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
   P.xm1 = entropy_xm1<float>(e, P.e_int, P.k, P.w);
   P.rho_s = e.rho0 * sf;
   if (!(P.e_int == P.e_int) || !(P.xm1 == P.xm1) || !isfinite(P.k.p)) st |= HYP_CELL_NONFINITE;
   return st;
 }
 
+template <int kDef = -1>
 __device__ __forceinline__ int speeds2_m(const Eos2M& E, const float* Q, float& smin, float& smax) {
   int st = 0;
   for (int p = 0; p < 2; ++p) {
     PrimM2 P;
-    st |= cons_to_prim_f2(E.m[p], Q + 15 * p, P);
+    st |= cons_to_prim_f2<kDef>(E.m[p], Q + 15 * p, P);
     const StressCT<float> c = stress_coeffs<float>(E.m[p].f, P.k, P.w, P.xm1);
     const float cm = phase_cmax_m2(E.m[p].f, P, c);
     const float lo = P.u[0] - cm, hi = P.u[0] + cm;
@@ -180,9 +184,10 @@ struct PhaseBM {
   float true_den, u[3], A[9], K0[3], T;
 };
 
+template <int kDef = -1>
 __device__ __forceinline__ int phase_b_m(const EosMixed& em, const float* q, PhaseBM& b) {
   PrimM2 P;
-  const int st = cons_to_prim_f2(em, q, P);
+  const int st = cons_to_prim_f2<kDef>(em, q, P);
   const StressCT<float> c = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
   stress_row0<float>(P.rho_s, P.k, c, b.K0);
   b.T = em.f.t0 * P.w.Pg * (P.xm1 + 1.0f);
@@ -193,9 +198,10 @@ __device__ __forceinline__ int phase_b_m(const EosMixed& em, const float* q, Pha
 }
 
 // bcol of B(Q) (noncons_bcol in FP32).
+template <int kDef = -1>
 __device__ __forceinline__ int noncons_bcol_m(const Eos2M& E, const float* Q, float* bcol) {
   PhaseBM b[2];
-  const int st = phase_b_m(E.m[0], Q, b[0]) | phase_b_m(E.m[1], Q + 15, b[1]);
+  const int st = phase_b_m<kDef>(E.m[0], Q, b[0]) | phase_b_m<kDef>(E.m[1], Q + 15, b[1]);
   float uI[3], sI[3];
   for (int a = 0; a < 3; ++a) uI[a] = 0.5f * b[0].u[a] + 0.5f * b[1].u[a];
   const float iden = __frcp_rn(0.5f * b[0].T + 0.5f * b[1].T);
@@ -218,6 +224,7 @@ __device__ __forceinline__ int noncons_bcol_m(const Eos2M& E, const float* Q, fl
   return st;
 }
 
+template <int kDef = -1>
 __device__ __forceinline__ int path_integral_add_m(const Eos2M& E, const Quad6F& qd, const float* Qa, const float* Qb,
                                                    float* acc) {
   const float da0 = Qb[0] - Qa[0], da1 = Qb[15] - Qa[15];
@@ -226,7 +233,7 @@ __device__ __forceinline__ int path_integral_add_m(const Eos2M& E, const Quad6F&
   for (int i = 0; i < 6; ++i) {
     const float s = qd.x[i];
     for (int k = 0; k < 30; ++k) u[k] = fmaf(s, Qb[k] - Qa[k], Qa[k]);  // Qa + s (Qb - Qa)
-    st |= noncons_bcol_m(E, u, bc);
+    st |= noncons_bcol_m<kDef>(E, u, bc);
     const float wd0 = qd.w[i] * da0, wd1 = qd.w[i] * da1;
     for (int k = 0; k < 30; ++k)
       if (k != 1 && k != 16) acc[k] = fmaf(bc[k], k < 15 ? wd0 : wd1, acc[k]);  // rows 1 and 16 of B are 0
@@ -235,12 +242,13 @@ __device__ __forceinline__ int path_integral_add_m(const Eos2M& E, const Quad6F&
 }
 
 // Path-conservative HLL fluctuations of one face (hll_face2 in FP32).
+template <int kDef = -1>
 __device__ __forceinline__ int hll_face2_m(const Eos2M& E, const Quad6F& qd, const float* QL, const float* QR,
                                            const float* dF, float sminL, float smaxR, float* dm, float* dp) {
   float Qm[30];
   for (int k = 0; k < 30; ++k) Qm[k] = 0.5f * (QL[k] + QR[k]);
   float mmin = 0.0f, mmax = 0.0f;
-  int st = speeds2_m(E, Qm, mmin, mmax);
+  int st = speeds2_m<kDef>(E, Qm, mmin, mmax);
   float sl = 0.0f;
   if (mmin < sl) sl = mmin;
   if (sminL < sl) sl = sminL;
@@ -250,14 +258,14 @@ __device__ __forceinline__ int hll_face2_m(const Eos2M& E, const Quad6F& qd, con
   const float idsr = 1.0f / (sr - sl);
   float acc[30], Qh[30];
   for (int k = 0; k < 30; ++k) acc[k] = 0.0f;
-  st |= path_integral_add_m(E, qd, QL, QR, acc);
+  st |= path_integral_add_m<kDef>(E, qd, QL, QR, acc);
   for (int k = 0; k < 30; ++k) {
     Qh[k] = ((QR[k] * sr - QL[k] * sl) - (acc[k] + dF[k])) * idsr;
     acc[k] = 0.0f;
   }
   // B_int(Q_l, Q_hll) + B_int(Q_hll, Q_r) in one accumulator
-  st |= path_integral_add_m(E, qd, QL, Qh, acc);
-  st |= path_integral_add_m(E, qd, Qh, QR, acc);
+  st |= path_integral_add_m<kDef>(E, qd, QL, Qh, acc);
+  st |= path_integral_add_m<kDef>(E, qd, Qh, QR, acc);
   const float cm = (-sl) * idsr, cp = sr * idsr, cq = (sl * sr) * idsr;
   for (int k = 0; k < 30; ++k) {
     const float inner = dF[k] + acc[k];
@@ -269,6 +277,7 @@ __device__ __forceinline__ int hll_face2_m(const Eos2M& E, const Quad6F& qd, con
 }
 
 // Path-conservative LxF face (lxf_face2 in FP32).
+template <int kDef = -1>
 __device__ __forceinline__ int lxf_face2_m(const Eos2M& E, const Quad6F& lobatto, const float* QL, const float* QR,
                                            const float* fl, const float* fr, float lambda, float* F, float* dm,
                                            float* dp) {
@@ -276,7 +285,7 @@ __device__ __forceinline__ int lxf_face2_m(const Eos2M& E, const Quad6F& lobatto
   for (int k = 0; k < 30; ++k) F[k] = 0.5f * (fl[k] + fr[k]) - hl * (QR[k] - QL[k]);
   float acc[30];
   for (int k = 0; k < 30; ++k) acc[k] = 0.0f;
-  const int st = path_integral_add_m(E, lobatto, QL, QR, acc);
+  const int st = path_integral_add_m<kDef>(E, lobatto, QL, QR, acc);
   for (int k = 0; k < 30; ++k) dm[k] = dp[k] = 0.5f * acc[k];
   return st;
 }

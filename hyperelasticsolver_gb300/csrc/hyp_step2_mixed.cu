@@ -23,6 +23,7 @@ __device__ __forceinline__ void record_err2m(DevState* S, int code, long long ce
 
 // at most 85 registers: 3 blocks of 256 per SM (0.02-0.03 ms per step better at 2^22
 // cells than 2 blocks at its natural 99)
+template <int kDef>
 __global__ void __launch_bounds__(kBlock, 3) cell2_mixed_kernel(const float* __restrict__ Qh,
                                                              const float* __restrict__ Ql, int64_t pitch, int64_t n,
                                                              Eos2M E, float* __restrict__ F, int64_t fpitch,
@@ -39,7 +40,7 @@ __global__ void __launch_bounds__(kBlock, 3) cell2_mixed_kernel(const float* __r
       ql[v] = Ql[v * pitch + i];
     }
     float lo = 0.0f, hi = 0.0f;
-    int st = cell2_mixed(E, qh, ql, f, lo, hi);
+    int st = cell2_mixed<kDef>(E, qh, ql, f, lo, hi);
     for (int v = 0; v < 30; ++v) F[v * fpitch + i] = f[v];
     smin[i] = lo;
     smax[i] = hi;
@@ -63,6 +64,7 @@ __device__ __forceinline__ void load_face_states(const float* Qh, int64_t pitch,
   }
 }
 
+template <int kDef>
 __global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
     const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, Quad6F qd, const float* __restrict__ F,
     int64_t fpitch, const float* __restrict__ smin, const float* __restrict__ smax, float* __restrict__ DM,
@@ -79,7 +81,7 @@ __global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
     float QL[30], QR[30], fl[30], fr[30];
     load_face_states(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
     for (int v = 0; v < 30; ++v) fr[v] -= fl[v];  // f(Q_r) - f(Q_l)
-    const int st = hll_face2_m(E, qd, QL, QR, fr, smin[L], smax[R], dm, dp);
+    const int st = hll_face2_m<kDef>(E, qd, QL, QR, fr, smin[L], smax[R], dm, dp);
     if (st) record_err2m(S, st, R);
   }
   for (int v = 0; v < 30; ++v) {
@@ -91,6 +93,7 @@ __global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
 // 128 registers (8 blocks of 64 per SM) with a small spill: 2.00 ms per step at 2^22
 // cells against 2.36 ms at its natural 197 registers. The HLL face kernel, with three
 // path integrals live, spills heavily under the same cap and stays uncapped.
+template <int kDef>
 __global__ void __launch_bounds__(kFaceBlockM, 8) face2_lxf_mixed_kernel(
     const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, Quad6F lobatto, const float* __restrict__ F,
     int64_t fpitch, const unsigned long long* lam_now, double cfl, double dx, float* __restrict__ FF,
@@ -105,7 +108,7 @@ __global__ void __launch_bounds__(kFaceBlockM, 8) face2_lxf_mixed_kernel(
   const float lam = (float)(dx / dt);  // lambda = dx/dt (main.jl:223)
   float QL[30], QR[30], fl[30], fr[30], ff_[30], dm[30], dp[30];
   load_face_states(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
-  const int st = lxf_face2_m(E, lobatto, QL, QR, fl, fr, lam, ff_, dm, dp);
+  const int st = lxf_face2_m<kDef>(E, lobatto, QL, QR, fl, fr, lam, ff_, dm, dp);
   if (st) record_err2m(S, st, R);
   for (int v = 0; v < 30; ++v) {
     FF[v * nf + f] = ff_[v];
@@ -166,21 +169,29 @@ static Eos2M eos2m(const hyp_ctx* c) {
   return E;
 }
 
+// Both phases with the reference's default exponents: the kernels compiled with the
+// integer powers only (kDef = 1), whose smaller code the face kernel's instruction
+// fetch feels (3.26 -> 3.05 ms per two-phase HLL step at 2^22 cells); else the
+// general form (kDef = -1).
+static bool default_exps(const hyp_ctx* c) { return c->eos[0].default_exp && c->eos[1].default_exp; }
+
 cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end) {
-  cell2_mixed_kernel<<<grid_m(c->n, kBlock), kBlock, 0, c->stream>>>(c->Qh[p], c->Ql[p], c->mpitch, c->n, eos2m(c),
-                                                                      c->F32, c->n, c->smin32, c->smax32, lam_slot,
-                                                                      t_now, t_end, c->st);
+  auto kern = default_exps(c) ? cell2_mixed_kernel<1> : cell2_mixed_kernel<-1>;
+  kern<<<grid_m(c->n, kBlock), kBlock, 0, c->stream>>>(c->Qh[p], c->Ql[p], c->mpitch, c->n, eos2m(c), c->F32, c->n,
+                                                        c->smin32, c->smax32, lam_slot, t_now, t_end, c->st);
   return cudaGetLastError();
 }
 
 cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
   if (c->cfg.flux == HYP_FLUX_LXF) {
     const double dx = c->cfg.x_length / (double)c->n;
-    face2_lxf_mixed_kernel<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
+    auto kern = default_exps(c) ? face2_lxf_mixed_kernel<1> : face2_lxf_mixed_kernel<-1>;
+    kern<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
         c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->lobatto), c->F32, c->n, &c->st->lam_bits[p], c->cfg.cfl, dx,
         c->FF32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
   } else {
-    face2_hll_mixed_kernel<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
+    auto kern = default_exps(c) ? face2_hll_mixed_kernel<1> : face2_hll_mixed_kernel<-1>;
+    kern<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
         c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n, c->smin32, c->smax32, c->DM32, c->DP32,
         &c->st->t[p], t_end, c->st);
   }
