@@ -92,7 +92,9 @@ __global__ void __launch_bounds__(kFaceBlockM) face2_hll_mixed_kernel(
 
 // 128 registers (8 blocks of 64 per SM) with a small spill: 2.00 ms per step at 2^22
 // cells against 2.36 ms at its natural 197 registers. The HLL face kernel, with three
-// path integrals live, spills heavily under the same cap and stays uncapped.
+// path integrals live, spills heavily under the same cap and stays uncapped (200
+// registers for 10 warps per SM: 3.23 against 3.05 ms per step). At 168 registers
+// (12 warps, no spills) this kernel takes 1.96 against 1.79 ms per step.
 template <int kDef>
 __global__ void __launch_bounds__(kFaceBlockM, 8) face2_lxf_mixed_kernel(
     const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, Quad6F lobatto, const float* __restrict__ F,
