@@ -135,6 +135,38 @@ def test_riemann_problem_200_steps(hyp, orc):
     print(f"riemann N=1000, 200 steps: max per-variable relative error {err:.2e}")
 
 
+@pytest.mark.parametrize("flux", ["rusanov", "lxf"])
+def test_riemann_problem_nondefault_exponents(hyp, orc, flux):
+    """The Riemann problem with non-integer beta, gamma (main.jl:133's alternative
+    Barton2009 parameters), whose powers take the exp/log branch of the step kernels:
+    FP64 against the oracle after 100 steps; mixed against FP64 (L1 density <= 1e-6)."""
+    from hyperelasticsolver_gb300._cases import riemann_1ph, initial_condition
+    eos = hyp.Barton2009(_beta=3.577, _gamma=2.088)
+    nx = 1000
+    pb = orc.problem(nx=nx, cfl=0.5, flux=orc.FLUX_LXF if flux == "lxf" else orc.FLUX_RUSANOV,
+                     eos=(orc.barton2009(beta=3.577, gamma=2.088),) * 2)
+    Pl, Pr = riemann_1ph(eos)
+    Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
+    Qo, _, to, _ = orc.run(pb, Q0, max_steps=100)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with hyp.Solver(eos, nx, cfl=0.5, flux=flux, precision=prec) as s:
+            s.upload(Q0)
+            steps, t = s.step(max_steps=100)
+            assert steps == 100
+            out[prec] = (s.download(), t)
+    assert abs(out["fp64"][1] - to) <= RTOL_FP64 * to
+    err = assert_close_soa(out["fp64"][0], Qo, RTOL_FP64, f"non-default exponents ({flux})")
+    def density(Q):  # sqrt(det(rho A) / rho0), cons2prim's density
+        m = Q[5:14]
+        return np.sqrt((m[0] * (m[4] * m[8] - m[5] * m[7]) - m[3] * (m[1] * m[8] - m[7] * m[2])
+                        + m[6] * (m[1] * m[5] - m[4] * m[2])) / 8.93)
+    a, b = density(out["mixed"][0]), density(out["fp64"][0])
+    l1 = np.sum(np.abs(a - b)) / np.sum(np.abs(b))
+    print(f"riemann non-default exponents ({flux}): FP64 vs oracle {err:.1e}, mixed density L1 {l1:.1e}")
+    assert l1 <= 1e-6
+
+
 def test_riemann_problem_full_run(hyp, orc):
     """The same problem to t_end = 0.3 / max lambda(t=0) (1113 steps). Over that
     many steps the problem itself amplifies rounding: the oracle run on its own

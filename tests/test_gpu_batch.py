@@ -65,6 +65,30 @@ def test_fp64_batch_matches_oracle(hyp, orc):
         o += n
 
 
+def test_batch_nondefault_exponents(hyp, orc):
+    """Non-integer beta, gamma (main.jl:133's alternative Barton2009 parameters): the
+    FP64 batch against the oracle, and the mixed batch against single mixed runs."""
+    sizes = np.array([40, 17, 64], dtype=np.int64)
+    Q0 = make_batch_state(orc, sizes, seed=6)
+    eos = hyp.Barton2009(_beta=3.577, _gamma=2.088)
+    oeos = (orc.barton2009(beta=3.577, gamma=2.088),) * 2
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with hyp.Batch(eos, sizes, precision=prec) as b:
+            b.upload(Q0)
+            b.step(25)
+            out[prec] = b.download()
+    o = 0
+    for n in sizes:
+        Qo, _, _, _ = orc.run(orc.problem(nx=int(n), cfl=0.5, eos=oeos), Q0[:, o:o + n], max_steps=25)
+        assert_close_soa(out["fp64"][:, o:o + n], Qo, RTOL_FP64, f"FP64 problem of {n} cells")
+        with hyp.Solver(eos, int(n), precision="mixed") as s:
+            s.upload(np.ascontiguousarray(Q0[:, o:o + n]))
+            s.step(max_steps=25)
+            assert_close_soa(out["mixed"][:, o:o + n], s.download(), MIXED_AGREE, f"mixed problem of {n} cells")
+        o += n
+
+
 def test_mixed_batch_accuracy_and_autotune(hyp, orc):
     """500 steps on 48 problems (256..4096 cells): per-problem relative L1 density
     error of the mixed batch against the FP64 batch <= 1e-6; every autotuner variant

@@ -205,3 +205,35 @@ def test_mixed_twophase_uniform_state_preserved(hyp, orc):
     # through it cancel only to rounding: the state stays uniform to that level.
     scale = np.max(np.abs(Qa), axis=1, keepdims=True)
     assert np.max(np.abs(Qb - Qa) / np.maximum(scale, 1e-30)) < 1e-9
+
+
+@pytest.mark.parametrize("flux", ["hll", "lxf"])
+def test_nondefault_exponents_twophase(hyp, orc, flux):
+    """Phase 1 with non-integer beta, gamma (the alternative Barton2009 parameters of
+    main.jl:133): the step runs the kernels' general-exponent instances (powers through
+    exp/log), which the default parameters never reach. FP64 against the oracle at
+    RTOL_FP64 after 30 steps of test case 6; mixed against FP64 after 100 steps."""
+    from hyperelasticsolver_gb300._cases import mph_case, initial_condition
+    eos = (hyp.Barton2009(_beta=3.577, _gamma=2.088), hyp.Barton2009(_b0=B0_SOFT))
+    oflux = orc.FLUX_HLL if flux == "hll" else orc.FLUX_LXF
+    nx = 200
+    pb = orc.problem(model=orc.MODEL_MULTI, flux=oflux, nx=nx, cfl=0.6,
+                     eos=(orc.barton2009(beta=3.577, gamma=2.088), orc.barton2009(b0=B0_SOFT)))
+    Pl, Pr = mph_case(6)
+    Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
+    Qo, _, to, _ = orc.run(pb, Q0, max_steps=30)
+    with hyp.Solver(eos, nx, model="multi", flux=flux, cfl=0.6) as s:
+        s.upload(Q0)
+        n, t = s.step(max_steps=30)
+        assert n == 30 and abs(t - to) <= RTOL_FP64 * to
+        err = assert_close_soa(s.download(), Qo, RTOL_FP64, f"non-default exponents ({flux})")
+    out = {}
+    for prec in ("fp64", "mixed"):
+        with hyp.Solver(eos, nx, model="multi", flux=flux, precision=prec, cfl=0.6) as s:
+            s.upload(Q0)
+            assert s.step(max_steps=100)[0] == 100
+            out[prec] = s.download()
+    errs = [l1_linf(a, b) for a, b in zip(phase_densities(out["mixed"]), phase_densities(out["fp64"]))]
+    print(f"two-phase non-default exponents ({flux}): FP64 vs oracle {err:.1e}; mixed density L1/Linf "
+          + ", ".join(f"{l1:.1e}/{li:.1e}" for l1, li in errs))
+    assert max(e[0] for e in errs) <= 1e-6
