@@ -121,7 +121,6 @@ __device__ __forceinline__ bool updated(int64_t i, int64_t n, int trans) { retur
 
 __device__ __forceinline__ double face_lambda(double la, double lb) { return la > lb ? la : lb; }
 
-__device__ __forceinline__ double dtdx_of(const AdjArgs& g, double lmax) { return ((g.cfl * g.dx) / lmax) / g.dx; }
 
 // Partial sums of r * rb_n, where rb_n = -sum_{updated i} Qb'_i . (F_{i+1/2} - F_{i-1/2})
 // and, for an updated cell, F_{i+1/2} - F_{i-1/2} = (Q_i - Q'_i) / r with Q' the step's
@@ -158,7 +157,7 @@ __global__ void __launch_bounds__(kAdjBlock) adj_cell_kernel(AdjArgs g, EosC e) 
   __shared__ double s_lamb_max;
   const int64_t n = g.n;
   const double lmax = __longlong_as_double((long long)*g.lmax);
-  const double r = dtdx_of(g, lmax);
+  const double r = step_scalars(g.cfl, g.dx, lmax, false).dtdx;  // dt/dx of the forward step
   if (threadIdx.x < 32) {  // rb_n: the partial sums in a fixed order
     double s = 0.0;
     for (int k = threadIdx.x; k < g.part_grid; k += 32) s += g.rpart[k];

@@ -183,9 +183,8 @@ __global__ void __launch_bounds__(kBlock) batch_f64_update_kernel(const double* 
     const bool active = tn < t_end;
     const double lmax = __longlong_as_double((long long)b.slots[par * P + p]);
     const double dx = b.dx[p];
-    const double dt = (cfl * dx) / lmax;
-    const double lam_lxf = dx / dt;
-    const double dtdx = lxf ? 1.0 / lam_lxf : dt / dx;
+    const StepScalars sc = step_scalars(cfl, dx, lmax, lxf);
+    const double dt = sc.dt, lam_lxf = sc.lam_lxf, dtdx = sc.dtdx;
     if (d.lead && threadIdx.x == 0) {
       b.t[(1 - par) * P + p] = active ? tn + dt : tn;
       b.slots[(1 - par) * P + p] = 0ull;

@@ -72,6 +72,27 @@ __device__ __forceinline__ void rusanov_face(const double* __restrict__ Q, const
   }
 }
 
+// A step's dt = cfl dx / max lambda, the LxF lambda = dx / dt and dt/dx (main.jl:223-225;
+// for LxF the update's dt/dx is 1 / lambda, main.jl:40), evaluated by lane 0 of each
+// warp and broadcast: the same expressions, so the same bits, as evaluating them in
+// every thread, at 1/32 of the FP64 divisions on the FP64 pipe that bounds the FP64
+// kernels. Every lane of the warp must call it (no thread may have returned).
+struct StepScalars {
+  double dt, lam_lxf, dtdx;
+};
+__device__ __forceinline__ StepScalars step_scalars(double cfl, double dx, double lmax, bool lxf) {
+  StepScalars s{0.0, 0.0, 0.0};
+  if ((threadIdx.x & 31) == 0) {
+    s.dt = (cfl * dx) / lmax;
+    s.lam_lxf = dx / s.dt;
+    s.dtdx = lxf ? 1.0 / s.lam_lxf : s.dt / dx;
+  }
+  s.dt = __shfl_sync(0xffffffffu, s.dt, 0);
+  s.lam_lxf = __shfl_sync(0xffffffffu, s.lam_lxf, 0);
+  s.dtdx = __shfl_sync(0xffffffffu, s.dtdx, 0);
+  return s;
+}
+
 // The two phases' EOS, passed to the two-phase kernels by value.
 struct Eos2 {
   EosC e[2];

@@ -78,10 +78,9 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
   const double tn = *t_in;
   const bool active = tn < t_end;
   const double lmax = __longlong_as_double((long long)*lam_in);
-  const double dt = (cfl * dx) / lmax;
   // Rusanov / HLL: dt/dx (main.jl:225); LxF: 1/lambda with lambda = dx/dt (main.jl:223, :40)
-  const double lam_lxf = dx / dt;
-  const double dtdx = flux == HYP_FLUX_LXF ? 1.0 / lam_lxf : dt / dx;
+  const StepScalars sc = step_scalars(cfl, dx, lmax, flux == HYP_FLUX_LXF);
+  const double dt = sc.dt, lam_lxf = sc.lam_lxf, dtdx = sc.dtdx;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *t_out = active ? tn + dt : tn;
     *lam_next = 0ull;

@@ -101,13 +101,12 @@ __global__ void __launch_bounds__(kFaceBlock) face2_lxf_f64_kernel(
     const unsigned long long* lam_now, double cfl, double dx, double* __restrict__ FF, double* __restrict__ DM,
     double* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
   if (!(*t_now < t_end)) return;
+  const double lmax = __longlong_as_double((long long)*lam_now);
+  const double lam = step_scalars(cfl, dx, lmax, true).lam_lxf;  // lambda = dx/dt (main.jl:223)
   const int64_t f = (int64_t)blockIdx.x * kFaceBlock + threadIdx.x;  // face between cells f-1 and f
   if (f > n) return;
   const int64_t nf = n + 1;
   const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
-  const double lmax = __longlong_as_double((long long)*lam_now);
-  const double dt = (cfl * dx) / lmax;
-  const double lam = dx / dt;  // lambda = dx/dt (main.jl:223)
   double QL[30], QR[30], fl[30], fr[30], ff[30], dm[30], dp[30];
   for (int v = 0; v < 30; ++v) {
     QL[v] = Q[v * n + L];
@@ -135,8 +134,8 @@ __global__ void __launch_bounds__(kBlock) update2_f64_kernel(const double* __res
   const double tn = *t_in;
   const bool active = tn < t_end;
   const double lmax = __longlong_as_double((long long)*lam_in);
-  const double dt = (cfl * dx) / lmax;
-  const double dtdx = dt / dx;
+  const StepScalars sc = step_scalars(cfl, dx, lmax, false);
+  const double dt = sc.dt, dtdx = sc.dtdx;
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     *t_out = active ? tn + dt : tn;
     *lam_next = 0ull;
