@@ -123,15 +123,24 @@ __global__ void __launch_bounds__(kBlock) update2_mixed_kernel(
     const float* __restrict__ Qh, const float* __restrict__ Ql, float* __restrict__ Qh_out, float* __restrict__ Ql_out,
     int64_t pitch, int64_t n, const float* __restrict__ FF, const float* __restrict__ DM, const float* __restrict__ DP,
     const unsigned long long* lam_in, unsigned long long* lam_next, const double* t_in, double* t_out,
-    long long* steps, double t_end, double cfl, double dx, int bc) {
-  const double tn = *t_in;
-  const bool active = tn < t_end;
-  const double lmax = __longlong_as_double((long long)*lam_in);
-  const double dt = (cfl * dx) / lmax;  // used by thread 0 only
-  // dt/dx = cfl / lmax in FP32: two FP64 divisions in every thread cost this
-  // memory-bound kernel a quarter of its time (0.65 -> 0.49 ms at 2^22 cells)
-  const float dtdx = (float)cfl / (float)lmax;
+    long long* steps, double t_end, double cfl, float cfl_f, double dx, int bc) {
+  // lane 0 reads the control and broadcasts: dt/dx = cfl / lmax in FP32, cfl_f = cfl
+  // rounded on the host (two FP64 divisions in every thread cost this memory-bound
+  // kernel a quarter of its time: 0.65 -> 0.49 ms at 2^22 cells; the broadcast of
+  // the FP64 compare, 0.49 -> 0.48 ms)
+  double tn = 0.0, lmax = 0.0;
+  int act = 0;
+  float dtdx_0 = 0.0f;
+  if ((threadIdx.x & 31) == 0) {
+    tn = *t_in;
+    act = tn < t_end;
+    lmax = __longlong_as_double((long long)*lam_in);
+    dtdx_0 = cfl_f / (float)lmax;
+  }
+  const bool active = __shfl_sync(0xffffffffu, act, 0) != 0;
+  const float dtdx = __shfl_sync(0xffffffffu, dtdx_0, 0);
   if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double dt = (cfl * dx) / lmax;
     *t_out = active ? tn + dt : tn;
     *lam_next = 0ull;
     if (active) *steps += 1;
@@ -209,7 +218,7 @@ cudaError_t launch_update2_mixed(hyp_ctx* c, int p, double t_end) {
   update2_mixed_kernel<<<grid_m(c->n, kBlock), kBlock, 0, c->stream>>>(
       c->Qh[p], c->Ql[p], c->Qh[1 - p], c->Ql[1 - p], c->mpitch, c->n, c->FF32, c->DM32, c->DP32,
       &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p], &c->st->t[1 - p], &c->st->steps, t_end,
-      c->cfg.cfl, dx, c->cfg.bc);
+      c->cfg.cfl, (float)c->cfg.cfl, dx, c->cfg.bc);
   return cudaGetLastError();
 }
 
