@@ -59,6 +59,7 @@ static int free_ctx(hyp_ctx* c) {
   cudaFree(c->DP32);
   cudaFree(c->FF32);
   cudaFree(c->st);
+  cudaFree(c->hist_dev);
   if (c->st_host) cudaFreeHost(c->st_host);
   for (auto& e : c->ev)
     if (e) cudaEventDestroy(e);
@@ -369,7 +370,7 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
     // steps always precede inactive ones, so the state index is steps0 + active.
     long long k = steps0 + launched;
     long long s = 0;
-    if (!prof) {
+    if (!prof && !c->hist_on) {
       while (rc == HYP_OK && todo - s >= gs) {
         rc = ensure_graph(c, k, t_end);
         if (rc == HYP_OK) {
@@ -380,7 +381,14 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
         k += gs;
       }
     }
-    for (; rc == HYP_OK && s < todo; ++s, ++k) rc = enqueue_step(c, k, t_end, prof);
+    for (; rc == HYP_OK && s < todo; ++s, ++k) {
+      rc = enqueue_step(c, k, t_end, prof);
+      if (rc == HYP_OK && c->hist_on) {  // t after step k (an inactive step carries t across)
+        cudaError_t e = cudaMemcpyAsync(c->hist_dev + (k - steps0), &c->st->t[(k + 1) & 1], sizeof(double),
+                                        cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) rc = set_err(c, HYP_ERR_CUDA, std::string("cudaMemcpyAsync(t): ") + cudaGetErrorString(e));
+      }
+    }
     launched += todo;
     if (rc != HYP_OK) break;
     if (!std::isinf(t_end)) {
@@ -406,6 +414,31 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
   if (steps_done) *steps_done = (int)active;
   if (t_out) *t_out = c->t_host;
   return check_cell_error(c);
+}
+
+extern "C" int hyp_step_times(hyp_ctx* c, int max_steps, double t_end, int* steps_done, double* t_out,
+                              double* t_hist) {
+  if (!c) return HYP_ERR_INVALID;
+  if (max_steps <= 0 || !t_hist) return set_err(c, HYP_ERR_INVALID, "hyp_step_times: needs max_steps >= 1 and t_hist");
+  CK(cudaSetDevice(c->device));
+  if (c->hist_cap < max_steps) {
+    cudaFree(c->hist_dev);
+    c->hist_dev = nullptr;
+    c->hist_cap = 0;
+    CK(cudaMalloc(&c->hist_dev, (size_t)max_steps * sizeof(double)));
+    c->hist_cap = max_steps;
+  }
+  c->hist_on = 1;
+  int done = 0;
+  const int rc = hyp_step(c, max_steps, t_end, &done, t_out);
+  c->hist_on = 0;
+  if (steps_done) *steps_done = done;
+  const bool cell_err = rc == HYP_ERR_NEG_DET || rc == HYP_ERR_NONFINITE;
+  if ((rc == HYP_OK || cell_err) && done > 0) {  // the steps taken before a cell error are logged too
+    CK(cudaMemcpyAsync(t_hist, c->hist_dev, (size_t)done * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+  }
+  return rc;
 }
 
 extern "C" int hyp_set_wait_limit(hyp_ctx* c, int tries) {

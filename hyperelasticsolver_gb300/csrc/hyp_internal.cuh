@@ -171,6 +171,11 @@ struct hyp_ctx {
   // FP64: buffer parity; 6 for mixed: parity x three max-lambda slots)
   cudaGraphExec_t graph[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int graph_steps = 0;
+  // hyp_step_times: while set, every step is launched on its own and followed by
+  // a copy of its new time into hist_dev[step index within the call]
+  double* hist_dev = nullptr;
+  long long hist_cap = 0;
+  int hist_on = 0;
   double graph_t_end = 0.0;
   std::string err;
   int64_t err_cell = -1;

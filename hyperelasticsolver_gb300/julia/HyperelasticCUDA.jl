@@ -193,6 +193,18 @@ function step!(s::Solver; max_steps::Integer=0, T::Float64=Inf)
   (n[], t[])
 end
 
+"""step_times!(s; max_steps, T): step! that also returns the time after every step
+taken (the Step / t / dt log line of main.jl:229-237), read back once at the end:
+(steps, t, t_hist); dt of step j is t_hist[j] - t_hist[j-1]."""
+function step_times!(s::Solver; max_steps::Integer, T::Float64=Inf)
+  max_steps >= 1 || throw(ArgumentError("max_steps >= 1"))
+  n, t = Ref{Cint}(0), Ref{Float64}(0.0)
+  hist = Vector{Float64}(undef, max_steps)
+  check(ccall((:hyp_step_times, libhyp), Cint, (Ptr{Cvoid}, Cint, Float64, Ref{Cint}, Ref{Float64}, Ptr{Float64}),
+              s.h, max_steps, T, n, t, hist), "hyp_step_times", s.h)
+  (n[], t[], hist[1:n[]])
+end
+
 # ---- queries, kernel choices and timing of a context ----
 "error_cell(s): the first cell that raised NEG_DET / NONFINITE in the last call (-1: none)"
 error_cell(s::Solver) = ccall((:hyp_error_cell, libhyp), Int64, (Ptr{Cvoid},), s.h)

@@ -68,6 +68,18 @@ class Solver:
                 self._h, "hyp_step")
         return s.value, t.value
 
+    def step_times(self, max_steps, t_end=math.inf):
+        """step() that also returns the time and dt of every step taken (the Step / t /
+        dt line main.jl:229-237 logs), read back once at the end: (t, dt) arrays."""
+        t0 = self.time()[0]
+        hist = np.empty(max(int(max_steps), 1))
+        s = ctypes.c_int(0)
+        t = ctypes.c_double(0.0)
+        L.check(L.load().hyp_step_times(self._h, int(max_steps), float(t_end), ctypes.byref(s), ctypes.byref(t),
+                                        L.ptr(hist)), self._h, "hyp_step_times")
+        th = hist[:s.value].copy()
+        return th, np.diff(np.concatenate(([t0], th)))
+
     def max_wavespeed(self):
         v = ctypes.c_double(0.0)
         L.check(L.load().hyp_max_wavespeed(self._h, ctypes.byref(v)), self._h, "hyp_max_wavespeed")

@@ -93,6 +93,13 @@ int hyp_download(hyp_ctx* ctx, double* Q, int64_t n_cells, int n_vars);
    (:212), t += dt (:214), update of the interior cells with frozen ends
    (:218-226). Reports the steps taken and the new time. */
 int hyp_step(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double* t_out);
+/* hyp_step (max_steps >= 1) that also returns the time after every step taken,
+   t_hist[0 .. *steps_done - 1] (host, max_steps entries): the Step / t / dt line
+   main.jl:229-237 logs each step, read back once at the end rather than with a
+   host round trip per step. dt of step j is t_hist[j] - t_hist[j - 1] (the time
+   before the call for j = 0). The steps are the same launches as hyp_step's, so
+   state and times agree bitwise with it. */
+int hyp_step_times(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double* t_out, double* t_hist);
 
 /* max_i lambda_i of the current state, lambda_i = max |get_eigvals(Q_i)|
    (main.jl:204-211; HyperelasticityMPh.jl:252-266). */

@@ -333,3 +333,36 @@ def test_contexts_on_concurrent_host_threads(hyp, orc):
         t.join()
     for k in range(len(jobs)):
         assert np.array_equal(alone[k][0], together[k][0]) and alone[k][1] == together[k][1]
+
+
+@pytest.mark.parametrize("model,precision", [("single", "fp64"), ("single", "mixed"), ("multi", "mixed")])
+def test_step_times_log(hyp, orc, model, precision):
+    """hyp_step_times returns the time after every step (the Step / t / dt line of
+    main.jl:229-237), read back once; its steps are hyp_step's, so the log equals the
+    times of single steps and the state is the same, bitwise. With t_end inside the
+    run the log stops with the steps."""
+    if model == "single":
+        Q0, _ = c1_state(hyp, orc)
+        eos, kw = hyp.Barton2009(), {}
+    else:
+        from hyperelasticsolver_gb300._cases import mph_case, initial_condition
+        eos = (hyp.Barton2009(), hyp.Barton2009(_b0=2.1 * np.sqrt(0.1)))
+        pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, nx=1000, cfl=0.6,
+                         eos=(orc.barton2009(), orc.barton2009(b0=2.1 * np.sqrt(0.1))))
+        Pl, Pr = mph_case(6)
+        Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), 1000)
+        kw = dict(model="multi", flux="hll")
+    with hyp.Solver(eos, 1000, cfl=0.5, precision=precision, **kw) as s:
+        s.upload(Q0)
+        th, dt = s.step_times(60)
+        Qa = s.download()
+        s.upload(Q0)
+        ts = [s.step(max_steps=1)[1] for _ in range(60)]
+        assert len(th) == 60 and np.array_equal(th, ts)
+        assert np.array_equal(s.download(), Qa)
+        assert np.all(dt > 0) and abs(np.sum(dt) - th[-1]) <= 1e-14 * th[-1]
+        s.upload(Q0)
+        th2, _ = s.step_times(60, t_end=0.5 * (th[29] + th[30]))
+        assert np.array_equal(th2, th[:31])
+        with pytest.raises(hyp._lib.HypError):
+            s.step_times(0)
