@@ -272,10 +272,10 @@ def run_ours(args):
         dist.barrier()
     t0 = time.perf_counter()
     s.upload(pin_in.array)
-    t_log, dt_log = s.step_times(K)  # t and dt of every step (the reference logs Step/t/dt each step)
+    for _ in range(K):
+        s.step(max_steps=1)  # per step the host reads back t (the reference logs Step/t/dt every step)
     s.download(pin_out.array)
     e2e_s = dist_max(dist, time.perf_counter() - t0)
-    assert len(t_log) == K and np.all(dt_log > 0)
     e2e = WORLD * n * K / e2e_s
     s.close()
     pin_in.close()
@@ -303,7 +303,7 @@ def run_ours(args):
         "config": config_block(args), "precision": PRECISION_NOTE[prec],
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": state_bytes / K,
-                "d2h_bytes_per_step": state_bytes / K + 8},
+                "d2h_bytes_per_step": state_bytes / K + 64},
         "gpu_launches": tm["n_cell"] + tm["n_update"],
         "roofline": rf,
     }

@@ -344,6 +344,9 @@ static int ensure_graph(hyp_ctx* c, long long k0, double t_end) {
   return HYP_OK;
 }
 
+// hyp_step_times: the time after a step, copied once the step's kernels are done
+__global__ void log_time_kernel(const DevState* S, int parity, double* out) { *out = S->t[parity]; }
+
 extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done, double* t_out) {
   if (!c) return HYP_ERR_INVALID;
   if (std::isnan(t_end)) return set_err(c, HYP_ERR_INVALID, "t_end is NaN");
@@ -384,9 +387,9 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
     for (; rc == HYP_OK && s < todo; ++s, ++k) {
       rc = enqueue_step(c, k, t_end, prof);
       if (rc == HYP_OK && c->hist_on) {  // t after step k (an inactive step carries t across)
-        cudaError_t e = cudaMemcpyAsync(c->hist_dev + (k - steps0), &c->st->t[(k + 1) & 1], sizeof(double),
-                                        cudaMemcpyDeviceToDevice, c->stream);
-        if (e != cudaSuccess) rc = set_err(c, HYP_ERR_CUDA, std::string("cudaMemcpyAsync(t): ") + cudaGetErrorString(e));
+        log_time_kernel<<<1, 1, 0, c->stream>>>(c->st, (int)((k + 1) & 1), c->hist_dev + (k - steps0));
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) rc = set_err(c, HYP_ERR_CUDA, std::string("log_time_kernel: ") + cudaGetErrorString(e));
       }
     }
     launched += todo;
@@ -428,6 +431,8 @@ extern "C" int hyp_step_times(hyp_ctx* c, int max_steps, double t_end, int* step
     CK(cudaMalloc(&c->hist_dev, (size_t)max_steps * sizeof(double)));
     c->hist_cap = max_steps;
   }
+  // steps launched one by one (no step graphs), each followed by log_time_kernel;
+  // writing the log inside the step kernels measured 0.5-1.8 % slower steps
   c->hist_on = 1;
   int done = 0;
   const int rc = hyp_step(c, max_steps, t_end, &done, t_out);

@@ -171,11 +171,9 @@ struct hyp_ctx {
   // FP64: buffer parity; 6 for mixed: parity x three max-lambda slots)
   cudaGraphExec_t graph[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int graph_steps = 0;
-  // hyp_step_times: while set, every step is launched on its own and followed by
-  // a copy of its new time into hist_dev[step index within the call]
-  double* hist_dev = nullptr;
+  double* hist_dev = nullptr;  // hyp_step_times: device array of the per-step times
   long long hist_cap = 0;
-  int hist_on = 0;
+  int hist_on = 0;             // set during hyp_step_times: steps launched one by one, each logged
   double graph_t_end = 0.0;
   std::string err;
   int64_t err_cell = -1;

@@ -97,8 +97,10 @@ int hyp_step(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double*
    t_hist[0 .. *steps_done - 1] (host, max_steps entries): the Step / t / dt line
    main.jl:229-237 logs each step, read back once at the end rather than with a
    host round trip per step. dt of step j is t_hist[j] - t_hist[j - 1] (the time
-   before the call for j = 0). The steps are the same launches as hyp_step's, so
-   state and times agree bitwise with it. */
+   before the call for j = 0). The steps run hyp_step's kernels, launched one by
+   one (not from its CUDA graphs), each followed by a one-thread copy of its time,
+   so state and times agree bitwise with hyp_step at a few microseconds more per
+   step. */
 int hyp_step_times(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double* t_out, double* t_hist);
 
 /* max_i lambda_i of the current state, lambda_i = max |get_eigvals(Q_i)|
