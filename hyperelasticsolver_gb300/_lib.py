@@ -84,6 +84,7 @@ _SIGS = {
     "hyp_upload": ([ctypes.c_void_p, _dp, _i64, ctypes.c_int, ctypes.c_double], ctypes.c_int),
     "hyp_download": ([ctypes.c_void_p, _dp, _i64, ctypes.c_int], ctypes.c_int),
     "hyp_step": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int), _dp], ctypes.c_int),
+    "hyp_set_eos": ([ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(Barton2009C)], ctypes.c_int),
     "hyp_step_times": ([ctypes.c_void_p, ctypes.c_int, ctypes.c_double, ctypes.POINTER(ctypes.c_int), _dp, _dp],
                        ctypes.c_int),
     "hyp_max_wavespeed": ([ctypes.c_void_p, _dp], ctypes.c_int),

@@ -222,6 +222,7 @@ int ctx_finish_install(hyp_ctx* c, double t0) {
   int rc = sync_state(c);
   if (rc != HYP_OK) return rc;
   c->cur = 0;
+  c->has_state = 1;
   c->t_host = t0;
   c->steps_host = 0;
   c->err_cell = -1;
@@ -444,6 +445,42 @@ extern "C" int hyp_step_times(hyp_ctx* c, int max_steps, double t_end, int* step
     CK(cudaStreamSynchronize(c->stream));
   }
   return rc;
+}
+
+extern "C" int hyp_set_eos(hyp_ctx* c, int phase, const hyp_barton2009* eos) {
+  if (!c || !eos) return HYP_ERR_INVALID;
+  if (phase < 0 || phase > 1 || (phase == 1 && c->cfg.model != HYP_MODEL_MULTI))
+    return set_err(c, HYP_ERR_INVALID, "hyp_set_eos: phase must be 0, or 1 for a two-phase context");
+  if (!valid_eos(*eos)) return set_err(c, HYP_ERR_INVALID, "hyp_set_eos: invalid Barton2009 parameters");
+  CK(cudaSetDevice(c->device));
+  CK(cudaStreamSynchronize(c->stream));
+  c->cfg.eos[phase] = *eos;
+  c->eos[phase] = to_eos(*eos);
+  if (c->cfg.model == HYP_MODEL_SINGLE) {  // a single-phase context keeps both slots equal (hyp_create)
+    c->cfg.eos[1] = *eos;
+    c->eos[1] = c->eos[0];
+  }
+  c->eos2.e[0] = c->eos[0];
+  c->eos2.e[1] = c->eos[1];
+  c->eos_mixed = make_eos_mixed(c->eos[0]);
+  for (auto& g : c->graph)  // the captured steps hold the old parameters by value
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+  c->graph_steps = 0;
+  free_tape(c);  // a recorded run belongs to the old parameters
+  if (mixed1(c) && c->has_state) {
+    // the mixed step caches each cell's wave speed and float-float islands, which
+    // depend on the EOS: recompute them for the current state (its slot k % 3)
+    unsigned long long* slot = &c->st->lam_slots[c->steps_host % 3];
+    CK(cudaMemsetAsync(slot, 0, sizeof *slot, c->stream));
+    CK(launch_lam1_mixed(c, c->cur, slot));
+    int rc = sync_state(c);
+    if (rc != HYP_OK) return rc;
+    return check_cell_error(c);
+  }
+  return HYP_OK;
 }
 
 extern "C" int hyp_set_wait_limit(hyp_ctx* c, int tries) {

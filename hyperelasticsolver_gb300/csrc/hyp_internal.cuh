@@ -159,6 +159,7 @@ struct hyp_ctx {
   hyp::DevState* st = nullptr;
   hyp::DevState* st_host = nullptr;  // pinned mirror
   int cur = 0;             // parity of the buffer that holds the current state
+  int has_state = 0;       // a state was uploaded or installed
   long long steps_host = 0;
   double t_host = 0.0;
   int profiling = 0;

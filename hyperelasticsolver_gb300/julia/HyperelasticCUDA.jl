@@ -179,6 +179,9 @@ end
 upload!(s::Solver, Q::Matrix{Float64}, t0=0.0) =
   check(ccall((:hyp_upload, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64, Cint, Float64), s.h, Q, s.n, s.nvar, t0),
         "hyp_upload", s.h)
+"set_eos!(s, phase, eos): replace the Barton2009 parameters of phase 0 (or 1, two phases); state and t are kept"
+set_eos!(s::Solver, phase::Integer, eos::Barton2009C) =
+  check(ccall((:hyp_set_eos, libhyp), Cint, (Ptr{Cvoid}, Cint, Ref{Barton2009C}), s.h, phase, eos), "hyp_set_eos", s.h)
 function download(s::Solver)
   Q = Matrix{Float64}(undef, s.n, s.nvar)
   check(ccall((:hyp_download, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Int64, Cint), s.h, Q, s.n, s.nvar),

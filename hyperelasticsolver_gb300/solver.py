@@ -68,6 +68,15 @@ class Solver:
                 self._h, "hyp_step")
         return s.value, t.value
 
+    def set_eos(self, eos, phase=0):
+        """Replace the Barton2009 parameters of one phase (1: two-phase contexts only);
+        the state and time are kept (the reference passes eos to every call, main.jl:134)."""
+        c = eos.c()
+        L.check(L.load().hyp_set_eos(self._h, int(phase), ctypes.byref(c)), self._h, "hyp_set_eos")
+        self.cfg.eos[int(phase)] = c
+        if self.model == L.HYP_MODEL_SINGLE:
+            self.cfg.eos[1] = c
+
     def step_times(self, max_steps, t_end=math.inf):
         """step() that also returns the time and dt of every step taken (the Step / t /
         dt line main.jl:229-237 logs), read back once at the end: (t, dt) arrays."""

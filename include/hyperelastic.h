@@ -93,6 +93,11 @@ int hyp_download(hyp_ctx* ctx, double* Q, int64_t n_cells, int n_vars);
    (:212), t += dt (:214), update of the interior cells with frozen ends
    (:218-226). Reports the steps taken and the new time. */
 int hyp_step(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double* t_out);
+/* Replace the Barton2009 parameters (EquationsOfState.jl:71-116) of one phase of a
+   context: phase 0, or 1 for a two-phase context. The state and time are kept; the
+   next step uses the new EOS (the reference passes eos to every call, main.jl:134,
+   so a driver may change it between steps). A recorded adjoint run is discarded. */
+int hyp_set_eos(hyp_ctx* ctx, int phase, const hyp_barton2009* eos);
 /* hyp_step (max_steps >= 1) that also returns the time after every step taken,
    t_hist[0 .. *steps_done - 1] (host, max_steps entries): the Step / t / dt line
    main.jl:229-237 logs each step, read back once at the end rather than with a

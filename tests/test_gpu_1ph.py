@@ -366,3 +366,50 @@ def test_step_times_log(hyp, orc, model, precision):
         assert np.array_equal(th2, th[:31])
         with pytest.raises(hyp._lib.HypError):
             s.step_times(0)
+
+
+@pytest.mark.parametrize("model,precision", [("single", "fp64"), ("single", "mixed"), ("multi", "fp64"),
+                                             ("multi", "mixed")])
+def test_set_eos_between_steps(hyp, orc, model, precision):
+    """hyp_set_eos between steps: 20 steps with one EOS, then the EOS of a phase
+    changed and 20 more steps, equal a fresh context with the new EOS continued from
+    the 20-step state (FP64 bitwise; mixed to the rounding of re-splitting the state
+    into hi/lo pairs). Setting the same EOS again leaves the run unchanged, bitwise."""
+    Q0 = c1_state(hyp, orc, nx=600)[0]
+    new = hyp.Barton2009(_b0=2.3, _beta=3.577)
+    if model == "single":
+        eos_a, eos_b, phase, kw = hyp.Barton2009(), new, 0, {}
+    else:
+        from hyperelasticsolver_gb300 import HyperelasticityMPh as HM
+        from hyperelasticsolver_gb300._cases import mph_interface_prims
+        soft = hyp.Barton2009(_b0=2.1 * np.sqrt(0.1))
+        eos_a, eos_b, phase = (hyp.Barton2009(), soft), (hyp.Barton2009(), new), 1
+        Q0 = np.ascontiguousarray(HM.prim2cons_mph(eos_a, mph_interface_prims(eos_a[0], 600)).T)
+        kw = dict(model="multi", flux="hll")
+    with hyp.Solver(eos_a, 600, precision=precision, **kw) as s:
+        s.upload(Q0)
+        s.step(max_steps=20)
+        Q20, t20 = s.download(), s.time()[0]
+        s.set_eos(new, phase=phase)
+        _, t_switch = s.step(max_steps=20)
+        Q_switch = s.download()
+        s.upload(Q0)
+        s.step(max_steps=20)
+        s.set_eos(eos_a[phase] if model == "multi" else eos_a, phase=phase)  # the same parameters again
+        s.step(max_steps=20)
+        Q_same = s.download()
+        with pytest.raises(hyp._lib.HypError):
+            s.set_eos(new, phase=1 if model == "single" else 2)
+    with hyp.Solver(eos_a, 600, precision=precision, **kw) as s:
+        s.upload(Q0)
+        s.step(max_steps=40)
+        assert np.array_equal(s.download(), Q_same)
+    with hyp.Solver(eos_b, 600, precision=precision, **kw) as s:
+        s.upload(Q20, t0=t20)
+        _, t_fresh = s.step(max_steps=20)
+        Q_fresh = s.download()
+    if precision == "fp64":
+        assert t_fresh == t_switch and np.array_equal(Q_fresh, Q_switch)
+    else:
+        assert abs(t_fresh - t_switch) <= 1e-12 * t_fresh
+        assert_close_soa(Q_switch, Q_fresh, 1e-9, "set_eos vs fresh context")
