@@ -374,9 +374,10 @@ def test_set_eos_between_steps(hyp, orc, model, precision):
     """hyp_set_eos between steps: 20 steps with one EOS, then the EOS of a phase
     changed and 20 more steps, equal a fresh context with the new EOS continued from
     the 20-step state (FP64 bitwise; mixed to the rounding of re-splitting the state
-    into hi/lo pairs). Setting the same EOS again leaves the run unchanged, bitwise."""
+    into hi/lo pairs; stale cached speeds or islands would differ by far more).
+    Setting the same EOS again leaves the run unchanged, bitwise."""
     Q0 = c1_state(hyp, orc, nx=600)[0]
-    new = hyp.Barton2009(_b0=2.3, _beta=3.577)
+    new = hyp.Barton2009(_rho0=9.0, _b0=2.3, _beta=3.577)  # changes the cached islands and speeds too
     if model == "single":
         eos_a, eos_b, phase, kw = hyp.Barton2009(), new, 0, {}
     else:
@@ -410,6 +411,6 @@ def test_set_eos_between_steps(hyp, orc, model, precision):
         Q_fresh = s.download()
     if precision == "fp64":
         assert t_fresh == t_switch and np.array_equal(Q_fresh, Q_switch)
-    else:
-        assert abs(t_fresh - t_switch) <= 1e-12 * t_fresh
-        assert_close_soa(Q_switch, Q_fresh, 1e-9, "set_eos vs fresh context")
+    else:  # dt from an FP32 max speed: a re-split state may move it by an ulp
+        assert abs(t_fresh - t_switch) <= 1e-6 * t_fresh
+        assert_close_soa(Q_switch, Q_fresh, 1e-6, "set_eos vs fresh context")
