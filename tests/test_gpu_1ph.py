@@ -375,7 +375,9 @@ def test_set_eos_between_steps(hyp, orc, model, precision):
     changed and 20 more steps, equal a fresh context with the new EOS continued from
     the 20-step state (FP64 bitwise; mixed to the rounding of re-splitting the state
     into hi/lo pairs; stale cached speeds or islands would differ by far more).
-    Setting the same EOS again leaves the run unchanged, bitwise."""
+    Setting the same EOS again leaves the run unchanged: bitwise, except that the
+    single-phase mixed step's cached speeds and islands are then recomputed by the
+    upload's kernel, which agrees with the step's own to rounding."""
     Q0 = c1_state(hyp, orc, nx=600)[0]
     new = hyp.Barton2009(_rho0=9.0, _b0=2.3, _beta=3.577)  # changes the cached islands and speeds too
     if model == "single":
@@ -394,9 +396,11 @@ def test_set_eos_between_steps(hyp, orc, model, precision):
         s.set_eos(new, phase=phase)
         _, t_switch = s.step(max_steps=20)
         Q_switch = s.download()
-        s.upload(Q0)
+        orig = eos_a[phase] if model == "multi" else eos_a
+        s.upload(Q0)  # the EOS set last stays in force across uploads: restore the original
+        s.set_eos(orig, phase=phase)
         s.step(max_steps=20)
-        s.set_eos(eos_a[phase] if model == "multi" else eos_a, phase=phase)  # the same parameters again
+        s.set_eos(orig, phase=phase)  # the same parameters again
         s.step(max_steps=20)
         Q_same = s.download()
         with pytest.raises(hyp._lib.HypError):
@@ -404,7 +408,10 @@ def test_set_eos_between_steps(hyp, orc, model, precision):
     with hyp.Solver(eos_a, 600, precision=precision, **kw) as s:
         s.upload(Q0)
         s.step(max_steps=40)
-        assert np.array_equal(s.download(), Q_same)
+        if precision == "fp64" or model == "multi":
+            assert np.array_equal(s.download(), Q_same)
+        else:  # the single-phase mixed caches are recomputed by the upload's kernel, to rounding
+            assert_close_soa(s.download(), Q_same, 1e-6, "same EOS set again")
     with hyp.Solver(eos_b, 600, precision=precision, **kw) as s:
         s.upload(Q20, t0=t20)
         _, t_fresh = s.step(max_steps=20)
