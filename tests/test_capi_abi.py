@@ -61,3 +61,10 @@ def test_invalid_arguments_rejected_before_any_device_work(hyp):
     cfg = hyp._model.config(hyp.Barton2009(), 5, n_cells=100)  # bad model
     assert L.hyp_create(cfg, ctypes.byref(h)) == hyp._lib.HYP_ERR_INVALID
     assert L.hyp_create(None, ctypes.byref(h)) == hyp._lib.HYP_ERR_INVALID
+    # calls on a missing context are refused before any device work
+    n, t = ctypes.c_int(0), ctypes.c_double(0.0)
+    hist = (ctypes.c_double * 4)()
+    b = hyp.Barton2009().c()
+    assert L.hyp_set_eos(None, 0, ctypes.byref(b)) == hyp._lib.HYP_ERR_INVALID
+    assert L.hyp_step_times(None, 4, float("inf"), ctypes.byref(n), ctypes.byref(t), hist) == hyp._lib.HYP_ERR_INVALID
+    assert L.hyp_step(None, 4, float("inf"), ctypes.byref(n), ctypes.byref(t)) == hyp._lib.HYP_ERR_INVALID
