@@ -114,6 +114,34 @@ def main():
                           "energy": f(e_int), "invariants": [f(x) for x in inv],
                           "pressure": f(L.hank_pressure(h, mp.mpf(den), e_int, inv)),
                           "stress": [f(x) for x in L.hank_stress(h, mp.mpf(den), mp.mpf(pres), Fm)]})
+    # the alternative Barton2009 parameters of main.jl:133 (non-integer beta, gamma: the
+    # general powers), from their own generator so the entries above keep their inputs
+    alt = [8.93, 6.22, 9.0e-4, 300, 3.16, 1, 3.577, 2.088]
+    ea = L.Barton(*alt)
+    ra = np.random.default_rng(20261204)
+    g["nondefault"] = {"eos": alt, "tensors": [], "cells": []}
+    for k in range(4):
+        F = np.eye(3) + 0.06 * ra.standard_normal((3, 3))
+        if np.linalg.det(F) <= 0:
+            F = np.eye(3)
+        Fv = [float(x) for x in F.reshape(-1, order="F")]
+        S = float(ra.uniform(0, 1.5e-3))
+        Fm = [mp.mpf(x) for x in Fv]
+        G = L.finger(Fm)
+        ac = L.acoustic(ea, mp.mpf(S), Fm)
+        g["nondefault"]["tensors"].append({
+            "F": Fv, "S": S, "energy": f(L.energy(ea, mp.mpf(S), G)),
+            "stress": [f(x) for x in L.stress(ea, mp.mpf(S), Fm)],
+            "acoustic": [f(x) for x in ac], "moduli": [float(x) for x in L.eig_moduli(ac)]})
+    for k in range(3):
+        F = np.eye(3) + 0.05 * ra.standard_normal((3, 3))
+        u = ra.uniform(-1, 1, 3)
+        S = float(ra.uniform(0, 1e-3))
+        P = [1.0, 8.93 / np.linalg.det(F), *u, S, *F.reshape(-1, order="F")]
+        Q = L.prim2cons(ea, [mp.mpf(float(x)) for x in P])
+        g["nondefault"]["cells"].append({
+            "P": [float(x) for x in P], "Q": [f(x) for x in Q],
+            "flux": [f(x) for x in L.flux(ea, Q)], "speeds": [float(x) for x in L.speeds(ea, Q)]})
     with open(OUT, "w") as fh:
         json.dump(g, fh, indent=1)
     print("wrote", OUT)

@@ -100,6 +100,29 @@ def test_golden_cells(orc, golden):
         assert abs(np.max(np.abs(s)) - np.max(np.abs(c["speeds"]))) < 1e-14 * np.max(np.abs(c["speeds"]))
 
 
+def test_golden_nondefault_exponents(orc, golden):
+    """main.jl:133's alternative Barton2009 parameters (beta = 3.577, gamma = 2.088: the
+    general powers through exp/log) against the 40-digit transliteration."""
+    nd = golden["nondefault"]
+    e = orc.barton2009(*nd["eos"])
+    for t in nd["tensors"]:
+        F = np.array(t["F"])
+        G = orc.finger(F)
+        assert rel_err(orc.energy(e, t["S"], G), t["energy"]) < 1e-12
+        assert rel_err(orc.stress(e, t["S"], F), t["stress"]) < 1e-13
+        assert rel_err(orc.acoustic(e, t["S"], F), t["acoustic"]) < 1e-13
+        got = np.sort(orc.eig3_moduli(np.array(t["acoustic"])))[::-1]
+        assert abs(got[0] - t["moduli"][0]) <= 1e-14 * t["moduli"][0]
+    pb = orc.problem(eos=(e, e))
+    for c in nd["cells"]:
+        Q = orc.prim2cons(pb, np.array(c["P"])[1:])
+        assert rel_err(Q, c["Q"][1:]) < 1e-14
+        Qg = np.array(c["Q"][1:])
+        assert rel_err(orc.flux(pb, Qg), c["flux"][1:]) < 1e-13
+        s = orc.speeds(pb, Qg)
+        assert abs(np.max(np.abs(s)) - np.max(np.abs(c["speeds"]))) < 1e-14 * np.max(np.abs(c["speeds"]))
+
+
 def test_golden_twophase_noncons_and_hll(orc, golden):
     eos = (orc.barton2009(), orc.barton2009(b0=golden["eos2_b0"]))
     pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, eos=eos)
