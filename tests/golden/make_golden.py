@@ -142,6 +142,18 @@ def main():
         g["nondefault"]["cells"].append({
             "P": [float(x) for x in P], "Q": [f(x) for x in Q],
             "flux": [f(x) for x in L.flux(ea, Q)], "speeds": [float(x) for x in L.speeds(ea, Q)]})
+    # a two-phase HLL face (test case 6 states) with phase 1 on the alternative parameters
+    eosa = (ea, e2)
+    Qla = [mp.mpf(float(x)) for x in L.prim2cons(ea, [mp.mpf(float(x)) for x in Pl[:15]])
+           + L.prim2cons(e2, [mp.mpf(float(x)) for x in Pl[15:]])]
+    Qra = [mp.mpf(float(x)) for x in L.prim2cons(ea, [mp.mpf(float(x)) for x in Pr[:15]])
+           + L.prim2cons(e2, [mp.mpf(float(x)) for x in Pr[15:]])]
+    sL = L.speeds(ea, Qla[:15]) + L.speeds(e2, Qla[15:])
+    sR = L.speeds(ea, Qra[:15]) + L.speeds(e2, Qra[15:])
+    dm, dp = L.hll(eosa, Qla, Qra, sL, sR)
+    g["nondefault"]["hll"] = {"Ql": [float(x) for x in Qla], "Qr": [float(x) for x in Qra],
+                              "spdL": [float(x) for x in sL], "spdR": [float(x) for x in sR],
+                              "dm": [f(x) for x in dm], "dp": [f(x) for x in dp]}
     with open(OUT, "w") as fh:
         json.dump(g, fh, indent=1)
     print("wrote", OUT)

@@ -134,6 +134,18 @@ def test_golden_twophase_noncons_and_hll(orc, golden):
         assert rel_err(dp, h["dp"]) < 1e-12
 
 
+def test_golden_twophase_hll_nondefault_exponents(orc, golden):
+    """The two-phase HLL face with phase 1 on main.jl:133's alternative parameters."""
+    nd = golden["nondefault"]
+    h = nd["hll"]
+    eos = (orc.barton2009(*nd["eos"]), orc.barton2009(b0=golden["eos2_b0"]))
+    pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, eos=eos)
+    assert rel_err(np.sort(orc.speeds(pb, np.array(h["Ql"]))), np.sort(h["spdL"])) < 1e-13  # HLL takes min / max
+    dm, dp = orc.hll(pb, np.array(h["Ql"]), np.array(h["Qr"]), np.array(h["spdL"]), np.array(h["spdR"]))
+    assert rel_err(dm, h["dm"]) < 1e-12
+    assert rel_err(dp, h["dp"]) < 1e-12
+
+
 def test_golden_twophase_lxf(orc, golden):
     """The two-phase LxF face (NumFluxes.jl:25-60): flux and D+- = half the
     Gauss-Lobatto path integral, against the 40-digit transliteration."""
