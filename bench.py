@@ -312,8 +312,55 @@ def run_ours(args):
     if not args.no_cpu:
         v, sample = cpu_sample(Q0, args.cpu_seconds, os.cpu_count())
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": os.cpu_count(), "kind": "port", "sample": sample}
+    if WORLD == 1 and not args.no_workloads:
+        line["workloads"] = workload_summaries(args)
     print(json.dumps(line))
     return 0
+
+
+def emit(line, args):
+    """Print a workload's line (standalone run), or hand it back to the default run."""
+    if getattr(args, "nested", False):
+        return line
+    print(json.dumps(line))
+    return 0
+
+
+def nested_args(args, workload):
+    """The arguments of one of the other workloads at its own default size and steps,
+    for its summary inside the default line."""
+    a = argparse.Namespace(**vars(args))
+    a.nested = True
+    a.workload = workload
+    a.steps = DEFAULT_STEPS[workload]
+    a.n_cells = DEFAULT_CELLS[workload]
+    a.warmup = max(3, args.warmup if workload != "adjoint" else 1)
+    a.flux = "hll"
+    return a
+
+
+def workload_summaries(args):
+    """Compact results of the batch (4096 problems x 500 steps), two-phase (2^22 cells x
+    300 HLL steps) and adjoint (65,536 cells x 1000 steps) workloads."""
+    out = {}
+    b = run_batch(nested_args(args, "batch"))
+    out["batch"] = {"workload": b["config"]["workload"], "value": b["value"], "unit": b["unit"],
+                    "ms_per_step": b["ms_per_step"], "hbm_frac": b["roofline"]["frac"],
+                    "fp64_value": b["fp64_batch"]["value"], "mixed_over_fp64": b["value"] / b["fp64_batch"]["value"],
+                    "density_l1_max_vs_fp64": b["density_error_vs_fp64_per_problem"]["l1_max"],
+                    "clocks": b["clocks"]}
+    m = run_mph(nested_args(args, "mph"))
+    out["mph"] = {"workload": m["config"]["workload"], "value": m["value"], "unit": m["unit"],
+                  "ms_per_step": m["ms_per_step"], "hbm_frac": m["roofline"]["frac"], "fp64_value": m["fp64"]["value"],
+                  "mixed_over_fp64": m["fp64"]["mixed_over_fp64"],
+                  "density_l1_vs_fp64_per_phase": [e["l1"] for e in m["density_error_vs_fp64_per_phase"]],
+                  "clocks": m["clocks"]}
+    a = run_adjoint(nested_args(args, "adjoint"))
+    out["adjoint"] = {"workload": a["config"]["workload"], "adjoint_over_forward": a["adjoint_over_forward"],
+                      "adjoint_over_forward_dense_seed": a["dense_seed"]["adjoint_over_forward"],
+                      "ms_forward": a["ms"]["forward"], "ms_reverse": a["ms"]["recompute"] + a["ms"]["adjoint"],
+                      "fd_max_rel": a["fd_check"]["max_rel"], "clocks": a["clocks"]}
+    return out
 
 
 def run_batch(args):
@@ -370,8 +417,7 @@ def run_batch(args):
             "fp64_batch": {"value": total * K / (ms64 / 1e3), "ms_per_step": ms64 / K},
             "density_error_vs_fp64_per_problem": {"l1_max": float(l1.max()), "l1_median": float(np.median(l1)),
                                                   "linf_max": float(linf.max())}}
-    print(json.dumps(line))
-    return 0
+    return emit(line, args)
 
 
 def phase_densities(Q, rho0=8.93):
@@ -437,8 +483,7 @@ def run_mph(args):
                                              "update": tm64["ms_update"] / max(1, tm64["n_update"])},
                      "mixed_over_fp64": tm64["ms_total"] / tm["ms_total"]},
             "density_error_vs_fp64_per_phase": errs}
-    print(json.dumps(line))
-    return 0
+    return emit(line, args)
 
 
 def run_adjoint(args):
@@ -498,8 +543,7 @@ def run_adjoint(args):
             "loss": L,
             "fd_check": {"max_rel": float(rel.max()), "per_param": {PARAM_NAMES[k]: float(rel[k]) for k in range(15)},
                          "step_rel": 1e-6}}
-    print(json.dumps(line))
-    return 0
+    return emit(line, args)
 
 
 def run_evaluators(args):
@@ -580,6 +624,10 @@ def run_evaluators(args):
     return 0
 
 
+DEFAULT_STEPS = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000, "evaluators": 3}
+DEFAULT_CELLS = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536, "evaluators": 1 << 20}
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -593,6 +641,8 @@ def main():
     ap.add_argument("--no-fp64", action="store_true", help="skip the FP64 comparison run")
     ap.add_argument("--cpu-seconds", type=float, default=12.0)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-workloads", action="store_true",
+                    help="single workload: skip the batch / two-phase / adjoint summaries in its line")
     ap.add_argument("--workload", choices=["single", "batch", "mph", "adjoint", "evaluators"], default="single",
                     help="single: the headline single-phase step; batch: 4096 ragged problems; mph: two-phase HLL; "
                          "adjoint: gradient of a 1000-step run; evaluators: the function-level API")
@@ -602,13 +652,11 @@ def main():
     args = ap.parse_args()
     if args.warmup < 1:
         ap.error("--warmup must be >= 1")
-    steps = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000, "evaluators": 3}
-    cells = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536, "evaluators": 1 << 20}
     wl = "single" if args.impl == "reference" else args.workload
     if args.steps is None:
-        args.steps = steps[wl]
+        args.steps = DEFAULT_STEPS[wl]
     if args.n_cells is None:
-        args.n_cells = cells[wl]
+        args.n_cells = DEFAULT_CELLS[wl]
     if args.impl == "reference":
         return run_reference(args)
     runner = {"batch": run_batch, "adjoint": run_adjoint, "mph": run_mph,

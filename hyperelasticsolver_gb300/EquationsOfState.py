@@ -6,6 +6,7 @@ with the same device code as the solver step.
 import numpy as np
 
 from . import _lib as L
+from . import _model as M
 
 
 class Barton2009:
@@ -90,19 +91,50 @@ def entropy(eos, e_int, G):
 
 
 def stress(eos, *args):
-    """Cauchy stress: stress(eos::Barton2009, ent, F) = -2 rho G dE/dG, rho = rho0/det F
-    (EquationsOfState.jl:179-190), or stress(eos::Hank2016, den, pressure, distortion)
-    = -2 den G dE/dG with G = finger(inv(F)) (EquationsOfState.jl:354-361); column-major."""
+    """Cauchy stress, column-major 9-vector (or (n, 9)), by the reference's methods:
+    stress(eos::Barton2009, ent, F) = -2 rho G dE/dG, rho = rho0/det F
+    (EquationsOfState.jl:179-190); stress(eos::Barton2009, den, e_int, F), the entropy from
+    e_int and den as given (EquationsOfState.jl:162-176); stress(eos::Hank2016, den,
+    pressure, distortion) = -2 den G dE/dG with G = finger(inv(F)) (EquationsOfState.jl:354-361)."""
     if isinstance(eos, Hank2016):
         den, pres, F = args
         return _eval_hank("hyp_eval_hank2016_stress", eos, den, pres, F, 9, 9)
+    if len(args) == 3:
+        den, e_int, F = args
+        m, n, single = L.soa(F, 9)
+        den, e_int = _scalar_vec(den, n), _scalar_vec(e_int, n)
+        out = np.empty((9, n))
+        L.check(L.load().hyp_eval_stress_den(eos.c(), L.ptr(den), L.ptr(e_int), L.ptr(m), L.ptr(out), n),
+                what="hyp_eval_stress_den")
+        return L.unsoa(out, single)
     ent, F = args
     return _eval("hyp_eval_stress", eos, ent, F, 9)
 
 
-def acoustic(eos, ent, F, n=(1, 0, 0)):
-    """Acoustic tensor along n = e1 (EquationsOfState.jl:223-246) as a 3x3 matrix (or (n,3,3))."""
-    if tuple(np.asarray(n).tolist()) != (1, 0, 0):
-        raise NotImplementedError("the x-split solver evaluates the acoustic tensor along n = [1, 0, 0] only")
-    r = _eval("hyp_eval_acoustic", eos, ent, F, 9)
+def _mat3(r):
     return r.reshape(3, 3, order="F") if r.ndim == 1 else r.reshape(-1, 3, 3).transpose(0, 2, 1)
+
+
+def acoustic(eos, *args):
+    """Acoustic tensor as a 3x3 matrix (or (m, 3, 3)), by the reference's methods:
+    acoustic(eos, ent, F, n=[1,0,0]) (EquationsOfState.jl:223-246), the entropy held;
+    acoustic(eos, P, n) with P one phase's primitives [alpha, rho, u(3), S, A(9)]
+    (EquationsOfState.jl:192-221), the internal energy and alpha*rho held. n: one
+    direction (3,) or one per item (m, 3)."""
+    if len(args) == 2 and np.asarray(args[0]).shape[-1:] == (15,) and np.asarray(args[1]).shape[-1:] == (3,):
+        P, n_dir = args
+        p, n, single = L.soa(P, 15)
+        out = np.empty((9, n))
+        L.check(L.load().hyp_eval_acoustic_prim(eos.c(), L.ptr(p), L.ptr(M.dirs(n_dir, n)), L.ptr(out), n),
+                what="hyp_eval_acoustic_prim")
+        return _mat3(L.unsoa(out, single))
+    ent, F = args[0], args[1]
+    n_dir = args[2] if len(args) > 2 else (1, 0, 0)
+    if M.is_e1(n_dir):
+        return _mat3(_eval("hyp_eval_acoustic", eos, ent, F, 9))
+    m, n, single = L.soa(F, 9)
+    ent = _scalar_vec(ent, n)
+    out = np.empty((9, n))
+    L.check(L.load().hyp_eval_acoustic_dir(eos.c(), L.ptr(ent), L.ptr(m), L.ptr(M.dirs(n_dir, n)), L.ptr(out), n),
+            what="hyp_eval_acoustic_dir")
+    return _mat3(L.unsoa(out, single))

@@ -44,7 +44,7 @@ def flux(eos, Q):
 
 
 def get_eigvals(eos, Q, n=(1, 0, 0)):
-    """u1 +- sqrt|eig(acoustic)| (HyperelasticityMPh.jl:258-266), 6 speeds."""
-    if tuple(np.asarray(n).tolist()) != (1, 0, 0):
-        raise NotImplementedError("the x-split solver evaluates wave speeds along n = [1, 0, 0] only")
-    return M.call("hyp_eval_eigvals", _cfg(eos), Q, 14, 6)
+    """u.n + sqrt|mu_k| then u.n - sqrt|mu_k| (HyperelasticityMPh.jl:258-266), 6 speeds, mu_k
+    the eigenvalues of acoustic(eos, S, A, n) in Julia's eigvals order (ascending real
+    part). n: one direction (3,) or one per state (m, 3)."""
+    return M.eigvals_call(_cfg(eos), Q, 14, 6, n)

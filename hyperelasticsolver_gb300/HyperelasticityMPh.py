@@ -28,10 +28,10 @@ def flux_mph(eos, Q):
 
 
 def get_eigvals(eos, Q, n=(1, 0, 0)):
-    """Wave speeds u1 +- sqrt|eig(acoustic)| of both phases, n = e1 (HyperelasticityMPh.jl:252-266)."""
-    if tuple(np.asarray(n).tolist()) != (1, 0, 0):
-        raise NotImplementedError("the x-split solver evaluates wave speeds along n = [1, 0, 0] only")
-    return M.call("hyp_eval_eigvals", _cfg(eos), Q, 30, 12)
+    """Wave speeds u.n +- sqrt|eig(acoustic)| of both phases (HyperelasticityMPh.jl:252-266):
+    per phase the three u.n + c_k, then the three u.n - c_k, in Julia's eigvals order
+    (ascending real part of the eigenvalue). n: one direction (3,) or one per state."""
+    return M.eigvals_call(_cfg(eos), Q, 30, 12, n)
 
 
 def noncons_flux(eos, Q):

@@ -8,13 +8,23 @@ from . import _model as M
 def hll(eos, Q_l, Q_r, eigvals=None):
     """Two-phase path-conservative HLL (NumFluxes.jl:70-132): returns (zeros(30), D-, D+).
 
-    The wave-speed bounds come from Q_l and Q_r, as main.jl:225 passes the eigenvalues of
-    the two cells; `eigvals` is accepted for signature compatibility and not used."""
+    eigvals = [eig_l, eig_r], each 12 speeds (or (n, 12)): s_l = min(0, min speed of the
+    face midpoint, minimum(eig_l)) and s_r = max(0, max speed of the midpoint,
+    maximum(eig_r)) (NumFluxes.jl:90-91), as the reference uses them. main.jl:225 passes
+    the two cells' own get_eigvals; eigvals=None computes exactly those."""
     cfg = M.config(eos, L.HYP_MODEL_MULTI, flux=L.HYP_FLUX_HLL)
     l, n, single = L.soa(Q_l, 30)
     r, _, _ = L.soa(Q_r, 30)
     dm, dp = np.empty((30, n)), np.empty((30, n))
-    L.check(L.load().hyp_eval_hll(cfg, L.ptr(l), L.ptr(r), L.ptr(dm), L.ptr(dp), n), what="hll")
+    if eigvals is None:
+        L.check(L.load().hyp_eval_hll(cfg, L.ptr(l), L.ptr(r), L.ptr(dm), L.ptr(dp), n), what="hll")
+    else:
+        el, n_l, _ = L.soa(eigvals[0], 12)
+        er, n_r, _ = L.soa(eigvals[1], 12)
+        if n_l != n or n_r != n:
+            raise ValueError("eigvals must hold 12 speeds per face for each side")
+        L.check(L.load().hyp_eval_hll_eigvals(cfg, L.ptr(l), L.ptr(r), L.ptr(el), L.ptr(er), L.ptr(dm), L.ptr(dp), n),
+                what="hll")
     zero = np.zeros(30) if single else np.zeros((n, 30))
     return zero, L.unsoa(dm, single), L.unsoa(dp, single)
 

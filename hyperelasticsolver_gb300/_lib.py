@@ -96,6 +96,12 @@ _SIGS = {
     "hyp_set_wait_limit": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "hyp_step_noalloc_f64": ([ctypes.POINTER(ConfigC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_double, ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "hyp_set_slab": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int], ctypes.c_int),
+    "hyp_slab_local_max": ([ctypes.c_void_p, _dp], ctypes.c_int),
+    "hyp_slab_step": ([ctypes.c_void_p, ctypes.c_double, _dp], ctypes.c_int),
+    "hyp_cell_record_size": ([ctypes.c_void_p, ctypes.POINTER(ctypes.c_int)], ctypes.c_int),
+    "hyp_get_cells": ([ctypes.c_void_p, _i64, _i64, ctypes.c_void_p], ctypes.c_int),
+    "hyp_set_cells": ([ctypes.c_void_p, _i64, _i64, ctypes.c_void_p], ctypes.c_int),
     "hyp_batch_create": ([ctypes.POINTER(ConfigC), ctypes.POINTER(ctypes.c_int64), ctypes.c_int,
                           ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "hyp_batch_destroy": ([ctypes.c_void_p], ctypes.c_int),
@@ -127,6 +133,9 @@ _SIGS = {
     "hyp_eval_entropy": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_stress": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_acoustic": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_acoustic_dir": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_stress_den": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_acoustic_prim": ([ctypes.POINTER(Barton2009C), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_hank2016_energy": ([ctypes.POINTER(Hank2016C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_hank2016_pressure": ([ctypes.POINTER(Hank2016C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_hank2016_stress": ([ctypes.POINTER(Hank2016C), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
@@ -135,9 +144,11 @@ _SIGS = {
     "hyp_eval_prim2cons_vjp": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_flux": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_eigvals": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_eigvals_dir": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_lxf": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_noncons": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_eval_hll": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_hll_eigvals": ([ctypes.POINTER(ConfigC), _dp, _dp, _dp, _dp, _dp, _dp, _i64], ctypes.c_int),
 }
 
 _lib = None

@@ -25,3 +25,26 @@ def call(fname, cfg, X, k_in, k_out):
     out = np.empty((k_out, n))
     L.check(getattr(L.load(), fname)(cfg, L.ptr(x), L.ptr(out), n), what=fname)
     return L.unsoa(out, single)
+
+
+def dirs(d, n):
+    """Directions as SoA [3][n] from one 3-vector or an (n, 3) array."""
+    d = np.asarray(d, dtype=np.float64)
+    d = np.broadcast_to(d.reshape(1, 3), (n, 3)) if d.size == 3 else d.reshape(n, 3)
+    return np.ascontiguousarray(d.T)
+
+
+def is_e1(d):
+    d = np.asarray(d, dtype=np.float64)
+    return d.size == 3 and bool(np.all(d.reshape(3) == (1.0, 0.0, 0.0)))
+
+
+def eigvals_call(cfg, Q, nv, ns, n_dir):
+    """get_eigvals over states Q along n_dir (one 3-vector or one per state)."""
+    if is_e1(n_dir):
+        return call("hyp_eval_eigvals", cfg, Q, nv, ns)
+    q, n, single = L.soa(Q, nv)
+    out = np.empty((ns, n))
+    L.check(L.load().hyp_eval_eigvals_dir(cfg, L.ptr(q), L.ptr(dirs(n_dir, n)), L.ptr(out), n),
+            what="hyp_eval_eigvals_dir")
+    return L.unsoa(out, single)

@@ -353,6 +353,8 @@ static MixedArrays batch_arrays(hyp_batch* b, int p) {
   a.isl_out = b->isl[1 - p];
   a.stride = b->mpitch;
   a.n = b->total;
+  a.own_lo = 0;
+  a.own_hi = b->total;
   return a;
 }
 

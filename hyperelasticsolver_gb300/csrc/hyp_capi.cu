@@ -65,6 +65,9 @@ static int free_ctx(hyp_ctx* c) {
     if (e) cudaEventDestroy(e);
   for (auto& e : c->prof_ev) cudaEventDestroy(e);
   if (c->stream) cudaStreamDestroy(c->stream);
+  if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
+  for (auto& e : c->row_ev)
+    if (e) cudaEventDestroy(e);
   delete c;
   return HYP_OK;
 }
@@ -102,6 +105,11 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
   if ((e = cudaGetDevice(&c->device)) != cudaSuccess) fail(e, "cudaGetDevice");
   if (rc == HYP_OK && (e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess)
     fail(e, "cudaStreamCreate");
+  if (rc == HYP_OK && (e = cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking)) != cudaSuccess)
+    fail(e, "cudaStreamCreate");
+  for (auto& ev : c->row_ev)
+    if (rc == HYP_OK && (e = cudaEventCreateWithFlags(&ev, cudaEventDisableTiming)) != cudaSuccess)
+      fail(e, "cudaEventCreate");
   const size_t nq = (size_t)c->nvar * c->n * sizeof(double);
   c->eos2.e[0] = c->eos[0];
   c->eos2.e[1] = c->eos[1];
@@ -209,15 +217,20 @@ static int check_cell_error(hyp_ctx* c) {
 // the FP64 buffer of parity 0, or the mixed contexts' staging block.
 double* ctx_install_target(hyp_ctx* c) { return mixed(c) ? (double*)c->Qh[1] : c->Q[0]; }
 
-// Makes the FP64 state at ctx_install_target the current state at time t0 (splits
-// it into (hi, lo) pairs for mixed precision) and resets the loop control.
-int ctx_finish_install(hyp_ctx* c, double t0) {
+// Makes the FP64 state at src (null: ctx_install_target) the current state at time
+// t0 (splits it into (hi, lo) pairs for mixed precision; for the single-phase mixed
+// step, in the same pass, each cell's wave speed and islands) and resets the loop
+// control.
+int ctx_finish_install_from(hyp_ctx* c, const double* src, double t0) {
   std::memset(c->st_host, 0, sizeof(DevState));
   c->st_host->t[0] = c->st_host->t[1] = t0;
   CK(cudaMemcpyAsync(c->st, c->st_host, sizeof(DevState), cudaMemcpyHostToDevice, c->stream));
   if (mixed(c)) {
-    CK(launch_split(c, ctx_install_target(c), c->Qh[0], c->Ql[0]));
-    if (mixed1(c)) CK(launch_lam1_mixed(c, 0, &c->st->lam_slots[0]));
+    const double* q = src ? src : ctx_install_target(c);
+    if (mixed1(c))
+      CK(launch_install1_mixed(c, q, &c->st->lam_slots[0]));
+    else
+      CK(launch_split(c, q, c->Qh[0], c->Ql[0]));
   }
   int rc = sync_state(c);
   if (rc != HYP_OK) return rc;
@@ -229,10 +242,28 @@ int ctx_finish_install(hyp_ctx* c, double t0) {
   return check_cell_error(c);
 }
 
+int ctx_finish_install(hyp_ctx* c, double t0) { return ctx_finish_install_from(c, nullptr, t0); }
+
+// Device address of page-locked host memory (cudaHostAlloc / cudaHostRegister), or
+// null for memory the device does not map (pageable, or not host memory).
+static const double* mapped_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    (void)cudaGetLastError();
+    return nullptr;
+  }
+  return a.type == cudaMemoryTypeHost ? (const double*)a.devicePointer : nullptr;
+}
+
 extern "C" int hyp_upload(hyp_ctx* c, const double* Q, int64_t n_cells, int n_vars, double t0) {
   if (!c || !Q) return HYP_ERR_INVALID;
   if (n_cells != c->n || n_vars != c->nvar) return set_err(c, HYP_ERR_INVALID, "hyp_upload: size mismatch");
   CK(cudaSetDevice(c->device));
+  // Mixed precision from page-locked memory: the install kernel reads the host array
+  // in place (one pass over the host link, split and wave speeds included) instead of
+  // a copy into the staging block followed by a pass over it.
+  const double* mapped = mixed(c) ? mapped_host(Q) : nullptr;
+  if (mapped) return ctx_finish_install_from(c, mapped, t0);
   const size_t bytes = (size_t)n_vars * n_cells * sizeof(double);
   CK(cudaMemcpyAsync(ctx_install_target(c), Q, bytes, cudaMemcpyHostToDevice, c->stream));
   return ctx_finish_install(c, t0);
@@ -245,10 +276,25 @@ extern "C" int hyp_download(hyp_ctx* c, double* Q, int64_t n_cells, int n_vars) 
   const size_t bytes = (size_t)n_vars * n_cells * sizeof(double);
   if (!mixed(c)) {
     CK(cudaMemcpyAsync(Q, c->Q[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
-  } else {
+  } else if (bytes < ((size_t)64 << 20)) {
     double* stage = (double*)c->Qh[1 - c->cur];  // the other parity's block is free between steps
     CK(launch_join(c, c->Qh[c->cur], c->Ql[c->cur], stage));
     CK(cudaMemcpyAsync(Q, stage, bytes, cudaMemcpyDeviceToHost, c->stream));
+  } else {
+    // large states: join one variable row at a time on the context stream and copy each
+    // row out on the copy stream as soon as it is joined, so the joins hide behind the
+    // device-to-host copies
+    double* stage = (double*)c->Qh[1 - c->cur];
+    const size_t row = (size_t)n_cells * sizeof(double);
+    for (int v = 0; v < n_vars; ++v) {
+      CK(launch_join_n(c->stream, c->Qh[c->cur] + (size_t)v * c->mpitch, c->Ql[c->cur] + (size_t)v * c->mpitch,
+                       stage + (size_t)v * n_cells, 1, n_cells, c->mpitch));
+      CK(cudaEventRecord(c->row_ev[v], c->stream));
+      CK(cudaStreamWaitEvent(c->copy_stream, c->row_ev[v], 0));
+      CK(cudaMemcpyAsync(Q + (size_t)v * n_cells, stage + (size_t)v * n_cells, row, cudaMemcpyDeviceToHost,
+                         c->copy_stream));
+    }
+    CK(cudaStreamSynchronize(c->copy_stream));
   }
   CK(cudaStreamSynchronize(c->stream));
   return HYP_OK;
@@ -354,6 +400,7 @@ extern "C" int hyp_step(hyp_ctx* c, int max_steps, double t_end, int* steps_done
   CK(cudaSetDevice(c->device));
   const bool unlimited = max_steps <= 0;
   if (unlimited && std::isinf(t_end)) return set_err(c, HYP_ERR_INVALID, "hyp_step: neither max_steps nor t_end bounds the run");
+  if (c->slab) return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_step: a slab steps with the global max (hyp_slab_step)");
   c->timing = StepTiming();
   c->prof_used = 0;
   const long long steps0 = c->steps_host;

@@ -86,6 +86,26 @@ __global__ void k_acoustic(EosC e, const double* S, const double* F, double* out
   acoustic_SF(e, S[i], f, s);
   ST(out, s, 9);
 }
+__global__ void k_acoustic_dir(EosC e, const double* S, const double* F, const double* D, double* out, int64_t n) {
+  IDX double f[9], s[9], dir[3];
+  LD(f, F, 9);
+  LD(dir, D, 3);
+  acoustic_SFn(e, S[i], f, dir, s);
+  ST(out, s, 9);
+}
+__global__ void k_stress_den(EosC e, const double* den, const double* E, const double* F, double* out, int64_t n) {
+  IDX double f[9], s[9];
+  LD(f, F, 9);
+  stress_den_eF(e, den[i], E[i], f, s);
+  ST(out, s, 9);
+}
+__global__ void k_acoustic_prim(EosC e, const double* P, const double* D, double* out, int64_t n) {
+  IDX double p[15], s[9], dir[3];
+  LD(p, P, 15);
+  LD(dir, D, 3);
+  acoustic_Pn(e, p, dir, s);
+  ST(out, s, 9);
+}
 
 __device__ void phase_flux15(const EosC& e, const double* q, double* f) {
   Prim P;
@@ -95,19 +115,24 @@ __device__ void phase_flux15(const EosC& e, const double* q, double* f) {
   f[0] = 0.0;
   phase_flux(e, q[0], P, c, f + 1, s0);
 }
-__device__ void phase_eigvals(const EosC& e, const double* q, double* out6) {
+// get_eigvals for one phase (HyperelasticityMPh.jl:258-266) along direction n:
+// u.n + c_k then u.n - c_k, c_k = sqrt|mu_k| in the order of eig_sorted3 (the
+// order Julia's eigvals gives the reference).
+__device__ void phase_eigvals(const EosC& e, const double* q, const double* n, double* out6) {
   Prim P;
   cons_to_prim(e, q[0], q + 2, q[5], q + 6, P);
   StressC c = stress_coeffs(e, P.k, P.w, P.xm1);
-  double rho_s = e.rho0 * P.k.s, s0[3], s0r[3], om[9], m[3];
-  stress_row0(rho_s, P.k, c, s0);
-  for (int j = 0; j < 3; ++j) s0r[j] = s0[j] / rho_s;
-  acoustic_omega(e, P.k, P.w, c, P.xm1, s0r, om);
-  eig_moduli3(om, m);
+  const double rho_s = e.rho0 * P.k.s;
+  double sig[9], sn[3], om[9], m[3];
+  stress_full(rho_s, P.k, c, sig);
+  for (int k = 0; k < 3; ++k) sn[k] = (sig[k] * n[0] + sig[k + 3] * n[1] + sig[k + 6] * n[2]) / rho_s;
+  acoustic_omega_dir(e, P.k, P.w, c, P.xm1, false, false, sn, n, om);
+  eig_sorted3(om, m);
+  const double un = (P.u[0] * n[0] + P.u[1] * n[1]) + P.u[2] * n[2];  // dot(P[3:5], n)
   for (int k = 0; k < 3; ++k) {
-    double cs = sqrt(m[k]);
-    out6[k] = P.u[0] + cs;
-    out6[3 + k] = P.u[0] - cs;
+    const double cs = sqrt(m[k]);
+    out6[k] = un + cs;
+    out6[3 + k] = un - cs;
   }
 }
 
@@ -151,10 +176,12 @@ __global__ void k_flux(ModelArg m, const double* Q, double* F, int64_t n) {
   for (int ph = 0; ph < np; ++ph) phase_flux15(m.e[ph], q + 15 * ph, f + 15 * ph);
   store_cell(m, F, n, i, f);
 }
-__global__ void k_eigvals(ModelArg m, const double* Q, double* out, int64_t n) {
-  IDX double q[30], s[12];
+// D: directions [3][n], or null for n = e1 (the direction main.jl's step uses).
+__global__ void k_eigvals(ModelArg m, const double* Q, const double* D, double* out, int64_t n) {
+  IDX double q[30], s[12], dir[3] = {1.0, 0.0, 0.0};
+  if (D) LD(dir, D, 3);
   int np = load_cell(m, Q, n, i, q);
-  for (int ph = 0; ph < np; ++ph) phase_eigvals(m.e[ph], q + 15 * ph, s + 6 * ph);
+  for (int ph = 0; ph < np; ++ph) phase_eigvals(m.e[ph], q + 15 * ph, dir, s + 6 * ph);
   ST(out, s, 6 * np);
 }
 __global__ void k_lxf1(ModelArg m, const double* Ql, const double* Qr, const double* lam, double* cons, double* dm,
@@ -230,6 +257,36 @@ extern "C" int hyp_eval_acoustic(const hyp_barton2009* eos, const double* S, con
   return run(n, {{S, nullptr, 1}, {F, nullptr, 9}, {nullptr, ac, 9}},
              [](int64_t n, double** d, const void* a) {
                k_acoustic<<<grid(n), kBlock>>>(*(const EosC*)a, d[0], d[1], d[2], n);
+             },
+             &ec);
+}
+extern "C" int hyp_eval_acoustic_dir(const hyp_barton2009* eos, const double* S, const double* F, const double* dir,
+                                     double* ac, int64_t n) {
+  if (!eos) return HYP_ERR_INVALID;
+  EosC ec = eos_of(eos);
+  return run(n, {{S, nullptr, 1}, {F, nullptr, 9}, {dir, nullptr, 3}, {nullptr, ac, 9}},
+             [](int64_t n, double** d, const void* a) {
+               k_acoustic_dir<<<grid(n), kBlock>>>(*(const EosC*)a, d[0], d[1], d[2], d[3], n);
+             },
+             &ec);
+}
+extern "C" int hyp_eval_stress_den(const hyp_barton2009* eos, const double* den, const double* e_int, const double* F,
+                                   double* sigma, int64_t n) {
+  if (!eos) return HYP_ERR_INVALID;
+  EosC ec = eos_of(eos);
+  return run(n, {{den, nullptr, 1}, {e_int, nullptr, 1}, {F, nullptr, 9}, {nullptr, sigma, 9}},
+             [](int64_t n, double** d, const void* a) {
+               k_stress_den<<<grid(n), kBlock>>>(*(const EosC*)a, d[0], d[1], d[2], d[3], n);
+             },
+             &ec);
+}
+extern "C" int hyp_eval_acoustic_prim(const hyp_barton2009* eos, const double* P, const double* dir, double* ac,
+                                      int64_t n) {
+  if (!eos) return HYP_ERR_INVALID;
+  EosC ec = eos_of(eos);
+  return run(n, {{P, nullptr, 15}, {dir, nullptr, 3}, {nullptr, ac, 9}},
+             [](int64_t n, double** d, const void* a) {
+               k_acoustic_prim<<<grid(n), kBlock>>>(*(const EosC*)a, d[0], d[1], d[2], n);
              },
              &ec);
 }
@@ -325,7 +382,19 @@ extern "C" int hyp_eval_eigvals(const hyp_config* cfg, const double* Q, double* 
   int ns = cfg->model == HYP_MODEL_SINGLE ? 6 : 12;
   return run(n, {{Q, nullptr, k}, {nullptr, out, ns}},
              [](int64_t n, double** d, const void* a) {
-               k_eigvals<<<grid(n), kBlock>>>(*(const ModelArg*)a, d[0], d[1], n);
+               k_eigvals<<<grid(n), kBlock>>>(*(const ModelArg*)a, d[0], nullptr, d[1], n);
+             },
+             &m);
+}
+extern "C" int hyp_eval_eigvals_dir(const hyp_config* cfg, const double* Q, const double* dir, double* out,
+                                    int64_t n) {
+  if (!model_ok(cfg)) return HYP_ERR_INVALID;
+  ModelArg m = model_arg(cfg);
+  int k = nvar_of(cfg);
+  int ns = cfg->model == HYP_MODEL_SINGLE ? 6 : 12;
+  return run(n, {{Q, nullptr, k}, {dir, nullptr, 3}, {nullptr, out, ns}},
+             [](int64_t n, double** d, const void* a) {
+               k_eigvals<<<grid(n), kBlock>>>(*(const ModelArg*)a, d[0], d[1], d[2], n);
              },
              &m);
 }
@@ -383,15 +452,28 @@ struct HllArg {
   ModelArg m;
   Quad6D qd;
 };
-__global__ void k_hll(HllArg a, const double* Ql, const double* Qr, double* DMo, double* DPo, int64_t n) {
+// EL, ER: the caller's wave speeds of the left and right cell ([12][n] each, the
+// eigvals[1], eigvals[2] of NumFluxes.jl:90-91), or null for the cells' own.
+__global__ void k_hll(HllArg a, const double* Ql, const double* Qr, const double* EL, const double* ER, double* DMo,
+                      double* DPo, int64_t n) {
   IDX double ql[30], qr[30], fl[30], fr[30], dm[30], dp[30];
   LD(ql, Ql, 30);
   LD(qr, Qr, 30);
   flux2(a.m.e, ql, fl);
   flux2(a.m.e, qr, fr);
   double lo_l, hi_l, lo_r, hi_r;
-  speeds2(a.m.e, ql, lo_l, hi_l);
-  speeds2(a.m.e, qr, lo_r, hi_r);
+  if (EL) {  // minimum(eigvals[1]), maximum(eigvals[2])
+    lo_l = EL[i];
+    hi_r = ER[i];
+    for (int k = 1; k < 12; ++k) {
+      const double a_ = EL[(int64_t)k * n + i], b_ = ER[(int64_t)k * n + i];
+      lo_l = a_ < lo_l ? a_ : lo_l;
+      hi_r = b_ > hi_r ? b_ : hi_r;
+    }
+  } else {
+    speeds2(a.m.e, ql, lo_l, hi_l);
+    speeds2(a.m.e, qr, lo_r, hi_r);
+  }
   hll_face2(a.m.e, a.qd, ql, qr, fl, fr, lo_l, hi_r, dm, dp);
   ST(DMo, dm, 30);
   ST(DPo, dp, 30);
@@ -414,7 +496,20 @@ extern "C" int hyp_eval_hll(const hyp_config* cfg, const double* Ql, const doubl
   HllArg a{model_arg(cfg), gauss_legendre6()};
   return run(n, {{Ql, nullptr, 30}, {Qr, nullptr, 30}, {nullptr, dm, 30}, {nullptr, dp, 30}},
              [](int64_t n, double** d, const void* p) {
-               k_hll<<<(unsigned)((n + 63) / 64), 64>>>(*(const HllArg*)p, d[0], d[1], d[2], d[3], n);
+               k_hll<<<(unsigned)((n + 63) / 64), 64>>>(*(const HllArg*)p, d[0], d[1], nullptr, nullptr, d[2], d[3],
+                                                        n);
+             },
+             &a);
+}
+extern "C" int hyp_eval_hll_eigvals(const hyp_config* cfg, const double* Ql, const double* Qr, const double* eig_l,
+                                    const double* eig_r, double* dm, double* dp, int64_t n) {
+  if (!model_ok(cfg) || cfg->model != HYP_MODEL_MULTI) return HYP_ERR_INVALID;
+  HllArg a{model_arg(cfg), gauss_legendre6()};
+  return run(n,
+             {{Ql, nullptr, 30}, {Qr, nullptr, 30}, {eig_l, nullptr, 12}, {eig_r, nullptr, 12}, {nullptr, dm, 30},
+              {nullptr, dp, 30}},
+             [](int64_t n, double** d, const void* p) {
+               k_hll<<<(unsigned)((n + 63) / 64), 64>>>(*(const HllArg*)p, d[0], d[1], d[2], d[3], d[4], d[5], n);
              },
              &a);
 }

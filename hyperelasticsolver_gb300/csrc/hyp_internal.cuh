@@ -93,6 +93,16 @@ __device__ __forceinline__ StepScalars step_scalars(double cfl, double dx, doubl
   return s;
 }
 
+// Which end cells of a single-phase step are held (not updated). The step kernels
+// take the context's bc: HYP_BC_FROZEN holds both ends (main.jl:219-220),
+// HYP_BC_TRANSMISSIVE neither; a slab of a decomposed domain (hyp_slab.cu) also
+// holds an end that is a ghost cell, whose value its neighbour supplies:
+// kBcHoldFirst / kBcHoldLast hold only the first / last cell.
+constexpr int kBcHoldFirst = 2, kBcHoldLast = 3;
+__host__ __device__ __forceinline__ bool bc_holds(int bc, bool first, bool last) {
+  return (first && (bc == HYP_BC_FROZEN || bc == kBcHoldFirst)) || (last && (bc == HYP_BC_FROZEN || bc == kBcHoldLast));
+}
+
 // The two phases' EOS, passed to the two-phase kernels by value.
 struct Eos2 {
   EosC e[2];
@@ -123,6 +133,8 @@ struct hyp_ctx {
   int nvar = 14;
   int64_t n = 0;
   cudaStream_t stream = nullptr;
+  cudaStream_t copy_stream = nullptr;  // downloads: device-to-host copies overlapping the next rows' join
+  cudaEvent_t row_ev[30] = {};         // one per variable row of a pipelined download
   // FP64 state, double-buffered: Q[p] is the state before a step of parity p.
   double* Q[2] = {nullptr, nullptr};
   double* F = nullptr;     // per-cell fluxes (scratch)
@@ -178,6 +190,11 @@ struct hyp_ctx {
   double graph_t_end = 0.0;
   std::string err;
   int64_t err_cell = -1;
+  // one slab of a decomposed domain (hyp_slab.cu): ghost ends, the global dx
+  int slab = 0;
+  int slab_ghost[2] = {0, 0};  // the first / last cell is a ghost
+  double slab_dx = 0.0;
+  long long slab_cell_pass = -1;  // FP64: the step whose cell pass (fluxes, speeds) is done
   hyp::AdjTape* tape = nullptr;  // checkpoints and buffers of the adjoint (hyp_adjoint.cu)
   hyp::SnapBuf* snap = nullptr;  // snapshot buffers and writer (hyp_snapshot.cu)
 };
@@ -192,6 +209,13 @@ int ctx_check_cell_error(hyp_ctx* c);
 // to ctx_install_target(c), then call ctx_finish_install(c, t0).
 double* ctx_install_target(hyp_ctx* c);
 int ctx_finish_install(hyp_ctx* c, double t0);
+// The same from an FP64 state [nvar][n] at src: device memory, or host memory the
+// device maps (mixed contexts read it in place, so the host link is the only transfer).
+int ctx_finish_install_from(hyp_ctx* c, const double* src, double t0);
+// The step's dx and kernel bc value of a context: the configuration's, or a slab's
+// (its global dx and held ghost ends).
+double ctx_dx(const hyp_ctx* c);
+int ctx_bc(const hyp_ctx* c);
 
 namespace hyp {
 // adjoint buffers of a context (hyp_adjoint.cu)
@@ -224,6 +248,7 @@ cudaError_t launch_update2_mixed(hyp_ctx* c, int p, double t_end);
 int setup_mixed_tma(hyp_ctx* c);
 cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q);
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot);
+cudaError_t launch_install1_mixed(hyp_ctx* c, const double* q, unsigned long long* slot);
 cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end);
 // two-phase FP64 launchers (hyp_step2.cu)
 cudaError_t launch_cell2_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);

@@ -28,6 +28,7 @@ struct MixedArrays {
   float* isl_out;
   int64_t stride;   // floats between rows (a multiple of 4)
   int64_t n;        // cells
+  int64_t own_lo, own_hi;  // cells whose new wave speed enters the step's max (a slab's ghosts do not)
 };
 
 // One cell's inputs to a tile.
@@ -151,7 +152,7 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
   float lnew = 0.0f;
   const bool own = j > 0 && j < BLOCK - 1 && i < hi;
   if (own) {
-    const bool frozen = bc == HYP_BC_FROZEN && (i == lo || i == hi - 1);
+    const bool frozen = bc_holds(bc, i == lo, i == hi - 1);
     Islands I = c.I0;
     if (frozen) {
       lnew = c.li;
@@ -193,15 +194,8 @@ __device__ __forceinline__ float mixed_tile(const MixedArrays& a, const EosMixed
 }
 
 // Wave speed and island outputs of one cell of a freshly uploaded state.
-__device__ __forceinline__ float mixed_cell_lambda(const MixedArrays& a, const EosMixed& em, int64_t i, DevState* S,
-                                                   float* lam_out, float* isl_out) {
-  const int64_t n = a.stride;
-  float qh[14], ql[14];
-#pragma unroll
-  for (int v = 0; v < 14; ++v) {
-    qh[v] = a.Qh[v * n + i];
-    ql[v] = a.Ql[v * n + i];
-  }
+__device__ __forceinline__ float mixed_cell_lambda_of(const EosMixed& em, const float* qh, const float* ql, int64_t i,
+                                                      int64_t n, DevState* S, float* lam_out, float* isl_out) {
   PrimM P;
   Islands I;
   int st = prim_mixed(em, qh, ql, P, I);
@@ -214,6 +208,17 @@ __device__ __forceinline__ float mixed_cell_lambda(const MixedArrays& a, const E
   isl_out[n + i] = I.e_int;
   isl_out[2 * n + i] = I.sm1;
   return l;
+}
+__device__ __forceinline__ float mixed_cell_lambda(const MixedArrays& a, const EosMixed& em, int64_t i, DevState* S,
+                                                   float* lam_out, float* isl_out) {
+  const int64_t n = a.stride;
+  float qh[14], ql[14];
+#pragma unroll
+  for (int v = 0; v < 14; ++v) {
+    qh[v] = a.Qh[v * n + i];
+    ql[v] = a.Ql[v * n + i];
+  }
+  return mixed_cell_lambda_of(em, qh, ql, i, n, S, lam_out, isl_out);
 }
 
 }  // namespace hyp

@@ -10,8 +10,8 @@
 // caller passes the input and output state, and everything else the step
 // needs (the second state buffer of the ping-pong, per-cell fluxes and wave
 // speeds, loop control) lives in one fixed, file-scope device array of
-// kNoAllocDoubles doubles (65,536 cells at most; 13.6 MiB that every GPU which
-// loads this library keeps until the process exits).
+// kNoAllocDoubles doubles (65,536 cells at most; 13,631,552 bytes = 13.0 MiB that
+// every GPU which loads this library keeps until the process exits).
 //
 // Set-up: the first call on a device looks up that array's device address with
 // cudaGetSymbolAddress (with that device current) and caches it; make that
@@ -20,7 +20,13 @@
 // reset at the start of every call, the other scratch is fully overwritten
 // before it is read. Calls that overlap on the GPU (different streams, or
 // different host threads on the same device) race on the array and must be
-// serialised by the caller.
+// serialised by the caller. Each call waits for `stream` to finish before it
+// returns (it reads the final time and error word back to the host).
+//
+// Errors: a launch error that earlier, unrelated work left pending in the CUDA
+// runtime is cleared on entry (cudaGetLastError) so that it is not reported as
+// this call's; the reset kernel and the first step's two launches are checked one
+// by one, so a launch that fails stops the call before the rest are queued.
 #include <mutex>
 #include "hyp_internal.cuh"
 
@@ -84,6 +90,7 @@ extern "C" int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in,
   if (cfg->bc != HYP_BC_FROZEN && cfg->bc != HYP_BC_TRANSMISSIVE) return HYP_ERR_INVALID;
   if (!(cfg->cfl > 0) || !(cfg->x_length > 0) || !(cfg->eos[0].rho0 > 0) || !(cfg->eos[0].cv > 0))
     return HYP_ERR_INVALID;
+  (void)cudaGetLastError();  // a pending error from the caller's earlier work is not this call's
   double* base = nullptr;
   int rc = scratch_base(&base);
   if (rc != HYP_OK) return rc;
@@ -103,13 +110,16 @@ extern "C" int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in,
       cudaMemcpyAsync(cur, d_Q_in, (size_t)14 * n * sizeof(double), cudaMemcpyDeviceToDevice, s) != cudaSuccess)
     return HYP_ERR_CUDA;
   noalloc_reset_kernel<<<1, 1, 0, s>>>(st, t0);
+  if (cudaGetLastError() != cudaSuccess) return HYP_ERR_CUDA;
   for (int k = 0; k < n_steps; ++k) {
     const int p = k & 1;
     double* nxt = (cur == d_Q_out) ? B : d_Q_out;
     cell1_f64_kernel<<<grid, kBlock, 0, s>>>(cur, n, eos, F, lam, &st->lam_bits[p], &st->t[p], INFINITY, st);
+    if (k == 0 && cudaGetLastError() != cudaSuccess) return HYP_ERR_CUDA;
     update1_f64_kernel<<<grid, kBlock, 0, s>>>(cur, nxt, n, F, lam, &st->lam_bits[p], &st->lam_bits[1 - p],
                                                &st->t[p], &st->t[1 - p], &st->steps, INFINITY, cfg->cfl, dx,
                                                cfg->flux, cfg->bc);
+    if (k == 0 && cudaGetLastError() != cudaSuccess) return HYP_ERR_CUDA;
     cur = nxt;
   }
   if (cudaGetLastError() != cudaSuccess) return HYP_ERR_CUDA;

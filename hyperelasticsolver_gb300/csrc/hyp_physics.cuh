@@ -275,6 +275,59 @@ HYP_HD void acoustic_omega(const EosT<R>& e, const KinT<R>& k, const PowsT<R>& w
   }
 }
 
+// Acoustic tensor along a general direction n (EquationsOfState.jl:192-246),
+// column-major: Omega[i][j] = (1/rho_s) sum_m n_m d_j sigma[m,i], d_j the
+// derivative along dA = e_j (A^T n)^T, for which dG = -(g_j n^T + n g_j^T)
+// (g_j = G e_j), d i1 = -2 (Gn)_j, d i2 = -2 i1 (Gn)_j + 2 (Hn)_j,
+// d p = -2 p n_j and d rho_s = -rho_s n_j; n = e1 gives acoustic_omega.
+// hold_energy = false: the entropy is held (acoustic(eos, ent, F, n), :223-246)
+// and sn_over_rho = (sigma n)/rho_s carries the density's derivative.
+// hold_energy = true: the density and the internal energy are held and the
+// entropy follows G through entropy(e_int, G) (acoustic(eos, P, n), :192-221,
+// over stress(eos, den, e_int, F), :162-176); sn_over_rho is not read, and an
+// entropy argument at its 1e-6 clamp (xm1_clamped) does not move.
+template <class R>
+HYP_HD void acoustic_omega_dir(const EosT<R>& e, const KinT<R>& k, const PowsT<R>& w, const StressCT<R>& c, R xm1,
+                               bool hold_energy, bool xm1_clamped, const R* sn_over_rho, const R* n, R* om) {
+  R Gn[3], Hn[3];
+  for (int i = 0; i < 3; ++i) {
+    Gn[i] = sym_at(k.G, i, 0) * n[0] + sym_at(k.G, i, 1) * n[1] + sym_at(k.G, i, 2) * n[2];
+    Hn[i] = sym_at(k.H, i, 0) * n[0] + sym_at(k.H, i, 1) * n[1] + sym_at(k.H, i, 2) * n[2];
+  }
+  const R nGn = n[0] * Gn[0] + n[1] * Gn[1] + n[2] * Gn[2];
+  const R nn = n[0] * n[0] + n[1] * n[1] + n[2] * n[2];
+  const R bs6 = e.b0sq_6;
+  for (int j = 0; j < 3; ++j) {
+    const R dp = R(-2) * k.p * n[j];
+    const R di1 = R(-2) * Gn[j];
+    const R dpsi = (R(2) / R(3)) * k.i1 * Gn[j] - R(2) * Hn[j];
+    const R dPb = R(0.5) * e.beta * w.Pb1 * dp;
+    const R dPa = R(0.5) * e.alpha * w.Pa1 * dp;
+    const R dPa1 = (R(0.5) * e.alpha - R(1)) * w.Pa2 * dp;
+    const R dPg1 = (R(0.5) * e.gamma - R(1)) * w.Pg2 * dp;
+    const R dPb1 = (R(0.5) * e.beta - R(1)) * w.Pb2 * dp;
+    const R dcG = -bs6 * (dPb * k.i1 + w.Pb * di1);
+    const R dcGG = R(0.5) * e.b0sq * dPb;
+    R dxm1 = R(0);
+    if (hold_energy && !xm1_clamped) {
+      const R dPg = R(0.5) * e.gamma * w.Pg1 * dp;
+      const R dW = R(0.5) * e.b0sq * (dPb * k.psi + w.Pb * dpsi);
+      const R dUc = R(2) * e.kU * w.Pam1 * dPa;
+      dxm1 = -(dW + dUc) * e.inv_cvt0 * w.inv_Pg - xm1 * dPg * w.inv_Pg;
+    }
+    const R dE3 = e.kE3a * (dPa * w.Pa1 + w.Pam1 * dPa1) + e.kE3g * (dPg1 * xm1 + w.Pg1 * dxm1) +
+                  e.kE3b * (dPb1 * k.psi + w.Pb1 * dpsi);
+    const R dcI = dE3 * k.p + c.E3 * dp;
+    for (int i = 0; i < 3; ++i) {
+      const R Gij = sym_at(k.G, i, j), Hij = sym_at(k.H, i, j);
+      const R ndG = -(Gn[j] * n[i] + nn * Gij);
+      const R ndH = -(Gn[j] * Gn[i] + nn * Hij + Hn[j] * n[i] + nGn * Gij);
+      const R v = dcG * Gn[i] + c.cG * ndG + dcGG * Hn[i] + c.cGG * ndH + dcI * n[i];
+      om[i + 3 * j] = R(-2) * v - (hold_energy ? R(0) : n[j] * sn_over_rho[i]);
+    }
+  }
+}
+
 // Eigenvalue moduli of a real 3x3 (column-major). Characteristic polynomial
 // mu^3 - c2 mu^2 + c1 mu - c0; single-precision closed-form seeds
 // (trigonometric for three real roots, Cardano otherwise), three Newton steps
@@ -447,6 +500,51 @@ HYP_HD void eig_moduli3(const double* a, double* mods) {
   mods[0] = v[0]; mods[1] = v[1]; mods[2] = v[2];
 }
 
+// Moduli |mu_k| of the eigenvalues of a real 3x3 in the order Julia's `eigvals`
+// returns them (HyperelasticityMPh.jl:263): ascending real part, LinearAlgebra's
+// default lexicographic (real, imag) sort; the two members of a complex pair share
+// a modulus, so their order does not show. Jacobi rotations for a matrix symmetric
+// to rounding (accurate to a few ulps for every root), else the Newton-polished
+// real root and the deflated quadratic.
+HYP_HD void eig_sorted3(const double* a, double* mods) {
+  double re[3], md[3];
+  if (symmetric_to_rounding(a)) {
+    sym_eig_jacobi(a, re);
+    for (int k = 0; k < 3; ++k) md[k] = fabs(re[k]);
+  } else {
+    const CubicTop<double> t = cubic_top(a);
+    double s, qq;
+    if (t.r != 0.0) {
+      s = t.c2 - t.r;
+      qq = t.c0 / t.r;
+    } else {
+      s = t.c2;
+      qq = t.c1;
+    }
+    re[0] = t.r;
+    md[0] = fabs(t.r);
+    const double dsc = s * s - 4.0 * qq;
+    if (dsc < 0.0) {  // complex pair: real part s/2, modulus sqrt(qq)
+      re[1] = re[2] = 0.5 * s;
+      md[1] = md[2] = sqrt(fabs(qq));
+    } else {
+      const double sq = sqrt(dsc);
+      const double ra = s >= 0.0 ? 0.5 * (s + sq) : 0.5 * (s - sq);
+      const double rb = ra != 0.0 ? qq / ra : s - ra;
+      re[1] = ra;
+      re[2] = rb;
+      md[1] = fabs(ra);
+      md[2] = fabs(rb);
+    }
+  }
+  for (int i = 1; i < 3; ++i)
+    for (int j = i; j > 0 && re[j] < re[j - 1]; --j) {
+      double t = re[j]; re[j] = re[j - 1]; re[j - 1] = t;
+      t = md[j]; md[j] = md[j - 1]; md[j - 1] = t;
+    }
+  mods[0] = md[0]; mods[1] = md[1]; mods[2] = md[2];
+}
+
 // ---- per-cell, per-phase evaluation ---------------------------------------
 
 // Status bits a cell can raise (reported through the context's error word).
@@ -570,6 +668,41 @@ HYP_HD void acoustic_SF(const EosC& e, double S, const double* F, double* om) {
   stress_row0(rho_s, k, c, s0);
   for (int i = 0; i < 3; ++i) s0r[i] = s0[i] / rho_s;
   acoustic_omega(e, k, w, c, xm1, s0r, om);
+}
+// acoustic(eos, ent, F, n) (EquationsOfState.jl:223-246) for any direction n.
+HYP_HD void acoustic_SFn(const EosC& e, double S, const double* F, const double* n, double* om) {
+  Kin k = kinematics(F, det3(F));
+  Pows w = powers(e, k);
+  const double xm1 = exp(S / e.cv) - 1.0;
+  StressC c = stress_coeffs(e, k, w, xm1);
+  const double rho_s = e.rho0 * k.s;
+  double sig[9], sn[3];
+  stress_full(rho_s, k, c, sig);
+  for (int i = 0; i < 3; ++i) sn[i] = (sig[i] * n[0] + sig[i + 3] * n[1] + sig[i + 6] * n[2]) / rho_s;
+  acoustic_omega_dir(e, k, w, c, xm1, false, false, sn, n, om);
+}
+// stress(eos, den, e_int, F) (EquationsOfState.jl:162-176): the entropy from the
+// internal energy (entropy(e_int, finger(F)), clamped), sigma = -2 den G dE/dG at
+// that entropy, with den given rather than rho0 / det F.
+HYP_HD void stress_den_eF(const EosC& e, double den, double eint, const double* F, double* sig) {
+  Kin k = kinematics(F, det3(F));
+  Pows w = powers(e, k);
+  StressC c = stress_coeffs(e, k, w, entropy_xm1(e, eint, k, w));
+  stress_full(den, k, c, sig);
+}
+// acoustic(eos, P, n) (EquationsOfState.jl:192-221), P = [alpha, rho, u(3), S, A(9)]:
+// e_int = energy(eos, S, finger(A)), then the Jacobian of stress(eos, den, e_int, F)
+// over F at F = A with den = alpha rho held, divided by den.
+HYP_HD void acoustic_Pn(const EosC& e, const double* P, const double* n, double* om) {
+  const double* F = P + 6;
+  Kin k = kinematics(F, det3(F));
+  Pows w = powers(e, k);
+  const double eint = e_cold(e, w) + e.cvt0 * w.Pg * (exp(P[5] / e.cv) - 1.0) + e_shear(e, k, w);
+  const double raw = (eint - e_shear(e, k, w) - e_cold(e, w)) * e.inv_cvt0 * w.inv_Pg;
+  const bool clamped = raw + 1.0 < 1e-6;
+  const double xm1 = clamped ? 1e-6 - 1.0 : raw;
+  StressC c = stress_coeffs(e, k, w, xm1);
+  acoustic_omega_dir(e, k, w, c, xm1, true, clamped, (const double*)nullptr, n, om);
 }
 // Invariants of a general (not necessarily symmetric) G (Strains.jl:46-52).
 HYP_HD void invariants_general(const double* g, double* out) {

@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(kBlock) update1_f64_kernel(const double* __res
   }
   __syncthreads();
   if (i >= n) return;
-  const bool frozen = bc == HYP_BC_FROZEN && (i == 0 || i == n - 1);
+  const bool frozen = bc_holds(bc, i == 0, i == n - 1);
 #pragma unroll
   for (int v = 0; v < 14; ++v) {
     const double qc = Q[v * n + i];
@@ -114,10 +114,9 @@ cudaError_t launch_cell1_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, co
 }
 
 cudaError_t launch_update1_f64(hyp_ctx* c, int p, double t_end) {
-  const double dx = c->cfg.x_length / (double)c->n;
   update1_f64_kernel<<<grid_for(c->n), kBlock, 0, c->stream>>>(
       c->Q[p], c->Q[1 - p], c->n, c->F, c->lam, &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p],
-      &c->st->t[1 - p], &c->st->steps, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc);
+      &c->st->t[1 - p], &c->st->steps, t_end, c->cfg.cfl, ctx_dx(c), c->cfg.flux, ctx_bc(c));
   return cudaGetLastError();
 }
 

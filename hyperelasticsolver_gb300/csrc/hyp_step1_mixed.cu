@@ -61,7 +61,9 @@ __global__ void __launch_bounds__(kBlock, 4)
   mixed_tile_load(first, 0, a.n, ld, c);  // issued before the control reads below
   float dtdx;
   if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
-  const float l = mixed_tile_run<kBlock>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld, c);
+  float l = mixed_tile_run<kBlock>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld, c);
+  const int64_t i = first - 1 + threadIdx.x;
+  if (i < a.own_lo || i >= a.own_hi) l = 0.0f;  // a slab's ghost cells: their owner reports them
   const float m = mixed_block_max<kBlock>(l);
   if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
 }
@@ -182,6 +184,32 @@ __global__ void __launch_bounds__(kBlock) lam1_mixed_kernel(MixedArrays a, EosMi
   if (threadIdx.x == 0) atomicMax(slot, (unsigned long long)__float_as_uint(m));
 }
 
+// An uploaded single-phase state installed in one pass: each thread reads its
+// cell's 14 FP64 values (from device memory, or straight from page-locked host
+// memory that the device maps, so that the host link is the only transfer), splits
+// them into (hi, lo) pairs exactly as split_kernel does, and computes the cell's
+// wave speed and island outputs from those pairs exactly as lam1_mixed_kernel does
+// (max into `slot`). a: parity-0 arrays as outputs (Qh_out, Ql_out, lam_out, isl_out).
+__global__ void __launch_bounds__(kBlock) install1_mixed_kernel(const double* __restrict__ q, MixedArrays a,
+                                                                EosMixed em, unsigned long long* slot, DevState* S) {
+  const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
+  float l = 0.0f;
+  if (i < a.n) {
+    float qh[14], ql[14];
+#pragma unroll
+    for (int v = 0; v < 14; ++v) {
+      const double x = q[v * a.n + i];
+      qh[v] = (float)x;
+      ql[v] = (float)(x - (double)qh[v]);
+      a.Qh_out[v * a.stride + i] = qh[v];
+      a.Ql_out[v * a.stride + i] = ql[v];
+    }
+    l = mixed_cell_lambda_of(em, qh, ql, i, a.stride, S, a.lam_out, a.isl_out);
+  }
+  const float m = mixed_block_max<kBlock>(l);
+  if (threadIdx.x == 0) atomicMax(slot, (unsigned long long)__float_as_uint(m));
+}
+
 // FP64 [14][n] -> (hi, lo) rows of pitch `pitch`, and back.
 __global__ void split_kernel(const double* __restrict__ q, float* __restrict__ hi, float* __restrict__ lo, int64_t n,
                              int64_t pitch, int64_t m) {
@@ -235,7 +263,16 @@ static MixedArrays arrays_of(hyp_ctx* c, int p) {
   a.isl_out = c->isl[1 - p];
   a.stride = c->mpitch;
   a.n = c->n;
+  a.own_lo = c->slab && c->slab_ghost[0] ? 1 : 0;
+  a.own_hi = c->slab && c->slab_ghost[1] ? c->n - 1 : c->n;
   return a;
+}
+
+cudaError_t launch_install1_mixed(hyp_ctx* c, const double* q, unsigned long long* slot) {
+  const unsigned grid = (unsigned)((c->n + kBlock - 1) / kBlock);
+  MixedArrays a = arrays_of(c, 1);  // outputs: parity 0
+  install1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(q, a, c->eos_mixed, slot, c->st);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot) {
@@ -273,8 +310,8 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   sl.rd = (int)(k % 3);
   sl.wr = (int)((k + 1) % 3);
   sl.clr = (int)((k + 2) % 3);
-  const double dx = c->cfg.x_length / (double)c->n;
-  if (c->mixed_tma) {
+  const double dx = ctx_dx(c);
+  if (c->mixed_tma && !c->slab) {
     const int ntiles = (int)((c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2));
     step1_mixed_tma_kernel<kTmaBlock, kTmaMinB><<<c->tma_grid, kTmaBlock, TmaTile<kTmaBlock>::kSmem, c->stream>>>(
         c->tmap, arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc, ntiles,
@@ -282,7 +319,7 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   } else {
     const unsigned grid = (unsigned)((c->n + kTileM - 1) / kTileM);
     step1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl,
-                                                       dx, c->cfg.flux, c->cfg.bc);
+                                                       dx, c->cfg.flux, ctx_bc(c));
   }
   return cudaGetLastError();
 }

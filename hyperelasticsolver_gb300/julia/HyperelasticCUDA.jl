@@ -71,6 +71,30 @@ module EquationsOfState
       $k == 1 ? vec(out) : out
     end
   end
+  """acoustic(eos, ent, F, n) for one direction per cell (dir: (m, 3)) (EquationsOfState.jl:223-246)"""
+  function acoustic(eos::Barton2009C, s::Vector{Float64}, M::Matrix{Float64}, dir::Matrix{Float64})
+    out = Matrix{Float64}(undef, size(M, 1), 9)
+    check(ccall((:hyp_eval_acoustic_dir, libhyp), Cint,
+                (Ref{Barton2009C}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                Ref(eos), s, M, dir, out, size(M, 1)), "acoustic")
+    out
+  end
+  """stress(eos, den, e_int, F) (EquationsOfState.jl:162-176): the entropy from e_int, den as given"""
+  function stress(eos::Barton2009C, den::Vector{Float64}, e_int::Vector{Float64}, M::Matrix{Float64})
+    out = Matrix{Float64}(undef, size(M, 1), 9)
+    check(ccall((:hyp_eval_stress_den, libhyp), Cint,
+                (Ref{Barton2009C}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                Ref(eos), den, e_int, M, out, size(M, 1)), "stress")
+    out
+  end
+  """acoustic(eos, P, n) (EquationsOfState.jl:192-221): P one phase's primitives (m, 15), dir (m, 3)"""
+  function acoustic(eos::Barton2009C, P::Matrix{Float64}, dir::Matrix{Float64})
+    out = Matrix{Float64}(undef, size(P, 1), 9)
+    check(ccall((:hyp_eval_acoustic_prim, libhyp), Cint,
+                (Ref{Barton2009C}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64), Ref(eos), P, dir, out, size(P, 1)),
+          "acoustic")
+    out
+  end
 end
 
 module Hank
@@ -113,6 +137,13 @@ module HyperelasticityMPh
     B[:, 16:30, 16] .= bcol[:, 16:30]
     B
   end
+  "get_eigvals(eos, Q, n) along one direction per cell (dir: (m, 3)), 12 speeds per cell"
+  function get_eigvals(eos, Q::Matrix{Float64}, dir::Matrix{Float64})
+    out = Matrix{Float64}(undef, size(Q, 1), 12)
+    check(ccall((:hyp_eval_eigvals_dir, libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                Ref(config(eos, HYP_MODEL_MULTI)), Q, dir, out, size(Q, 1)), "get_eigvals")
+    out
+  end
 end
 
 module Hyperelasticity
@@ -127,6 +158,13 @@ module Hyperelasticity
                   cfg, Q, out, size(Q, 1)), $(string(jl)))
       out
     end
+  end
+  "get_eigvals(eos, Q, n) along one direction per cell (dir: (m, 3)), 6 speeds per cell"
+  function get_eigvals(eos::Barton2009C, Q::Matrix{Float64}, dir::Matrix{Float64})
+    out = Matrix{Float64}(undef, size(Q, 1), 6)
+    check(ccall((:hyp_eval_eigvals_dir, libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64),
+                Ref(config(eos, HYP_MODEL_SINGLE)), Q, dir, out, size(Q, 1)), "get_eigvals")
+    out
   end
   "prim2cons_vjp(eos, P, Qbar) -> (Pbar, (dL/db0sq, dL/dk0)): the pullback of prim2cons over n cells"
   function prim2cons_vjp(eos::Barton2009C, P::Matrix{Float64}, Qbar::Matrix{Float64})
@@ -152,14 +190,22 @@ module NumFluxes
     cons, dm, dp
   end
   """hll(eos, Q_l, Q_r, eigvals) for two-phase cells (n, 30) (NumFluxes.jl:70-132): (zeros, D-, D+).
-  The speed bounds come from Q_l and Q_r as main.jl:225 passes them; `eigvals` is not used."""
+  eigvals = (eig_l, eig_r), each (n, 12): s_l from minimum(eig_l), s_r from maximum(eig_r)
+  (NumFluxes.jl:90-91); `nothing` takes the two cells' own speeds, as main.jl:225 passes them."""
   function hll(eos::Tuple, Ql::Matrix{Float64}, Qr::Matrix{Float64}, eigvals=nothing)
     n = size(Ql, 1)
     dm, dp = similar(Ql), similar(Ql)
     cfg = Ref(config(eos, HYP_MODEL_MULTI; flux=HYP_FLUX_HLL))
-    check(ccall((:hyp_eval_hll, libhyp), Cint,
-                (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64), cfg, Ql, Qr, dm, dp, n),
-          "hll")
+    if eigvals === nothing
+      check(ccall((:hyp_eval_hll, libhyp), Cint,
+                  (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Int64), cfg, Ql, Qr, dm, dp, n),
+            "hll")
+    else
+      el, er = eigvals
+      check(ccall((:hyp_eval_hll_eigvals, libhyp), Cint,
+                  (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64}, Ptr{Float64},
+                   Int64), cfg, Ql, Qr, el, er, dm, dp, n), "hll")
+    end
     zeros(size(Ql)), dm, dp
   end
 end
@@ -264,11 +310,49 @@ initial_condition_tanh!(s::Solver, Ql::Vector{Float64}, Qr::Vector{Float64}, eps
   check(ccall((:hyp_init_tanh, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64), s.h, Ql, Qr, eps),
         "hyp_init_tanh", s.h)
 
+# ---- domain decomposition: one slab per rank (a ghost cell at each inner end) ----
+"""set_slab!(s, dx, left_ghost, right_ghost): make s one slab of a decomposed domain with
+the global dx; hyp_step then refuses it (a slab steps with the global max)"""
+set_slab!(s::Solver, dx::Float64, left_ghost::Bool, right_ghost::Bool) =
+  check(ccall((:hyp_set_slab, libhyp), Cint, (Ptr{Cvoid}, Float64, Cint, Cint), s.h, dx, left_ghost, right_ghost),
+        "hyp_set_slab", s.h)
+"slab_local_max(s): the max wave speed over the cells the slab owns"
+function slab_local_max(s::Solver)
+  v = Ref{Float64}(0.0)
+  check(ccall((:hyp_slab_local_max, libhyp), Cint, (Ptr{Cvoid}, Ref{Float64}), s.h, v), "hyp_slab_local_max", s.h)
+  v[]
+end
+"slab_step!(s, lam_max): one step with the global max (MPI.Allreduce of slab_local_max over the ranks); returns t"
+function slab_step!(s::Solver, lam_max::Float64)
+  t = Ref{Float64}(0.0)
+  check(ccall((:hyp_slab_step, libhyp), Cint, (Ptr{Cvoid}, Float64, Ref{Float64}), s.h, lam_max, t), "hyp_slab_step", s.h)
+  t[]
+end
+"cell_record_size(s): bytes per cell record (112 FP64, 128 mixed)"
+function cell_record_size(s::Solver)
+  b = Ref{Cint}(0)
+  check(ccall((:hyp_cell_record_size, libhyp), Cint, (Ptr{Cvoid}, Ref{Cint}), s.h, b), "hyp_cell_record_size", s.h)
+  Int(b[])
+end
+"get_cells!(s, first, rec): records of cells first .. first + size(rec, 1) - 1 (0-based) into rec (count, rows)"
+get_cells!(s::Solver, first::Integer, rec::AbstractMatrix) =
+  check(ccall((:hyp_get_cells, libhyp), Cint, (Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}), s.h, first, size(rec, 1), rec),
+        "hyp_get_cells", s.h)
+"set_cells!(s, first, rec): store records (a neighbour's boundary cells as this slab's ghosts)"
+set_cells!(s::Solver, first::Integer, rec::AbstractMatrix) =
+  check(ccall((:hyp_set_cells, libhyp), Cint, (Ptr{Cvoid}, Int64, Int64, Ptr{Cvoid}), s.h, first, size(rec, 1), rec),
+        "hyp_set_cells", s.h)
+
 # ---- caller-owned device memory and page-locked host memory ----
 """step_noalloc!(cfg, d_in, d_out, n_steps, t0; stream): single-phase FP64 steps on device
-buffers the caller owns (e.g. pointer(::CuArray)), allocating nothing; returns t"""
+buffers the caller owns (e.g. pointer(::CuArray)), allocating nothing; returns t.
+
+`stream` is required: pass the stream that wrote `d_in` (with CUDA.jl,
+`CUDA.stream().handle`). CUDA.jl queues its work on a task-local stream that need
+not order against the legacy default stream (C_NULL), so C_NULL is only safe after
+`CUDA.synchronize()`."""
 function step_noalloc!(cfg::ConfigC, d_in::Ptr{Float64}, d_out::Ptr{Float64}, n_steps::Integer, t0::Float64;
-                       stream::Ptr{Cvoid}=C_NULL)
+                       stream::Ptr{Cvoid})
   t, cell = Ref{Float64}(0.0), Ref{Int64}(-1)
   rc = ccall((:hyp_step_noalloc_f64, libhyp), Cint,
              (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64, Cint, Float64, Ptr{Cvoid}, Ref{Float64}, Ref{Int64}),

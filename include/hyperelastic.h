@@ -128,13 +128,16 @@ int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel
    device SoA states [14][n_cells] (may be the same buffer); cfg must be
    single-phase, FP64, Rusanov or LxF, with cfg->n_cells == n_cells. The step's
    scratch is one fixed static device array sized for at most 65,536 cells
-   (13.6 MiB per GPU that loads the library, held until exit); larger n_cells is
-   rejected with HYP_ERR_INVALID. The first call on a device looks up that array
-   (cudaGetSymbolAddress) and should come before any stream capture. Calls share
-   the array, so calls that overlap on the GPU race. Runs n_steps CFL steps from
-   time t0 on `stream` (a cudaStream_t, NULL = default stream), synchronises it,
-   and reports the new time; on HYP_ERR_NEG_DET / HYP_ERR_NONFINITE the first
-   failing cell is stored in *err_cell. */
+   (13,631,552 bytes = 13.0 MiB per GPU that loads the library, held until exit);
+   larger n_cells is rejected with HYP_ERR_INVALID. The first call on a device
+   looks up that array (cudaGetSymbolAddress) and should come before any stream
+   capture. Calls share the array, so calls that overlap on the GPU race. Runs
+   n_steps CFL steps from time t0 on `stream` (a cudaStream_t, NULL = the legacy
+   default stream: pass the stream that produced d_Q_in, or synchronise first),
+   waits for that stream to finish, and reports the new time; on HYP_ERR_NEG_DET /
+   HYP_ERR_NONFINITE the first failing cell is stored in *err_cell. A CUDA launch
+   error left pending by the caller's earlier work is cleared on entry, not
+   reported. */
 int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_Q_out, int64_t n_cells, int n_steps,
                          double t0, void* stream, double* t_out, int64_t* err_cell);
 
@@ -149,6 +152,36 @@ int hyp_set_mixed_kernel(hyp_ctx* ctx, int tma);
    state again). A budget of 0 makes every wait run out at once: the timeout path
    exercised without a fault. */
 int hyp_set_wait_limit(hyp_ctx* ctx, int tries);
+
+/* ---- domain decomposition: a context as one slab of a longer 1D domain ------ */
+/* The reference advances one domain with a thread pool over its cells (main.jl:206,
+   221). Split across processes (one GPU each), rank r's context holds the cells it
+   updates plus a ghost cell at each inner end (its neighbour's boundary cell), and
+   one step of main.jl:202-241 becomes: hyp_slab_local_max on every rank, a
+   max-allreduce of those values (the caller's communicator), hyp_slab_step with the
+   result, then the exchange of boundary cells (hyp_get_cells on the owner,
+   hyp_set_cells into the neighbour's ghost). The max is exact and every face sees the
+   cells it would see in one domain, so with the global dx the slabs step bitwise like
+   the single-domain run. Single-phase contexts (Rusanov or LxF, FP64 or mixed). */
+/* Make ctx a slab: dx of the global domain (X / global cells), whether its first and
+   last cells are ghosts (held by the step; the global ends keep cfg->bc). hyp_step
+   then refuses the context (a slab needs the global max). */
+int hyp_set_slab(hyp_ctx* ctx, double dx, int left_ghost, int right_ghost);
+/* Max wave speed over the cells the slab owns (ghosts excluded where their value is
+   stale) of the current state; FP64 runs the step's cell pass to get it. */
+int hyp_slab_local_max(hyp_ctx* ctx, double* lam);
+/* One step with the global max wave speed: dt = cfl dx / lam_max (main.jl:212),
+   t += dt, owned cells updated, ghosts held. Reports the new time. */
+int hyp_slab_step(hyp_ctx* ctx, double lam_max, double* t_out);
+/* Bytes per cell of a cell record: 112 (FP64: the 14 conservative values) or 128
+   (mixed: 14 hi, 14 lo FP32 parts, the cell's FP32 wave speed and its 3 island
+   outputs, so a ghost arrives with what its owner computed). */
+int hyp_cell_record_size(const hyp_ctx* ctx, int* bytes);
+/* Copy the records of cells [first, first + count) of the current state out to / in
+   from rec, laid out [row][count] (rows of 8-byte doubles or 4-byte floats as above);
+   rec may be host or device memory. */
+int hyp_get_cells(hyp_ctx* ctx, int64_t first, int64_t count, void* rec);
+int hyp_set_cells(hyp_ctx* ctx, int64_t first, int64_t count, const void* rec);
 
 /* ---- batches of independent single-phase problems -------------------------- */
 /* The reference advances one problem per main.jl run (main.jl:202-241). A batch
@@ -256,6 +289,20 @@ int hyp_eval_entropy(const hyp_barton2009* eos, const double* e, const double* G
 int hyp_eval_stress(const hyp_barton2009* eos, const double* S, const double* F, double* sigma, int64_t n);
 /* EquationsOfState.acoustic(eos, ent, F, [1,0,0]) (EquationsOfState.jl:223-246).  [9][n] */
 int hyp_eval_acoustic(const hyp_barton2009* eos, const double* S, const double* F, double* ac, int64_t n);
+/* EquationsOfState.acoustic(eos, ent, F, n) (EquationsOfState.jl:223-246) for a direction
+   n per item (dir: [3][n], not necessarily unit length, used as given).  ac: [9][n] */
+int hyp_eval_acoustic_dir(const hyp_barton2009* eos, const double* S, const double* F, const double* dir, double* ac,
+                          int64_t n);
+/* EquationsOfState.stress(eos, den, e_int, F) (EquationsOfState.jl:162-176): the entropy
+   from e_int (entropy(eos, e_int, finger(F)), clamped as :152-154), then
+   -2 den G dE/dG with den as given.  den, e_int: [n]; F, sigma: [9][n] */
+int hyp_eval_stress_den(const hyp_barton2009* eos, const double* den, const double* e_int, const double* F,
+                        double* sigma, int64_t n);
+/* EquationsOfState.acoustic(eos, P, n) (EquationsOfState.jl:192-221): P = one phase's
+   primitive 15-vector [alpha, rho, u(3), S, A(9)]; e_int = energy(eos, S, finger(A)),
+   then the Jacobian over F of stress(eos, alpha*rho, e_int, F) at F = A (the entropy
+   following F at fixed e_int), divided by alpha*rho.  P: [15][n]; dir: [3][n]; ac: [9][n] */
+int hyp_eval_acoustic_prim(const hyp_barton2009* eos, const double* P, const double* dir, double* ac, int64_t n);
 
 /* Hank2016 (EquationsOfState.jl:305-366), which the reference defines at function
    level only (its time step uses Barton2009). Defaults: rho0 2.7, mu 26e9, gamma 3.4,
@@ -285,9 +332,13 @@ int hyp_eval_prim2cons_vjp(const hyp_config* cfg, const double* P, const double*
 /* flux_mph / flux (HyperelasticityMPh.jl:140-175).  [nvar][n] */
 int hyp_eval_flux(const hyp_config* cfg, const double* Q, double* F, int64_t n);
 /* get_eigvals (HyperelasticityMPh.jl:252-266) with n = e1: per phase
-   u1 + c_k (k = 1..3) then u1 - c_k, c_k = sqrt|eig_k|, moduli in descending
-   order.  out: [6*phases][n] */
+   u1 + c_k (k = 1..3) then u1 - c_k, c_k = sqrt|mu_k|, mu_k the eigenvalues of the
+   acoustic tensor in the order Julia's eigvals returns them (HyperelasticityMPh.jl:263):
+   ascending real part (LinearAlgebra's default sort).  out: [6*phases][n] */
 int hyp_eval_eigvals(const hyp_config* cfg, const double* Q, double* out, int64_t n);
+/* get_eigvals(eos, Q, n) for a direction per item: u.n +- sqrt|mu_k| of
+   acoustic(eos, S, A, n), same order.  dir: [3][n]; out: [6*phases][n] */
+int hyp_eval_eigvals_dir(const hyp_config* cfg, const double* Q, const double* dir, double* out, int64_t n);
 /* NumFluxes.lxf(eos, Q_l, Q_r, lambda) (NumFluxes.jl:25-60): conservative part
    and the path-conservative D-, D+.  Ql, Qr, cons, dm, dp: [nvar][n]; lambda: [n] */
 int hyp_eval_lxf(const hyp_config* cfg, const double* Ql, const double* Qr, const double* lambda, double* cons,
@@ -301,6 +352,12 @@ int hyp_eval_noncons(const hyp_config* cfg, const double* Q, double* bcol, int64
    with the wave speeds of Q_l and Q_r as main.jl:225 passes them; the conservative
    part the reference returns is zeros(30).  Ql, Qr, dm, dp: [30][n] */
 int hyp_eval_hll(const hyp_config* cfg, const double* Ql, const double* Qr, double* dm, double* dp, int64_t n);
+/* NumFluxes.hll(eos, Q_l, Q_r, eigvals) (NumFluxes.jl:70-132) with the caller's
+   speeds, as the reference takes them: s_l = min(0, min speed of the face midpoint,
+   minimum(eig_l)), s_r = max(0, max speed of the midpoint, maximum(eig_r))
+   (NumFluxes.jl:90-91).  eig_l, eig_r: [12][n] (eigvals[1], eigvals[2]) */
+int hyp_eval_hll_eigvals(const hyp_config* cfg, const double* Ql, const double* Qr, const double* eig_l,
+                         const double* eig_r, double* dm, double* dp, int64_t n);
 
 #ifdef __cplusplus
 }

@@ -201,6 +201,50 @@ template <class T, class S, class PM> void acoustic(const BartonT<PM>& e, const 
     }
 }
 
+// EquationsOfState.jl:162-176  stress(eos, den, e_int, F): S = entropy(eos, e_int,
+// finger(F)), then -2 den G dE/dG at that entropy (the gradient over G with S held).
+template <class T, class U, class PM>
+void stress_den(const BartonT<PM>& e, const U& den, const U& e_int, const T* F, T* sig) {
+  T G[9], dedG[9], a[9];
+  finger(F, G);
+  T S = entropy(e, T(e_int), G);
+  denergy_dG(e, S, G, dedG);
+  for (int k = 0; k < 9; ++k) a[k] = (den * -2.0) * G[k];
+  matmul3(a, dedG, sig);
+}
+
+// EquationsOfState.jl:192-221  acoustic(eos, P, n), P = [alpha, rho, u(3), S, A(9)]:
+// den = P[1] P[2], e_int = energy(eos, S, finger(F)), the jacobian over F of
+// stress(eos, den, e_int, F) (den and e_int held, the entropy following F),
+// A = (1/den) dTdF, then the contraction of :207-218.
+inline void acoustic_prim(const Barton& e, const double* P, const double* n, double* ac) {
+  const double den = P[0] * P[1];
+  const double ent = P[5];
+  const double* F = P + 6;
+  double G0[9];
+  finger(F, G0);
+  const double e_int = energy(e, ent, G0);
+  using D = Dual<double, 9>;
+  D f[9], sd[9];
+  for (int k = 0; k < 9; ++k) {
+    f[k] = D(F[k]);
+    f[k].d[k] = 1.0;
+  }
+  stress_den(e, den, e_int, f, sd);
+  const double rden = 1.0 / den;
+  for (int i = 0; i < 3; ++i)
+    for (int j = 0; j < 3; ++j) {
+      double acc = 0.0;
+      for (int k = 0; k < 3; ++k)
+        for (int l = 0; l < 3; ++l)
+          for (int m = 0; m < 3; ++m) {
+            double A = rden * sd[m + 3 * i].d[j + 3 * l];
+            acc = acc + ((A * M3(F, k, l)) * n[m]) * n[k];
+          }
+      M3(ac, i, j) = acc;
+    }
+}
+
 // ---------------------------------------------------------------------------
 // EquationsOfState.jl:305-366  Hank2016: energy(eos, den, pres, G), pressure(eos,
 // den, e_int, i), stress(eos, den, pres, distortion) = -2 den G dE/dG with
@@ -373,6 +417,78 @@ template <class T> void eig3_moduli(const T* a, T* mods) {
   }
 }
 
+// The eigenvalues of a real 3x3 in the order Julia's `eigvals` returns them
+// (HyperelasticityMPh.jl:263): LinearAlgebra sorts them by default
+// lexicographically by (real, imag). Returned as moduli |mu| (what
+// sqrt.(abs.(eigvals(ac))) consumes). Roots: Jacobi for a matrix symmetric to
+// rounding (the symmetric path Julia's eigvals takes for an exactly symmetric
+// matrix), else the Newton-polished real root of the characteristic polynomial
+// and the two roots of the deflated quadratic (complex when its discriminant is
+// negative).
+inline void eig3_sorted(const double* a, double* mods) {
+  double re[3], im[3], md[3];
+  if (eig3_symmetric(a)) {
+    eig3_jacobi(a, re);
+    for (int k = 0; k < 3; ++k) {
+      im[k] = 0.0;
+      md[k] = std::fabs(re[k]);
+    }
+  } else {
+    const double c2 = (M3(a, 0, 0) + M3(a, 1, 1)) + M3(a, 2, 2);
+    const double c1 = ((M3(a, 0, 0) * M3(a, 1, 1) - M3(a, 0, 1) * M3(a, 1, 0)) +
+                       (M3(a, 0, 0) * M3(a, 2, 2) - M3(a, 0, 2) * M3(a, 2, 0))) +
+                      (M3(a, 1, 1) * M3(a, 2, 2) - M3(a, 1, 2) * M3(a, 2, 1));
+    const double c0 = det_(a);
+    const double p = c1 - c2 * c2 / 3.0;
+    const double q = -2.0 * c2 * c2 * c2 / 27.0 + c2 * c1 / 3.0 - c0;
+    const double disc = (q * 0.5) * (q * 0.5) + (p / 3.0) * (p / 3.0) * (p / 3.0);
+    double r;
+    if (disc < 0.0 && p < 0.0) {
+      const double m = 2.0 * std::sqrt(-p / 3.0);
+      const double th = std::acos(std::max(-1.0, std::min(1.0, 3.0 * q / (p * m)))) / 3.0;
+      r = 0.0;
+      for (int k = 0; k < 3; ++k) {
+        const double y = m * std::cos(th - 2.0 * M_PI * k / 3.0) + c2 / 3.0;
+        if (std::fabs(y) > std::fabs(r)) r = y;
+      }
+    } else {
+      const double sd = std::sqrt(std::max(disc, 0.0));
+      r = std::cbrt(-q * 0.5 + sd) + std::cbrt(-q * 0.5 - sd) + c2 / 3.0;
+    }
+    for (int it = 0; it < 50; ++it) {
+      const double f = ((r - c2) * r + c1) * r - c0;
+      const double fp = (3.0 * r - 2.0 * c2) * r + c1;
+      if (fp == 0.0) break;
+      const double dr = f / fp;
+      r -= dr;
+      if (std::fabs(dr) <= 1e-16 * std::fabs(r)) break;
+    }
+    const double sm = r != 0.0 ? c2 - r : c2, pr = r != 0.0 ? c0 / r : c1;
+    const double dsc = sm * sm - 4.0 * pr;
+    re[0] = r;
+    im[0] = 0.0;
+    md[0] = std::fabs(r);
+    if (dsc < 0.0) {
+      re[1] = re[2] = 0.5 * sm;
+      im[1] = -0.5 * std::sqrt(-dsc);
+      im[2] = -im[1];
+      md[1] = md[2] = std::sqrt(std::fabs(pr));
+    } else {
+      const double sq = std::sqrt(dsc);
+      const double ra = sm >= 0.0 ? 0.5 * (sm + sq) : 0.5 * (sm - sq);
+      const double rb = ra != 0.0 ? pr / ra : sm - ra;
+      re[1] = ra;
+      re[2] = rb;
+      im[1] = im[2] = 0.0;
+      md[1] = std::fabs(ra);
+      md[2] = std::fabs(rb);
+    }
+  }
+  int ord[3] = {0, 1, 2};
+  std::sort(ord, ord + 3, [&](int x, int y) { return re[x] < re[y] || (re[x] == re[y] && im[x] < im[y]); });
+  for (int k = 0; k < 3; ++k) mods[k] = md[ord[k]];
+}
+
 // ---------------------------------------------------------------------------
 // HyperelasticityMPh.jl:106-133  cons2prim for one phase.
 // Q[1] (alpha*rho) is never read: density comes from det(Q[7:15]/alpha).
@@ -446,15 +562,22 @@ template <class T, class PM> void flux(const BartonT<PM>& e, const T* Q, T* Fx) 
       Fx[6 + a + 3 * b] = den * (vel[0] * M3(A, a, b) - vel[a] * arow[b]);
 }
 
-// HyperelasticityMPh.jl:258-266  wave speeds u1 +- sqrt|eig(acoustic)| for one phase, n = e1.
-template <class T, class PM> void eigvals_phase(const BartonT<PM>& e, const T* Q, T* spd6) {
+// HyperelasticityMPh.jl:258-266  wave speeds u.n +- sqrt|eig(acoustic)| for one phase
+// (n = e1 on the step's path). In plain double the moduli come in Julia's eigvals
+// order (eig3_sorted); the dual-number runs consume only their min and max.
+template <class T, class PM> void eigvals_phase(const BartonT<PM>& e, const T* Q, T* spd6, const double* n = nullptr) {
+  static const double e1[3] = {1.0, 0.0, 0.0};
+  if (!n) n = e1;
   T P[15];
   cons2prim(e, Q, P);
-  const double n[3] = {1.0, 0.0, 0.0};
   T ac[9], mods[3];
   acoustic(e, P[5], P + 6, n, ac);
-  eig3_moduli(ac, mods);
-  T spd = ((T(0.0) + P[2] * 1.0) + P[3] * 0.0) + P[4] * 0.0;  // dot(P[3:5], n)
+  if constexpr (std::is_same<T, double>::value) {
+    eig3_sorted(ac, mods);
+  } else {
+    eig3_moduli(ac, mods);
+  }
+  T spd = ((T(0.0) + P[2] * n[0]) + P[3] * n[1]) + P[4] * n[2];  // dot(P[3:5], n)
   for (int k = 0; k < 3; ++k) {
     T c = sqrt(mods[k]);
     spd6[k] = spd + c;
@@ -618,14 +741,14 @@ template <class T, class PM> void cell_flux(const ProblemT<PM>& pb, const T* Q, 
   }
 }
 // get_eigvals (HyperelasticityMPh.jl:252-256): all phases' speeds.
-template <class T, class PM> void cell_speeds(const ProblemT<PM>& pb, const T* Q, T* spd) {
+template <class T, class PM> void cell_speeds(const ProblemT<PM>& pb, const T* Q, T* spd, const double* n = nullptr) {
   if (pb.model == MODEL_SINGLE) {
     T q15[15];
     expand1(Q, q15);
-    eigvals_phase(pb.eos[0], q15, spd);
+    eigvals_phase(pb.eos[0], q15, spd, n);
   } else {
-    eigvals_phase(pb.eos[0], Q, spd);
-    eigvals_phase(pb.eos[1], Q + 15, spd + 6);
+    eigvals_phase(pb.eos[0], Q, spd, n);
+    eigvals_phase(pb.eos[1], Q + 15, spd + 6, n);
   }
 }
 template <class T> T max_abs(const T* v, int n) {

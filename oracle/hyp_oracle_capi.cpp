@@ -95,6 +95,52 @@ int hyo_acoustic(const hyo_eos* eos, const double* S, const double* F, double* a
   }
   return 0;
 }
+// acoustic(eos, ent, F, n) with a direction per item (dir: [3][n]).
+int hyo_acoustic_dir(const hyo_eos* eos, const double* S, const double* F, const double* dir, double* ac, int64_t n) {
+  Barton b = to_barton(eos);
+  for (int64_t i = 0; i < n; ++i) {
+    double f[9], a[9], d[3];
+    GATHER(f, F, 9, n, i);
+    GATHER(d, dir, 3, n, i);
+    acoustic(b, S[i], f, d, a);
+    SCATTER(ac, a, 9, n, i);
+  }
+  return 0;
+}
+// stress(eos, den, e_int, F) (EquationsOfState.jl:162-176).
+int hyo_stress_den(const hyo_eos* eos, const double* den, const double* e_int, const double* F, double* sig,
+                   int64_t n) {
+  Barton b = to_barton(eos);
+  for (int64_t i = 0; i < n; ++i) {
+    double f[9], s[9];
+    GATHER(f, F, 9, n, i);
+    stress_den(b, den[i], e_int[i], f, s);
+    SCATTER(sig, s, 9, n, i);
+  }
+  return 0;
+}
+// acoustic(eos, P, n) (EquationsOfState.jl:192-221); P: [15][n].
+int hyo_acoustic_prim(const hyo_eos* eos, const double* P, const double* dir, double* ac, int64_t n) {
+  Barton b = to_barton(eos);
+  for (int64_t i = 0; i < n; ++i) {
+    double pp[15], a[9], d[3];
+    GATHER(pp, P, 15, n, i);
+    GATHER(d, dir, 3, n, i);
+    acoustic_prim(b, pp, d, a);
+    SCATTER(ac, a, 9, n, i);
+  }
+  return 0;
+}
+// Eigenvalue moduli in Julia's eigvals order (ascending real part).
+int hyo_eig3_sorted(const double* a, double* mods, int64_t n) {
+  for (int64_t i = 0; i < n; ++i) {
+    double m[9], r[3];
+    GATHER(m, a, 9, n, i);
+    eig3_sorted(m, r);
+    SCATTER(mods, r, 3, n, i);
+  }
+  return 0;
+}
 typedef struct { double rho0, mu, gamma, pres_inf, a; } hyo_hank;
 int hyo_hank_energy(const hyo_hank* p, const double* den, const double* pres, const double* G, double* e, int64_t n) {
   Hank2016 h{p->rho0, p->mu, p->gamma, p->pres_inf, p->a};
@@ -189,6 +235,19 @@ int hyo_speeds(const hyo_problem* p, const double* Q, double* spd, int64_t n) {
     double q[30], s[12];
     GATHER(q, Q, nv, n, i);
     cell_speeds(pb, q, s);
+    SCATTER(spd, s, ns, n, i);
+  }
+  return 0;
+}
+// get_eigvals(eos, Q, n) with a direction per item (dir: [3][n]).
+int hyo_speeds_dir(const hyo_problem* p, const double* Q, const double* dir, double* spd, int64_t n) {
+  Problem pb = to_problem(p);
+  int nv = nvar_of(pb.model), ns = nspd_of(pb.model);
+  for (int64_t i = 0; i < n; ++i) {
+    double q[30], s[12], d[3];
+    GATHER(q, Q, nv, n, i);
+    GATHER(d, dir, 3, n, i);
+    cell_speeds(pb, q, s, d);
     SCATTER(spd, s, ns, n, i);
   }
   return 0;

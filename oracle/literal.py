@@ -216,24 +216,61 @@ def stress(e, ent, F):  # :179-190
     return [_mm(a, dedG, i, j) for j in range(3) for i in range(3)]
 
 
-def acoustic(e, ent, F):  # :223-246, n = e1
+def acoustic(e, ent, F, n=(1, 0, 0)):  # :223-246
     sd = stress(e, ent, seed(F))
     den = e.rho0 / det_lu(F)
     ac = [None] * 9
     for i in range(3):
         for j in range(3):
-            ac[i + 3 * j] = sum(sd[0 + 3 * i].d[j + 3 * l] / den * mget(F, 0, l) for l in range(3))
+            ac[i + 3 * j] = sum(sd[m + 3 * i].d[j + 3 * l] / den * mget(F, k, l) * n[m] * n[k]
+                                for k in range(3) for l in range(3) for m in range(3) if n[m] != 0 and n[k] != 0)
+    return ac
+
+
+def stress_den(e, den, eint, F):  # :162-176, the entropy from e_int, den given
+    G = finger(F)
+    S = entropy(e, eint, G)
+    dedG = gradient(lambda g: energy(e, S, g), G)
+    a = [-2 * den * g for g in G]
+    return [_mm(a, dedG, i, j) for j in range(3) for i in range(3)]
+
+
+def acoustic_prim(e, P, n):  # :192-221
+    """acoustic(eos, P, n): the Jacobian of stress(eos, den, e_int, F) over F (den = P[1]
+    P[2] and e_int = energy(eos, S, finger(F)) held), here by central differences in
+    40-digit arithmetic (step 1e-15: truncation ~1e-30, cancellation ~1e-25), so this
+    check shares neither the dual numbers nor the closed forms of the other restatements."""
+    den = P[0] * P[1]
+    F = list(P[6:15])
+    eint = energy(e, P[5], finger(F))
+    h = mp.mpf("1e-15")
+    J = [[None] * 9 for _ in range(9)]  # J[p][q] = d sigma_p / d F_q
+    for q in range(9):
+        Fp, Fm = list(F), list(F)
+        Fp[q] += h
+        Fm[q] -= h
+        sp, sm = stress_den(e, den, eint, Fp), stress_den(e, den, eint, Fm)
+        for p_ in range(9):
+            J[p_][q] = (sp[p_] - sm[p_]) / (2 * h)
+    ac = [None] * 9
+    for i in range(3):
+        for j in range(3):
+            ac[i + 3 * j] = sum(J[m + 3 * i][j + 3 * l] / den * mget(F, k, l) * n[m] * n[k]
+                                for k in range(3) for l in range(3) for m in range(3))
     return ac
 
 
 def eig_moduli(M):
-    """All eigenvalue moduli of a real 3x3 (mpmath eig at 40 digits)."""
+    """Eigenvalue moduli of a real 3x3 (mpmath eig at 40 digits) in the order Julia's
+    eigvals returns the eigenvalues (HyperelasticityMPh.jl:263): LinearAlgebra's default
+    lexicographic sort by (real, imag)."""
     A = mp.matrix(3, 3)
     for i in range(3):
         for j in range(3):
             A[i, j] = val(mget(M, i, j))
     ev = mp.eig(A, left=False, right=False)
-    return sorted((abs(x) for x in ev), reverse=True)
+    ev = sorted(ev, key=lambda z: (mp.re(z), mp.im(z)))
+    return [abs(x) for x in ev]
 
 
 # --- HyperelasticityMPh.jl (one phase, 15-vector) ---
@@ -273,11 +310,12 @@ def flux(e, Q):  # :146-175
     return out
 
 
-def speeds(e, Q):  # :258-266 with n = e1
+def speeds(e, Q, n=(1, 0, 0)):  # :258-266
     P = cons2prim(e, Q)
-    mods = eig_moduli(acoustic(e, P[5], P[6:15]))
+    mods = eig_moduli(acoustic(e, P[5], P[6:15], n))
     c = [mp.sqrt(m) for m in mods]
-    return [P[2] + x for x in c] + [P[2] - x for x in c]
+    un = P[2] * n[0] + P[3] * n[1] + P[4] * n[2]
+    return [un + x for x in c] + [un - x for x in c]
 
 
 def noncons_cols(eos, Q):  # :178-250 (columns 1 and 16 of B)

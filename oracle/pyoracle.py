@@ -106,6 +106,11 @@ def lib():
             "hyo_stress": [ep, dp, dp, dp, i64],
             "hyo_acoustic": [ep, dp, dp, dp, i64],
             "hyo_eig3_moduli": [dp, dp, i64],
+            "hyo_eig3_sorted": [dp, dp, i64],
+            "hyo_acoustic_dir": [ep, dp, dp, dp, dp, i64],
+            "hyo_stress_den": [ep, dp, dp, dp, dp, i64],
+            "hyo_acoustic_prim": [ep, dp, dp, dp, i64],
+            "hyo_speeds_dir": [pp, dp, dp, dp, i64],
             "hyo_cons2prim": [pp, dp, dp, i64],
             "hyo_prim2cons": [pp, dp, dp, i64],
             "hyo_flux": [pp, dp, dp, i64],
@@ -195,12 +200,48 @@ def stress(eos, S, F):
     return _out(r, s)
 
 
-def acoustic(eos, S, F):
-    """Acoustic tensor for n = e1 (EquationsOfState.jl:223-246), column-major 9-vector."""
+def _dirs(d, n):
+    """Directions as SoA [3][n] from one 3-vector or an (n, 3) array."""
+    d = np.asarray(d, dtype=np.float64)
+    d = np.broadcast_to(d.reshape(-1, 3), (n, 3)) if d.size == 3 else d.reshape(n, 3)
+    return np.ascontiguousarray(d.T)
+
+
+def acoustic(eos, S, F, n_dir=None):
+    """Acoustic tensor (EquationsOfState.jl:223-246), column-major 9-vector; direction
+    n = e1 by default, else one 3-vector or one per item."""
     f, n, s = _soa(F, 9)
     S = _vec(S, n)
     r = np.empty((9, n))
-    lib().hyo_acoustic(ctypes.byref(eos), _ptr(S), _ptr(f), _ptr(r), n)
+    if n_dir is None:
+        lib().hyo_acoustic(ctypes.byref(eos), _ptr(S), _ptr(f), _ptr(r), n)
+    else:
+        lib().hyo_acoustic_dir(ctypes.byref(eos), _ptr(S), _ptr(f), _ptr(_dirs(n_dir, n)), _ptr(r), n)
+    return _out(r, s)
+
+
+def stress_den(eos, den, e_int, F):
+    """stress(eos, den, e_int, F) (EquationsOfState.jl:162-176)."""
+    f, n, s = _soa(F, 9)
+    den, e_int = _vec(den, n), _vec(e_int, n)
+    r = np.empty((9, n))
+    lib().hyo_stress_den(ctypes.byref(eos), _ptr(den), _ptr(e_int), _ptr(f), _ptr(r), n)
+    return _out(r, s)
+
+
+def acoustic_prim(eos, P, n_dir):
+    """acoustic(eos, P, n) (EquationsOfState.jl:192-221), P one phase's 15 primitives."""
+    p, n, s = _soa(P, 15)
+    r = np.empty((9, n))
+    lib().hyo_acoustic_prim(ctypes.byref(eos), _ptr(p), _ptr(_dirs(n_dir, n)), _ptr(r), n)
+    return _out(r, s)
+
+
+def eig3_sorted(M):
+    """Eigenvalue moduli in Julia's eigvals order (ascending real part)."""
+    m, n, s = _soa(M, 9)
+    r = np.empty((3, n))
+    lib().hyo_eig3_sorted(_ptr(m), _ptr(r), n)
     return _out(r, s)
 
 
@@ -236,8 +277,14 @@ def flux(pb, Q):
     return _model_call("hyo_flux", pb, Q, nvar(pb), nvar(pb))
 
 
-def speeds(pb, Q):
-    return _model_call("hyo_speeds", pb, Q, nvar(pb), 6 if pb.model == MODEL_SINGLE else 12)
+def speeds(pb, Q, n_dir=None):
+    """get_eigvals (HyperelasticityMPh.jl:252-266): n = e1 by default."""
+    if n_dir is None:
+        return _model_call("hyo_speeds", pb, Q, nvar(pb), 6 if pb.model == MODEL_SINGLE else 12)
+    q, n, s = _soa(Q, nvar(pb))
+    r = np.empty((6 if pb.model == MODEL_SINGLE else 12, n))
+    lib().hyo_speeds_dir(ctypes.byref(pb), _ptr(q), _ptr(_dirs(n_dir, n)), _ptr(r), n)
+    return _out(r, s)
 
 
 def noncons(pb, Q):

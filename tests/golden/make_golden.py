@@ -154,6 +154,51 @@ def main():
     g["nondefault"]["hll"] = {"Ql": [float(x) for x in Qla], "Qr": [float(x) for x in Qra],
                               "spdL": [float(x) for x in sL], "spdR": [float(x) for x in sR],
                               "dm": [f(x) for x in dm], "dp": [f(x) for x in dp]}
+    # function-level forms beside the step's path, from their own generator so the entries
+    # above keep their inputs: acoustic(eos, ent, F, n) for general n, stress(eos, den,
+    # e_int, F) (one state at the entropy clamp), acoustic(eos, P, n), get_eigvals along n,
+    # and an HLL face given speeds wider than its cells' own (NumFluxes.jl:90-91)
+    rx = np.random.default_rng(20261205)
+    x = {"acoustic_dir": [], "stress_den": [], "acoustic_prim": [], "speeds_dir": []}
+    for k in range(3):
+        F = np.eye(3) + 0.06 * rx.standard_normal((3, 3))
+        Fv = [float(v) for v in F.reshape(-1, order="F")]
+        S = float(rx.uniform(0, 1.5e-3))
+        nv = [float(v) for v in rx.standard_normal(3)]
+        ac = L.acoustic(e, mp.mpf(S), [mp.mpf(v) for v in Fv], [mp.mpf(v) for v in nv])
+        x["acoustic_dir"].append({"F": Fv, "S": S, "n": nv, "acoustic": [f(v) for v in ac]})
+    for k in range(3):
+        F = np.eye(3) + 0.06 * rx.standard_normal((3, 3))
+        Fv = [float(v) for v in F.reshape(-1, order="F")]
+        den = float(rx.uniform(8.5, 9.3))
+        Fm = [mp.mpf(v) for v in Fv]
+        eint = L.energy(e, mp.mpf(float(rx.uniform(0, 1e-3))), L.finger(Fm)) - (1 if k == 2 else 0)
+        eint = float(eint)
+        x["stress_den"].append({"F": Fv, "den": den, "e_int": eint,
+                                "stress": [f(v) for v in L.stress_den(e, mp.mpf(den), mp.mpf(eint), Fm)]})
+    for k in range(3):
+        F = np.eye(3) + 0.05 * rx.standard_normal((3, 3))
+        P = [float(rx.uniform(0.3, 1.0)), 8.93 / float(np.linalg.det(F)), *[float(v) for v in rx.uniform(-0.5, 0.5, 3)],
+             float(rx.uniform(0, 1e-3)), *[float(v) for v in F.reshape(-1, order="F")]]
+        nv = [1.0, 0.0, 0.0] if k == 0 else [float(v) for v in rx.standard_normal(3)]
+        ac = L.acoustic_prim(e, [mp.mpf(v) for v in P], [mp.mpf(v) for v in nv])
+        x["acoustic_prim"].append({"P": P, "n": nv, "acoustic": [f(v) for v in ac]})
+    for k in range(3):
+        F = np.eye(3) + 0.05 * rx.standard_normal((3, 3))
+        u = rx.uniform(-1, 1, 3)
+        S = float(rx.uniform(0, 1e-3))
+        P = [1.0, 8.93 / np.linalg.det(F), *u, S, *F.reshape(-1, order="F")]
+        Q = L.prim2cons(e, [mp.mpf(float(v)) for v in P])
+        Q = [mp.mpf(f(v)) for v in Q]
+        nv = [float(v) for v in rx.standard_normal(3)]
+        x["speeds_dir"].append({"Q": [float(v) for v in Q], "n": nv,
+                                "speeds": [f(v) for v in L.speeds(e, Q, [mp.mpf(v) for v in nv])]})
+    wl = [float(v) - 1.5 for v in spdL]
+    wr = [float(v) + 2.5 for v in spdR]
+    dmw, dpw = L.hll(eos, Ql, Qr, [mp.mpf(v) for v in wl], [mp.mpf(v) for v in wr])
+    x["hll_given"] = {"Ql": [float(v) for v in Ql], "Qr": [float(v) for v in Qr], "spdL": wl, "spdR": wr,
+                      "dm": [f(v) for v in dmw], "dp": [f(v) for v in dpw]}
+    g["extras"] = x
     with open(OUT, "w") as fh:
         json.dump(g, fh, indent=1)
     print("wrote", OUT)

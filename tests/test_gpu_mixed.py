@@ -184,3 +184,44 @@ def test_tma_wait_timeout_is_reported_and_recoverable(hyp, orc):
         Qb = t.download()
     scale = np.maximum(np.max(np.abs(Qb), axis=1, keepdims=True), 1e-30)
     assert np.max(np.abs(Qa - Qb) / scale) <= 1e-6
+
+
+@pytest.mark.parametrize("model", ["single", "multi"])
+@pytest.mark.parametrize("n", [1000, 1 << 22])
+def test_pinned_upload_and_pipelined_download_are_bitwise(hyp, orc, model, n):
+    """hyp_upload from page-locked memory (the install kernel reads the host array in place)
+    and from pageable memory (copied to the staging block first) install bitwise the same
+    state, wave speed and following steps; the row-pipelined download (large states) returns
+    bitwise what the one-pass download does."""
+    from hyperelasticsolver_gb300._lib import PinnedArray
+    from hyperelasticsolver_gb300 import Hyperelasticity as H, HyperelasticityMPh as HM
+    from hyperelasticsolver_gb300._cases import segment_states, segment_fill, mph_interface_prims
+    if model == "single":
+        eos = hyp.Barton2009()
+        Q0 = segment_fill(H.prim2cons(eos, segment_states(eos, 64)), n)
+    else:
+        eos = (hyp.Barton2009(), hyp.Barton2009(_b0=2.1 * np.sqrt(0.1)))
+        Q0 = np.ascontiguousarray(HM.prim2cons_mph(eos, mph_interface_prims(eos[0], n)).T)
+    pin = PinnedArray(Q0.shape)
+    pin.array[...] = Q0
+    out = {}
+    try:
+        for src in ("pageable", "pinned"):
+            with hyp.Solver(eos, n, model=model, flux="rusanov" if model == "single" else "hll",
+                            precision="mixed") as s:
+                s.upload(Q0 if src == "pageable" else pin.array)
+                lam = s.max_wavespeed()
+                first = s.download()
+                s.step(max_steps=5)
+                after = s.download()
+                again = s.download(pin.array if src == "pinned" else None)  # into page-locked memory too
+                out[src] = (lam, first, after, np.array(again))
+    finally:
+        pin.close()
+    a, b = out["pageable"], out["pinned"]
+    assert a[0] == b[0]
+    for x, y in zip(a[1:], b[1:]):
+        assert np.array_equal(x, y)
+    assert np.array_equal(a[2], a[3])
+    # the installed state is the uploaded one to the hi/lo pair's precision
+    assert np.max(np.abs(a[1] - Q0) / np.maximum(np.max(np.abs(Q0), axis=1, keepdims=True), 1e-300)) < 1e-13

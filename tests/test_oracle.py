@@ -83,8 +83,8 @@ def test_golden_tensor_functions(orc, golden):
         if np.max(np.abs(st)) > 1e-12:
             assert rel_err(orc.stress(e, t["S"], F), st) < 1e-13
         assert rel_err(orc.acoustic(e, t["S"], F), t["acoustic"]) < 1e-13
-        got = np.sort(orc.eig3_moduli(np.array(t["acoustic"])))[::-1]
-        assert abs(got[0] - t["moduli"][0]) <= 1e-14 * t["moduli"][0]
+        got = orc.eig3_sorted(np.array(t["acoustic"]))  # Julia's eigvals order, every modulus
+        assert np.max(np.abs(got - t["moduli"])) <= 1e-14 * np.max(t["moduli"])
 
 
 def test_golden_cells(orc, golden):
@@ -96,8 +96,8 @@ def test_golden_cells(orc, golden):
         Qg = np.array(c["Q"][1:])
         assert rel_err(orc.cons2prim(pb, Qg), c["prim"][1:]) < 1e-12
         assert rel_err(orc.flux(pb, Qg), c["flux"][1:]) < 1e-13
-        s = orc.speeds(pb, Qg)
-        assert abs(np.max(np.abs(s)) - np.max(np.abs(c["speeds"]))) < 1e-14 * np.max(np.abs(c["speeds"]))
+        s = orc.speeds(pb, Qg)  # all six speeds, in the reference's order
+        assert np.max(np.abs(s - c["speeds"])) < 1e-14 * np.max(np.abs(c["speeds"]))
 
 
 def test_golden_nondefault_exponents(orc, golden):
@@ -111,8 +111,8 @@ def test_golden_nondefault_exponents(orc, golden):
         assert rel_err(orc.energy(e, t["S"], G), t["energy"]) < 1e-12
         assert rel_err(orc.stress(e, t["S"], F), t["stress"]) < 1e-13
         assert rel_err(orc.acoustic(e, t["S"], F), t["acoustic"]) < 1e-13
-        got = np.sort(orc.eig3_moduli(np.array(t["acoustic"])))[::-1]
-        assert abs(got[0] - t["moduli"][0]) <= 1e-14 * t["moduli"][0]
+        got = orc.eig3_sorted(np.array(t["acoustic"]))
+        assert np.max(np.abs(got - t["moduli"])) <= 1e-14 * np.max(t["moduli"])
     pb = orc.problem(eos=(e, e))
     for c in nd["cells"]:
         Q = orc.prim2cons(pb, np.array(c["P"])[1:])
@@ -120,7 +120,7 @@ def test_golden_nondefault_exponents(orc, golden):
         Qg = np.array(c["Q"][1:])
         assert rel_err(orc.flux(pb, Qg), c["flux"][1:]) < 1e-13
         s = orc.speeds(pb, Qg)
-        assert abs(np.max(np.abs(s)) - np.max(np.abs(c["speeds"]))) < 1e-14 * np.max(np.abs(c["speeds"]))
+        assert np.max(np.abs(s - c["speeds"])) < 1e-14 * np.max(np.abs(c["speeds"]))
 
 
 def test_golden_twophase_noncons_and_hll(orc, golden):
@@ -268,3 +268,63 @@ def test_dual_run_gradient_matches_central_differences(orc):
         fd[k] = (loss(tp) - loss(tm)) / (tp[k] - tm[k])
     rel = np.abs(g - fd) / np.maximum(np.abs(fd), 1e-3 * np.max(np.abs(fd)))
     assert rel.max() <= 1e-6, rel
+
+
+def test_eigvals_order_is_julias(orc):
+    """get_eigvals returns u.n + c_k then u.n - c_k with c_k = sqrt|mu_k| and mu_k in the
+    order Julia's eigvals gives (ascending real part, HyperelasticityMPh.jl:263); checked
+    against LAPACK (numpy) eigenvalues sorted the same way, for all three moduli."""
+    rng = np.random.default_rng(8)
+    e = orc.barton2009()
+    for _ in range(50):
+        F = np.eye(3) + 0.15 * rng.standard_normal((3, 3))
+        if np.linalg.det(F) <= 0:
+            continue
+        ac = orc.acoustic(e, rng.uniform(0, 2e-3), F.reshape(-1, order="F"), rng.standard_normal(3))
+        ev = np.abs(sorted(np.linalg.eigvals(ac.reshape(3, 3, order="F")), key=lambda z: (z.real, z.imag)))
+        # eigenvalues are accurate relative to the matrix norm (LAPACK's bound), not each to itself
+        assert np.max(np.abs(orc.eig3_sorted(ac) - ev)) <= 1e-13 * np.max(ev)
+    # a non-symmetric matrix with a complex pair: the pair's real part orders it
+    M = np.array([[3.0, -2.0, 0.0], [2.0, 3.0, 0.0], [0.0, 0.0, 1.0]])
+    ev = sorted(np.linalg.eigvals(M), key=lambda z: (z.real, z.imag))
+    np.testing.assert_allclose(orc.eig3_sorted(M.reshape(-1, order="F")), np.abs(ev), rtol=1e-14)
+    M = np.array([[-5.0, 1.0, 0.0], [0.0, 2.0, 0.5], [0.3, 0.0, 0.5]])
+    ev = sorted(np.linalg.eigvals(M), key=lambda z: (z.real, z.imag))
+    np.testing.assert_allclose(orc.eig3_sorted(M.reshape(-1, order="F")), np.abs(ev), rtol=1e-13)
+
+
+def test_golden_function_forms(orc, golden):
+    """acoustic(eos, ent, F, n) for general n, stress(eos, den, e_int, F), acoustic(eos, P, n),
+    get_eigvals along n and an HLL face given wider speeds, against the 40-digit
+    transliteration (its acoustic(eos, P, n) by 40-digit central differences)."""
+    x = golden["extras"]
+    e = orc.barton2009()
+    for t in x["acoustic_dir"]:
+        assert rel_err(orc.acoustic(e, t["S"], np.array(t["F"]), t["n"]), t["acoustic"]) < 1e-13
+    for t in x["stress_den"]:
+        assert rel_err(orc.stress_den(e, t["den"], t["e_int"], np.array(t["F"])), t["stress"]) < 1e-12
+    for t in x["acoustic_prim"]:
+        assert rel_err(orc.acoustic_prim(e, np.array(t["P"]), t["n"]), t["acoustic"]) < 1e-12
+    pb = orc.problem()
+    for c in x["speeds_dir"]:
+        s = orc.speeds(pb, np.array(c["Q"])[1:], c["n"])
+        assert np.max(np.abs(s - c["speeds"])) < 1e-13 * np.max(np.abs(c["speeds"]))
+    h = x["hll_given"]
+    eos = (orc.barton2009(), orc.barton2009(b0=golden["eos2_b0"]))
+    pb2 = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, eos=eos)
+    dm, dp = orc.hll(pb2, np.array(h["Ql"]), np.array(h["Qr"]), np.array(h["spdL"]), np.array(h["spdR"]))
+    assert rel_err(dm, h["dm"]) < 1e-12 and rel_err(dp, h["dp"]) < 1e-12
+
+
+def test_acoustic_prim_holds_energy_not_entropy(orc):
+    """acoustic(eos, P, n) differs from acoustic(eos, S, A, n) only through the entropy
+    following F at fixed e_int: at S with exp(S/cv) = 1 (cold state) and no shear
+    deformation the two agree; in general they do not."""
+    e = orc.barton2009()
+    I9 = np.eye(3).reshape(-1, order="F")
+    P = np.concatenate([[1.0, 8.93, 0, 0, 0, 0.0], I9])
+    np.testing.assert_allclose(orc.acoustic_prim(e, P, [1.0, 0, 0]), orc.acoustic(e, 0.0, I9), rtol=1e-12, atol=1e-12)
+    rng = np.random.default_rng(3)
+    F = (np.eye(3) + 0.05 * rng.standard_normal((3, 3))).reshape(-1, order="F")
+    P = np.concatenate([[1.0, 8.93 / np.linalg.det(F.reshape(3, 3)), 0, 0, 0, 1e-3], F])
+    assert rel_err(orc.acoustic_prim(e, P, [1.0, 0, 0]), orc.acoustic(e, 1e-3, F)) > 1e-6

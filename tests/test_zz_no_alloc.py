@@ -28,23 +28,30 @@ def _riemann_state(orc, nx):
     return initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
 
 
-def test_noalloc_step_matches_context_step_twice(hyp, orc):
+@pytest.mark.parametrize("flux,bc", [("rusanov", "frozen"), ("lxf", "transmissive")])
+@pytest.mark.parametrize("k", [0, 24, 25])  # even: the input goes straight to the output; odd: via the scratch state
+@pytest.mark.parametrize("in_place", [False, True])
+def test_noalloc_step_matches_context_step_twice(hyp, orc, flux, bc, k, in_place):
     torch = pytest.importorskip("torch")
     assert torch.cuda.is_available()
     L = hyp._lib.load()
-    nx, k = 4096, 25
+    nx = 4096
     Q0 = _riemann_state(orc, nx)
-    # reference: the context API, k steps then k more
-    with hyp.Solver(hyp.Barton2009(), nx, cfl=0.5) as s:
-        s.upload(Q0)
-        s.step(max_steps=k)
-        ref1, (tr1, _) = s.download(), s.time()
-        s.step(max_steps=k)
-        ref2, (tr2, _) = s.download(), s.time()
-    cfg = hyp._model.config(hyp.Barton2009(), hyp._lib.HYP_MODEL_SINGLE, n_cells=nx, cfl=0.5)
+    fl = {"rusanov": hyp._lib.HYP_FLUX_RUSANOV, "lxf": hyp._lib.HYP_FLUX_LXF}[flux]
+    bcc = {"frozen": hyp._lib.HYP_BC_FROZEN, "transmissive": hyp._lib.HYP_BC_TRANSMISSIVE}[bc]
+    # reference: the context API, k steps then k more (no steps: the input itself)
+    ref1, ref2, tr1, tr2 = Q0, Q0, 0.0, 0.0
+    if k > 0:
+        with hyp.Solver(hyp.Barton2009(), nx, cfl=0.5, flux=flux, bc=bc) as s:
+            s.upload(Q0)
+            s.step(max_steps=k)
+            ref1, (tr1, _) = s.download(), s.time()
+            s.step(max_steps=k)
+            ref2, (tr2, _) = s.download(), s.time()
+    cfg = hyp._model.config(hyp.Barton2009(), hyp._lib.HYP_MODEL_SINGLE, n_cells=nx, flux=fl, bc=bcc, cfl=0.5)
     d_in = torch.from_numpy(Q0).cuda()
-    d_out = torch.empty_like(d_in)
-    d_out2 = torch.empty_like(d_in)
+    d_out = d_in if in_place else torch.empty_like(d_in)
+    d_out2 = d_in if in_place else torch.empty_like(d_in)
     torch.cuda.synchronize()
     t = ctypes.c_double(0.0)
     cell = ctypes.c_int64(0)
@@ -52,6 +59,7 @@ def test_noalloc_step_matches_context_step_twice(hyp, orc):
     rc = L.hyp_step_noalloc_f64(cfg, d_in.data_ptr(), d_out.data_ptr(), nx, k, 0.0, None, ctypes.byref(t),
                                 ctypes.byref(cell))
     assert rc == 0, rc
+    assert cell.value == -1
     free_after_first = torch.cuda.mem_get_info()[0]
     assert abs(t.value - tr1) <= RTOL_FP64 * tr1
     assert_close_soa(d_out.cpu().numpy(), ref1, RTOL_FP64, "no-alloc call 1")
@@ -63,6 +71,12 @@ def test_noalloc_step_matches_context_step_twice(hyp, orc):
     assert torch.cuda.mem_get_info()[0] == free_after_first  # nothing allocated by the second call
     assert abs(t.value - tr2) <= RTOL_FP64 * tr2
     assert_close_soa(d_out2.cpu().numpy(), ref2, RTOL_FP64, "no-alloc call 2")
+    if k > 0:  # and both calls against the oracle directly, not only through the context API
+        pb = orc.problem(nx=nx, cfl=0.5, flux={"rusanov": orc.FLUX_RUSANOV, "lxf": orc.FLUX_LXF}[flux],
+                         bc={"frozen": orc.BC_FROZEN, "transmissive": orc.BC_TRANSMISSIVE}[bc])
+        Qo, so, to, _ = orc.run(pb, Q0, max_steps=2 * k, nthreads=4)
+        assert so == 2 * k and abs(t.value - to) <= RTOL_FP64 * to
+        assert_close_soa(d_out2.cpu().numpy(), Qo, RTOL_FP64, "no-alloc call 2 vs oracle")
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(hyp):
