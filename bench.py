@@ -272,11 +272,16 @@ def run_ours(args):
         dist.barrier()
     t0 = time.perf_counter()
     s.upload(pin_in.array)
-    for _ in range(K):
-        s.step(max_steps=1)  # per step the host reads back t (the reference logs Step/t/dt every step)
+    t1 = time.perf_counter()
+    # the K steps with the time after each one read back (the reference logs Step / t / dt
+    # every step, main.jl:229-237), then the final state
+    s.step_times(max_steps=K)
+    t2 = time.perf_counter()
     s.download(pin_out.array)
-    e2e_s = dist_max(dist, time.perf_counter() - t0)
+    t3 = time.perf_counter()
+    e2e_s = dist_max(dist, t3 - t0)
     e2e = WORLD * n * K / e2e_s
+    e2e_parts = {"upload_ms": 1e3 * (t1 - t0), "steps_ms": 1e3 * (t2 - t1), "download_ms": 1e3 * (t3 - t2)}
     s.close()
     pin_in.close()
     pin_out.close()
@@ -303,7 +308,7 @@ def run_ours(args):
         "config": config_block(args), "precision": PRECISION_NOTE[prec],
         "clocks": clocks,
         "e2e": {"value": e2e, "unit": METRIC, "h2d_bytes_per_step": state_bytes / K,
-                "d2h_bytes_per_step": state_bytes / K + 64},
+                "d2h_bytes_per_step": state_bytes / K + 8, **e2e_parts},
         "gpu_launches": tm["n_cell"] + tm["n_update"],
         "roofline": rf,
     }
@@ -313,6 +318,7 @@ def run_ours(args):
         v, sample = cpu_sample(Q0, args.cpu_seconds, os.cpu_count())
         line["cpu_baseline"] = {"value": v, "unit": METRIC, "cores": os.cpu_count(), "kind": "port", "sample": sample}
     if WORLD == 1 and not args.no_workloads:
+        line["measured_rates"] = measure_rates()
         line["workloads"] = workload_summaries(args)
     print(json.dumps(line))
     return 0
@@ -361,6 +367,33 @@ def workload_summaries(args):
                       "ms_forward": a["ms"]["forward"], "ms_reverse": a["ms"]["recompute"] + a["ms"]["adjoint"],
                       "fd_max_rel": a["fd_check"]["max_rel"], "clocks": a["clocks"]}
     return out
+
+
+def measure_rates(reps=3, nbytes=1 << 30):
+    """FP64 / FP32 / packed-f32x2 FMA throughput and the host link's copy rates of this GPU
+    (hyp_measure_peaks): the denominators the driver's copy and GEMM peaks do not give."""
+    import ctypes
+    import hyperelasticsolver_gb300 as h
+    out = np.zeros(6)
+    h._lib.check(h._lib.load().hyp_measure_peaks(int(reps), int(nbytes), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                 what="hyp_measure_peaks")
+    return {"fp64_fma_tflops": out[0], "fp32_fma_tflops": out[1], "fp32x2_fma_tflops": out[2],
+            "h2d_gbs": out[3], "d2h_gbs": out[4], "bidirectional_gbs_each_way": out[5],
+            "copy_bytes": nbytes, "note": "best of %d; FMA: 8 independent chains per thread, 8 x 256-thread blocks per SM" % reps}
+
+
+def run_peaks(args):
+    import hyperelasticsolver_gb300 as h
+    h.build_library()
+    clk = ClockSampler()
+    clk.start()
+    r = measure_rates()
+    clocks = clk.stop()
+    line = {"metric": "measured rates", "value": r["fp64_fma_tflops"], "unit": "FP64 TFLOP/s", "n_gpus": 1,
+            "steps": 1, "warmup": 0, "higher_is_better": True, "data": "synthetic", "rates": r, "clocks": clocks,
+            "config": {"workload": "FMA chains and page-locked host copies"}}
+    print(json.dumps(line))
+    return 0
 
 
 def run_batch(args):
@@ -624,8 +657,9 @@ def run_evaluators(args):
     return 0
 
 
-DEFAULT_STEPS = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000, "evaluators": 3}
-DEFAULT_CELLS = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536, "evaluators": 1 << 20}
+DEFAULT_STEPS = {"single": 200, "batch": 500, "mph": 300, "adjoint": 1000, "evaluators": 3, "peaks": 1}
+DEFAULT_CELLS = {"single": 1 << 24, "batch": None, "mph": 1 << 22, "adjoint": 65536, "evaluators": 1 << 20,
+                 "peaks": None}
 
 
 def main():
@@ -643,7 +677,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-workloads", action="store_true",
                     help="single workload: skip the batch / two-phase / adjoint summaries in its line")
-    ap.add_argument("--workload", choices=["single", "batch", "mph", "adjoint", "evaluators"], default="single",
+    ap.add_argument("--workload", choices=["single", "batch", "mph", "adjoint", "evaluators", "peaks"], default="single",
                     help="single: the headline single-phase step; batch: 4096 ragged problems; mph: two-phase HLL; "
                          "adjoint: gradient of a 1000-step run; evaluators: the function-level API")
     ap.add_argument("--flux", choices=["hll", "lxf"], default="hll", help="two-phase workload's face flux")
@@ -660,7 +694,7 @@ def main():
     if args.impl == "reference":
         return run_reference(args)
     runner = {"batch": run_batch, "adjoint": run_adjoint, "mph": run_mph,
-              "evaluators": run_evaluators}.get(args.workload, run_ours)
+              "evaluators": run_evaluators, "peaks": run_peaks}.get(args.workload, run_ours)
     return runner(args)
 
 

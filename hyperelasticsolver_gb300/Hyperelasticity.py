@@ -48,3 +48,72 @@ def get_eigvals(eos, Q, n=(1, 0, 0)):
     the eigenvalues of acoustic(eos, S, A, n) in Julia's eigvals order (ascending real
     part). n: one direction (3,) or one per state (m, 3)."""
     return M.eigvals_call(_cfg(eos), Q, 14, 6, n)
+
+
+# ---- the 13-value layout of the reference's single-phase module ------------
+# Hyperelasticity.jl:25-114 stores a cell as 13 values: rho u (3), rho F row-major
+# (Q[3i + j] = rho F[i, j], 1-based, :82-86), rho E; its density is
+# sqrt(det(rho F) / rho0) (EquationsOfState.jl:259-264). That module calls EOS methods
+# the reference no longer defines (density and stress without the eos argument), so it
+# cannot run there; these functions give its names a working form, with the eos passed
+# in, by converting to the 14-value layout above and back.
+_ROW_TO_COL = np.array([3 * (k % 3) + k // 3 for k in range(9)])  # col-major slot c <- row-major slot
+
+
+def q13_to_q14(eos, Q13):
+    """(n, 13) or (13,) -> (n, 14): rho = sqrt(det(rho F)/rho0) prepended, rho F column-major."""
+    q = np.atleast_2d(np.asarray(Q13, dtype=np.float64))
+    rF_row = q[:, 3:12]
+    rF = rF_row.reshape(-1, 3, 3)  # [i][j] = rho F[i, j]
+    den = np.sqrt(np.linalg.det(rF) / eos.rho0)
+    out = np.empty((q.shape[0], 14))
+    out[:, 0] = den
+    out[:, 1:4] = q[:, 0:3]
+    out[:, 4] = q[:, 12]
+    out[:, 5:14] = rF_row[:, _ROW_TO_COL]
+    return out[0] if np.ndim(Q13) == 1 else out
+
+
+def q14_to_q13(Q14):
+    """(n, 14) or (14,) -> (n, 13): rho dropped, rho A written row-major."""
+    q = np.atleast_2d(np.asarray(Q14, dtype=np.float64))
+    out = np.empty((q.shape[0], 13))
+    out[:, 0:3] = q[:, 1:4]
+    out[:, 3:12][:, _ROW_TO_COL] = q[:, 5:14]
+    out[:, 12] = q[:, 4]
+    return out[0] if np.ndim(Q14) == 1 else out
+
+
+def cons2prim13(eos, Q13):
+    """cons2prim of Hyperelasticity.jl:25-36 with the eos: (den, vel (n, 3), F (n, 3, 3), e_int)."""
+    q14 = np.atleast_2d(q13_to_q14(eos, Q13))
+    den = q14[:, 0]
+    vel = q14[:, 1:4] / den[:, None]
+    F = (q14[:, 5:14] / den[:, None]).reshape(-1, 3, 3).transpose(0, 2, 1)
+    e_int = q14[:, 4] / den - 0.5 * np.sum(vel * vel, axis=1)
+    if np.ndim(Q13) == 1:
+        return den[0], vel[0], F[0], e_int[0]
+    return den, vel, F, e_int
+
+
+def prim2cons13(eos, vel, F, S):
+    """prim2cons of Hyperelasticity.jl:70-93 with the eos: vel (3,) / (n, 3), F (3, 3) / (n, 3, 3), S."""
+    single = np.ndim(vel) == 1
+    vel = np.atleast_2d(np.asarray(vel, dtype=np.float64))
+    F = np.asarray(F, dtype=np.float64).reshape(-1, 3, 3)
+    S = np.broadcast_to(np.asarray(S, dtype=np.float64), (F.shape[0],))
+    P = np.empty((F.shape[0], 14))
+    P[:, 0] = eos.rho0 / np.linalg.det(F)  # :78
+    P[:, 1:4] = vel
+    P[:, 4] = S
+    P[:, 5:14] = F.transpose(0, 2, 1).reshape(-1, 9)  # column-major
+    out = q14_to_q13(prim2cons(eos, P))
+    return out[0] if single else out
+
+
+def flux13(eos, Q13):
+    """flux of Hyperelasticity.jl:99-114 with the eos, 13 values: the rho F rows follow the
+    14-value flux (row 1 identically zero, :106), energy last."""
+    f14 = np.atleast_2d(flux(eos, np.atleast_2d(q13_to_q14(eos, Q13))))
+    out = q14_to_q13(f14)
+    return out[0] if np.ndim(Q13) == 1 else out

@@ -52,3 +52,12 @@ def initial_states(eos, testcase):
     L.check(L.load().hyp_initial_states(_cfg(eos), int(testcase), L.ptr(Ql), L.ptr(Qr)),
             what=f"initial_states({testcase})")
     return Ql, Qr
+
+
+def relax_pressure(eos, Q):
+    """Instantaneous pressure relaxation of two-phase cells (hyp_eval_relax): volume
+    fractions moved until both phases' mean-stress pressures agree, energies by
+    de = -p* dv, distortions scaled in their volumetric part. An extension (the
+    reference has no relaxation terms); cells with a phase below 1e-5 come back as they
+    are, a cell whose Newton iteration does not converge as NaN."""
+    return M.call("hyp_eval_relax", _cfg(eos), Q, 30, 30)

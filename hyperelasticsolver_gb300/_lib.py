@@ -23,6 +23,7 @@ HYP_MODEL_SINGLE, HYP_MODEL_MULTI = 1, 2
 HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = 0, 1, 2
 HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = 0, 1
 HYP_PREC_FP64, HYP_PREC_MIXED = 0, 1
+HYP_RELAX_NONE, HYP_RELAX_PRESSURE = 0, 1
 HYP_BATCH_NUM_VARIANTS = 6
 
 
@@ -96,6 +97,8 @@ _SIGS = {
     "hyp_set_wait_limit": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
     "hyp_step_noalloc_f64": ([ctypes.POINTER(ConfigC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_double, ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
+    "hyp_set_relaxation": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
+    "hyp_eval_relax": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
     "hyp_set_slab": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hyp_slab_local_max": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "hyp_slab_step": ([ctypes.c_void_p, ctypes.c_double, _dp], ctypes.c_int),
@@ -125,6 +128,7 @@ _SIGS = {
     "hyp_initial_states": ([ctypes.POINTER(ConfigC), ctypes.c_int, _dp, _dp], ctypes.c_int),
     "hyp_init_riemann": ([ctypes.c_void_p, _dp, _dp], ctypes.c_int),
     "hyp_init_tanh": ([ctypes.c_void_p, _dp, _dp, ctypes.c_double], ctypes.c_int),
+    "hyp_measure_peaks": ([ctypes.c_int, _i64, _dp], ctypes.c_int),
     "hyp_host_alloc": ([ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "hyp_host_free": ([ctypes.c_void_p], ctypes.c_int),
     "hyp_eval_finger": ([_dp, _dp, _i64], ctypes.c_int),

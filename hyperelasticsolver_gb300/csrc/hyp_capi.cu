@@ -4,6 +4,7 @@
 #include <cstring>
 #include <new>
 #include "hyp_internal.cuh"
+#include "hyp_relax.cuh"
 
 using namespace hyp;
 
@@ -205,6 +206,11 @@ static int check_cell_error(hyp_ctx* c) {
     snprintf(buf, sizeof buf, "a device wait for a tile load timed out (tile starting at cell %lld)", (long long)c->err_cell);
     return set_err(c, HYP_ERR_TIMEOUT, buf);
   }
+  if (code & HYP_CELL_RELAX) {
+    snprintf(buf, sizeof buf, "pressure relaxation did not converge in cell %lld (left unrelaxed)",
+             (long long)c->err_cell);
+    return set_err(c, HYP_ERR_NONFINITE, buf);
+  }
   if (code & HYP_CELL_NEG_DET) {
     snprintf(buf, sizeof buf, "det(rho A) <= 0 in cell %lld (reference: DomainError in sqrt)", (long long)c->err_cell);
     return set_err(c, HYP_ERR_NEG_DET, buf);
@@ -327,12 +333,14 @@ static int enqueue_step(hyp_ctx* c, long long k, double t_end, bool prof) {
     CK(launch_face2_mixed(c, p, t_end));
     if (prof) CK(cudaEventRecord(e1, c->stream));
     CK(launch_update2_mixed(c, p, t_end));
+    if (c->relax) CK(launch_relax2(c, p, t_end));
   } else if (c->cfg.model == HYP_MODEL_MULTI) {
     const int p = (int)(k & 1);
     CK(launch_cell2_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
     CK(launch_face2_f64(c, p, t_end));
     if (prof) CK(cudaEventRecord(e1, c->stream));
     CK(launch_update2_f64(c, p, t_end));
+    if (c->relax) CK(launch_relax2(c, p, t_end));
   } else if (!mixed(c)) {
     const int p = (int)(k & 1);
     CK(launch_cell1_f64(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));

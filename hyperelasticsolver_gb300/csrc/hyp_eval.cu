@@ -6,6 +6,7 @@
 #include <vector>
 #include "hyp_internal.cuh"
 #include "hyp_hank.cuh"
+#include "hyp_relax.cuh"
 
 using namespace hyp;
 
@@ -512,4 +513,26 @@ extern "C" int hyp_eval_hll_eigvals(const hyp_config* cfg, const double* Ql, con
                k_hll<<<(unsigned)((n + 63) / 64), 64>>>(*(const HllArg*)p, d[0], d[1], d[2], d[3], d[4], d[5], n);
              },
              &a);
+}
+
+// ---- two-phase pressure relaxation (hyp_relax.cuh) --------------------------
+namespace {
+__global__ void k_relax(ModelArg m, const double* Q, double* R, int64_t n) {
+  IDX double q[30];
+  LD(q, Q, 30);
+  if (relax_pressure2(m.e, q)) {
+    for (int c = 0; c < 30; ++c) q[c] = NAN;  // not converged
+  }
+  ST(R, q, 30);
+}
+}  // namespace
+
+extern "C" int hyp_eval_relax(const hyp_config* cfg, const double* Q, double* Q_out, int64_t n) {
+  if (!model_ok(cfg) || cfg->model != HYP_MODEL_MULTI) return HYP_ERR_INVALID;
+  ModelArg m = model_arg(cfg);
+  return run(n, {{Q, nullptr, 30}, {nullptr, Q_out, 30}},
+             [](int64_t n, double** d, const void* a) {
+               k_relax<<<grid(n), kBlock>>>(*(const ModelArg*)a, d[0], d[1], n);
+             },
+             &m);
 }

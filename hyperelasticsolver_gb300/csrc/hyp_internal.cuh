@@ -195,6 +195,7 @@ struct hyp_ctx {
   int slab_ghost[2] = {0, 0};  // the first / last cell is a ghost
   double slab_dx = 0.0;
   long long slab_cell_pass = -1;  // FP64: the step whose cell pass (fluxes, speeds) is done
+  int relax = HYP_RELAX_NONE;     // two-phase pressure relaxation after each step (hyp_relax.cu)
   hyp::AdjTape* tape = nullptr;  // checkpoints and buffers of the adjoint (hyp_adjoint.cu)
   hyp::SnapBuf* snap = nullptr;  // snapshot buffers and writer (hyp_snapshot.cu)
 };
@@ -254,6 +255,8 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end);
 cudaError_t launch_cell2_f64(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
 cudaError_t launch_face2_f64(hyp_ctx* c, int p, double t_end);
 cudaError_t launch_update2_f64(hyp_ctx* c, int p, double t_end);
+// two-phase pressure relaxation of the state the step of parity p wrote (hyp_relax.cu)
+cudaError_t launch_relax2(hyp_ctx* c, int p, double t_end);
 Quad6D gauss_legendre6();
 Quad6D gauss_lobatto6();
 }  // namespace hyp

@@ -32,6 +32,8 @@ end
 const HYP_MODEL_SINGLE, HYP_MODEL_MULTI = Cint(1), Cint(2)
 const HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = Cint(0), Cint(1), Cint(2)
 const HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = Cint(0), Cint(1)
+const HYP_RELAX_NONE = Cint(0)
+const HYP_RELAX_PRESSURE = Cint(1)
 const HYP_PREC_FP64, HYP_PREC_MIXED = Cint(0), Cint(1)
 
 struct HypError <: Exception
@@ -310,6 +312,18 @@ initial_condition_tanh!(s::Solver, Ql::Vector{Float64}, Qr::Vector{Float64}, eps
   check(ccall((:hyp_init_tanh, libhyp), Cint, (Ptr{Cvoid}, Ptr{Float64}, Ptr{Float64}, Float64), s.h, Ql, Qr, eps),
         "hyp_init_tanh", s.h)
 
+# ---- two-phase pressure relaxation (an extension: the reference has none) ----
+"set_relaxation!(s, mode): HYP_RELAX_NONE (default) or HYP_RELAX_PRESSURE after each two-phase step"
+set_relaxation!(s::Solver, mode::Integer) =
+  check(ccall((:hyp_set_relaxation, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, mode), "hyp_set_relaxation", s.h)
+"relax_pressure(eos, Q): instantaneous pressure relaxation of two-phase cells (n, 30)"
+function relax_pressure(eos::Tuple, Q::Matrix{Float64})
+  out = similar(Q)
+  check(ccall((:hyp_eval_relax, libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64),
+              Ref(config(eos, HYP_MODEL_MULTI)), Q, out, size(Q, 1)), "relax_pressure")
+  out
+end
+
 # ---- domain decomposition: one slab per rank (a ghost cell at each inner end) ----
 """set_slab!(s, dx, left_ghost, right_ghost): make s one slab of a decomposed domain with
 the global dx; hyp_step then refuses it (a slab steps with the global max)"""
@@ -359,6 +373,12 @@ function step_noalloc!(cfg::ConfigC, d_in::Ptr{Float64}, d_out::Ptr{Float64}, n_
              Ref(cfg), d_in, d_out, cfg.n_cells, n_steps, t0, stream, t, cell)
   rc == 0 || throw(HypError(rc, "hyp_step_noalloc_f64 (cell $(cell[]))"))
   t[]
+end
+"measure_peaks(; reps=3, bytes=1<<30): (fp64_tflops, fp32_tflops, fp32x2_tflops, h2d_gbs, d2h_gbs, bidir_gbs)"
+function measure_peaks(; reps::Integer=3, bytes::Integer=1 << 30)
+  out = zeros(6)
+  check(ccall((:hyp_measure_peaks, libhyp), Cint, (Cint, Int64, Ptr{Float64}), reps, bytes, out), "hyp_measure_peaks")
+  Tuple(out)
 end
 "pinned_matrix(n, k): a Matrix{Float64} in page-locked host memory (hyp_host_alloc) for fast copies"
 function pinned_matrix(n::Integer, k::Integer)

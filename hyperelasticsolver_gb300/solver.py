@@ -22,7 +22,8 @@ class Solver:
     eos (one Barton2009, or a pair for the two-phase model), nx, X, cfl, and
     the flux choice of main.jl:223-225. State arrays are SoA (nvar, nx)."""
 
-    def __init__(self, eos, nx, model="single", flux="rusanov", bc="frozen", precision="fp64", X=1.0, cfl=0.5):
+    def __init__(self, eos, nx, model="single", flux="rusanov", bc="frozen", precision="fp64", X=1.0, cfl=0.5,
+                 relax=None):
         self.model = _MODELS[model]
         self.nvar = M.nvar(self.model)
         self.nx = int(nx)
@@ -31,6 +32,14 @@ class Solver:
         h = ctypes.c_void_p()
         L.check(lib.hyp_create(self.cfg, ctypes.byref(h)), what="hyp_create")
         self._h = h
+        if relax is not None:
+            self.set_relaxation(relax)
+
+    def set_relaxation(self, mode):
+        """Two-phase pressure relaxation after each step: "pressure", or None (the reference's
+        model, the default). An extension: the reference has no relaxation terms."""
+        m = {None: L.HYP_RELAX_NONE, "none": L.HYP_RELAX_NONE, "pressure": L.HYP_RELAX_PRESSURE}[mode]
+        L.check(L.load().hyp_set_relaxation(self._h, m), self._h, "hyp_set_relaxation")
 
     def close(self):
         if getattr(self, "_h", None):

@@ -51,6 +51,9 @@ enum { HYP_FLUX_RUSANOV = 0, HYP_FLUX_LXF = 1, HYP_FLUX_HLL = 2 };
 enum { HYP_BC_FROZEN = 0, HYP_BC_TRANSMISSIVE = 1 };
 /* arithmetic: plain FP64, or FP32 fluxes with a compensated hi/lo FP32 state */
 enum { HYP_PREC_FP64 = 0, HYP_PREC_MIXED = 1 };
+/* two-phase relaxation after each step (hyp_set_relaxation): none (the reference's
+   model), or instantaneous pressure relaxation */
+enum { HYP_RELAX_NONE = 0, HYP_RELAX_PRESSURE = 1 };
 
 /* Barton2009 primary parameters (EquationsOfState.jl:71-116); b0sq and k0 are derived.
    Defaults of the reference constructor: 8.93, 4.6, 3.9e-4, 300, 2.1, 1, 3, 2. */
@@ -98,6 +101,21 @@ int hyp_step(hyp_ctx* ctx, int max_steps, double t_end, int* steps_done, double*
    next step uses the new EOS (the reference passes eos to every call, main.jl:134,
    so a driver may change it between steps). A recorded adjoint run is discarded. */
 int hyp_set_eos(hyp_ctx* ctx, int phase, const hyp_barton2009* eos);
+/* Two-phase contexts: relaxation applied to every cell after each step; off
+   (HYP_RELAX_NONE) by default. The reference has no relaxation terms (its two-phase
+   model, HyperelasticityMPh.jl, ends at the non-conservative interface terms); this
+   is an extension with no reference to match. HYP_RELAX_PRESSURE: instantaneous
+   pressure relaxation (Saurel, Petitpas & Berry 2009) with hyperelastic phases as
+   Favrie, Gavrilyuk & Saurel 2009 treat them: volume fractions move until both
+   phases' mean-stress pressures agree, each phase's internal energy follows
+   de = -p* dv and its distortion changes in its volumetric part only; each phase's
+   mass and momentum and the mixture's total energy are conserved. Cells with a phase
+   below 1e-5 are left as they are; with frozen ends the end cells too. Mixed
+   contexts relax in FP64. A cell that does not converge is left unrelaxed and the
+   step returns HYP_ERR_NONFINITE with its index. */
+int hyp_set_relaxation(hyp_ctx* ctx, int mode);
+/* The same relaxation of n two-phase cells (function level).  Q, Q_out: [30][n] */
+int hyp_eval_relax(const hyp_config* cfg, const double* Q, double* Q_out, int64_t n);
 /* hyp_step (max_steps >= 1) that also returns the time after every step taken,
    t_hist[0 .. *steps_done - 1] (host, max_steps entries): the Step / t / dt line
    main.jl:229-237 logs each step, read back once at the end rather than with a
@@ -269,6 +287,13 @@ int hyp_init_riemann(hyp_ctx* ctx, const double* Ql, const double* Qr);
    cell the primitive state of its side with alpha1 = 0.1 (tanh(4 (x - 1/2)/eps) + 1)
    + 0.4 and alpha2 = 1 - alpha1, x = (i - 1/2)/nx. */
 int hyp_init_tanh(hyp_ctx* ctx, const double* Ql, const double* Qr, double eps);
+
+/* Measured rates of this GPU for the roofline denominators the step needs (no
+   counterpart in the reference, which publishes no hardware figures): out[0..5] =
+   FP64 FMA TFLOP/s, FP32 FMA TFLOP/s, packed f32x2 FMA TFLOP/s, host-to-device GB/s,
+   device-to-host GB/s, and GB/s each way with both directions at once (page-locked
+   buffers of `bytes`); each the best of `reps`. */
+int hyp_measure_peaks(int reps, int64_t bytes, double* out);
 
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);

@@ -711,6 +711,78 @@ enum { MODEL_SINGLE = 1, MODEL_MULTI = 2 };
 enum { FLUX_RUSANOV = 0, FLUX_LXF = 1, FLUX_HLL = 2 };
 enum { BC_FROZEN = 0, BC_TRANSMISSIVE = 1 };
 
+// ---------------------------------------------------------------------------
+// Instantaneous pressure relaxation of a two-phase cell (an extension: the reference
+// has no relaxation terms, so nothing here is pinned to it). The procedure of Saurel,
+// Petitpas & Berry (2009) with hyperelastic phases as Favrie, Gavrilyuk & Saurel (2009)
+// treat them: unknowns alpha_1' and p*; per phase v' = alpha'/m, e' = e - p* (v' - v),
+// the distortion scaled by (v'/v)^(1/3), and p(e', v') = p* where p = -tr(sigma)/3 of
+// stress(eos, S, A') (the dual-number stress above) at S = entropy(eos, e', finger(A')).
+// Newton's method on the 2x2 system, its derivatives by central differences.
+inline double relax_pressure_of(const Barton& e, const double* A, double lam, double eint) {
+  double As[9], G[9], sig[9];
+  for (int c = 0; c < 9; ++c) As[c] = lam * A[c];
+  finger(As, G);
+  const double S = entropy(e, eint, G);
+  stress(e, S, As, sig);
+  return -(M3(sig, 0, 0) + M3(sig, 1, 1) + M3(sig, 2, 2)) / 3.0;
+}
+inline int relax_pressure2(const Barton* eos, double* Q) {
+  constexpr double kMinAlpha = 1e-5;
+  double P[2][15], m[2], v[2], a0[2] = {Q[0], Q[15]};
+  if (!(a0[0] >= kMinAlpha && a0[1] >= kMinAlpha)) return 0;
+  for (int k = 0; k < 2; ++k) {
+    cons2prim(eos[k], Q + 15 * k, P[k]);
+    m[k] = P[k][0] * P[k][1];
+    v[k] = 1.0 / P[k][1];
+  }
+  double e0[2], A[2][9], ke[2];
+  for (int k = 0; k < 2; ++k) {
+    for (int c = 0; c < 9; ++c) A[k][c] = P[k][6 + c];
+    ke[k] = 0.5 * (P[k][2] * P[k][2] + P[k][3] * P[k][3] + P[k][4] * P[k][4]);
+    e0[k] = Q[15 * k + 5] / m[k] - ke[k];
+  }
+  auto pres = [&](int k, double vk, double ek) { return relax_pressure_of(eos[k], A[k], std::cbrt(vk / v[k]), ek); };
+  double x = a0[0], ps = a0[0] * pres(0, v[0], e0[0]) + a0[1] * pres(1, v[1], e0[1]);
+  double pscale = std::fabs(ps);
+  for (int k = 0; k < 2; ++k) pscale = std::max(pscale, eos[k].k0 * eos[k].rho0);
+  bool done = false;
+  for (int it = 0; it < 40 && !done; ++it) {
+    double F[2], Jx[2], Jp[2];
+    for (int k = 0; k < 2; ++k) {
+      const double ak = k == 0 ? x : 1.0 - x, vk = ak / m[k], ek = e0[k] - ps * (vk - v[k]);
+      const double hv = 1e-7 * vk, he = 1e-7 * (std::fabs(ek) + std::fabs(ps * vk)) + 1e-12;
+      const double p0 = pres(k, vk, ek);
+      const double dpdv = (pres(k, vk + hv, ek) - pres(k, vk - hv, ek)) / (2.0 * hv);
+      const double dpde = (pres(k, vk, ek + he) - pres(k, vk, ek - he)) / (2.0 * he);
+      const double dvdx = k == 0 ? 1.0 / m[0] : -1.0 / m[1];
+      F[k] = p0 - ps;
+      Jx[k] = (dpdv - dpde * ps) * dvdx;
+      Jp[k] = -dpde * (vk - v[k]) - 1.0;
+    }
+    const double det = Jx[0] * Jp[1] - Jx[1] * Jp[0];
+    if (!(std::fabs(det) > 0.0) || !std::isfinite(det)) break;
+    double dx = (-F[0] * Jp[1] + F[1] * Jp[0]) / det, dp = (-Jx[0] * F[1] + Jx[1] * F[0]) / det;
+    for (int h = 0; h < 60 && !(x + dx > 0.0 && x + dx < 1.0); ++h) {
+      dx *= 0.5;
+      dp *= 0.5;
+    }
+    x += dx;
+    ps += dp;
+    done = std::fabs(dx) <= 1e-14 && std::fabs(dp) <= 1e-13 * pscale;
+  }
+  if (!done || !(x > 0.0 && x < 1.0) || !std::isfinite(ps)) return 8;  // not converged: left as it is
+  for (int k = 0; k < 2; ++k) {
+    const double ak = k == 0 ? x : 1.0 - x, vk = ak / m[k], ek = e0[k] - ps * (vk - v[k]);
+    const double lam = std::cbrt(vk / v[k]);
+    double* q = Q + 15 * k;
+    q[0] = ak;
+    q[5] = m[k] * (ek + ke[k]);
+    for (int c = 0; c < 9; ++c) q[6 + c] = q[6 + c] * lam;
+  }
+  return 0;
+}
+
 template <class PM> struct ProblemT {
   int model;
   BartonT<PM> eos[2];
@@ -719,6 +791,7 @@ template <class PM> struct ProblemT {
   int nx;
   double X;
   double cfl;
+  int relax = 0;  // two-phase pressure relaxation after each step (an extension: relax_pressure2)
 };
 using Problem = ProblemT<double>;
 inline int nvar_of(int model) { return model == MODEL_SINGLE ? 14 : 30; }
@@ -914,6 +987,12 @@ template <class T, class PM> T step(const ProblemT<PM>& pb, std::vector<T>& Q, i
       const T* dmr = &DM[(size_t)(i + 1) * nv];
       const T* dpl = &DP[(size_t)i * nv];
       for (int k = 0; k < nv; ++k) Q1[(size_t)i * nv + k] = q[k] - dtdx * ((Fr[k] - Fl[k]) + (dmr[k] + dpl[k]));
+    }
+  }
+  if constexpr (std::is_same<T, double>::value) {
+    if (pb.model == MODEL_MULTI && pb.relax) {
+#pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
+      for (int i = i0; i <= i1; ++i) relax_pressure2(pb.eos, &Q1[(size_t)i * nv]);
     }
   }
   Q.swap(Q1);

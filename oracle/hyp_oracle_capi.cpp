@@ -17,6 +17,7 @@ typedef struct {
   int model, flux, bc, nx;
   double X, cfl;
   hyo_eos eos[2];
+  int relax;
 } hyo_problem;
 
 static Barton to_barton(const hyo_eos* p) {
@@ -32,6 +33,7 @@ static Problem to_problem(const hyo_problem* p) {
   pb.nx = p->nx;
   pb.X = p->X;
   pb.cfl = p->cfl;
+  pb.relax = p->relax;
   return pb;
 }
 
@@ -249,6 +251,17 @@ int hyo_speeds_dir(const hyo_problem* p, const double* Q, const double* dir, dou
     GATHER(d, dir, 3, n, i);
     cell_speeds(pb, q, s, d);
     SCATTER(spd, s, ns, n, i);
+  }
+  return 0;
+}
+// The two-phase pressure relaxation of n cells (status per cell in st: 0 or 8).
+int hyo_relax(const hyo_problem* p, const double* Q, double* R, int* st, int64_t n) {
+  Problem pb = to_problem(p);
+  for (int64_t i = 0; i < n; ++i) {
+    double q[30];
+    GATHER(q, Q, 30, n, i);
+    st[i] = relax_pressure2(pb.eos, q);
+    SCATTER(R, q, 30, n, i);
   }
   return 0;
 }

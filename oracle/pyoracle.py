@@ -65,13 +65,14 @@ class Problem(ctypes.Structure):
         ("X", ctypes.c_double),
         ("cfl", ctypes.c_double),
         ("eos", Eos * 2),
+        ("relax", ctypes.c_int),
     ]
 
 
-def problem(model=MODEL_SINGLE, flux=FLUX_RUSANOV, bc=BC_FROZEN, nx=3, X=1.0, cfl=0.5, eos=None):
+def problem(model=MODEL_SINGLE, flux=FLUX_RUSANOV, bc=BC_FROZEN, nx=3, X=1.0, cfl=0.5, eos=None, relax=0):
     eos = eos if eos is not None else (barton2009(), barton2009())
     p = Problem()
-    p.model, p.flux, p.bc, p.nx, p.X, p.cfl = model, flux, bc, nx, X, cfl
+    p.model, p.flux, p.bc, p.nx, p.X, p.cfl, p.relax = model, flux, bc, nx, X, cfl, relax
     p.eos[0] = eos[0]
     p.eos[1] = eos[1]
     return p
@@ -111,6 +112,7 @@ def lib():
             "hyo_stress_den": [ep, dp, dp, dp, dp, i64],
             "hyo_acoustic_prim": [ep, dp, dp, dp, i64],
             "hyo_speeds_dir": [pp, dp, dp, dp, i64],
+            "hyo_relax": [pp, dp, dp, ctypes.POINTER(ctypes.c_int), i64],
             "hyo_cons2prim": [pp, dp, dp, i64],
             "hyo_prim2cons": [pp, dp, dp, i64],
             "hyo_flux": [pp, dp, dp, i64],
@@ -285,6 +287,16 @@ def speeds(pb, Q, n_dir=None):
     r = np.empty((6 if pb.model == MODEL_SINGLE else 12, n))
     lib().hyo_speeds_dir(ctypes.byref(pb), _ptr(q), _ptr(_dirs(n_dir, n)), _ptr(r), n)
     return _out(r, s)
+
+
+def relax(pb, Q):
+    """Two-phase pressure relaxation of cells (an extension; see hyp_oracle.hpp).
+    Returns (Q', status per cell: 0, or 8 when Newton did not converge)."""
+    q, n, s = _soa(Q, 30)
+    r = np.empty_like(q)
+    st = np.zeros(n, dtype=np.int32)
+    lib().hyo_relax(ctypes.byref(pb), _ptr(q), _ptr(r), st.ctypes.data_as(ctypes.POINTER(ctypes.c_int)), n)
+    return _out(r, s), (st[0] if s else st)
 
 
 def noncons(pb, Q):

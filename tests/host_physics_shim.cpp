@@ -4,6 +4,7 @@
 #include "../hyperelasticsolver_gb300/csrc/hyp_physics.cuh"
 #include "../hyperelasticsolver_gb300/csrc/hyp_adjoint.cuh"
 #include "../hyperelasticsolver_gb300/csrc/hyp_hank.cuh"
+#include "../hyperelasticsolver_gb300/csrc/hyp_relax.cuh"
 
 using namespace hyp;
 
@@ -19,6 +20,18 @@ void hs_stress(const double* ep, double S, const double* F, double* sig) { stres
 void hs_acoustic(const double* ep, double S, const double* F, double* om) { acoustic_SF(mk(ep), S, F, om); }
 double hs_spectral_radius(const double* a) { return spectral_radius(a); }
 void hs_eig_moduli3(const double* a, double* m) { eig_moduli3(a, m); }
+void hs_eig_sorted3(const double* a, double* m) { eig_sorted3(a, m); }
+// two-phase pressure relaxation of one cell in place (30 values); returns its status
+int hs_relax2(const double* ep1, const double* ep2, double* Q) {
+  EosC e[2] = {mk(ep1), mk(ep2)};
+  return relax_pressure2(e, Q);
+}
+// mean-stress pressure of one phase at e_int and distortion lam * A, and dp/de
+void hs_relax_pressure(const double* ep, const double* A, double lam, double eint, double* out) {
+  PhaseP r = relax_phase_pressure(mk(ep), A, lam, eint);
+  out[0] = r.p;
+  out[1] = r.dpde;
+}
 
 // one phase of a cell: q = [alpha, alpha*rho, alpha*rho*u(3), alpha*rho*E, alpha*rho*A(9)]
 // out: [flux(14 after alpha), u1, cmax, S, status]

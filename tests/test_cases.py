@@ -47,3 +47,19 @@ def test_batch_sizes_and_fill():
         left = np.arange(n) < n / 2  # (i - 1) < N/2 with 1-based i (main.jl:103)
         assert np.array_equal(Q[:, o:o + n][:, left], np.repeat(Pl[p][:, None], left.sum(), axis=1))
         assert np.array_equal(Q[:, o:o + n][:, ~left], np.repeat(Pr[p][:, None], (~left).sum(), axis=1))
+
+
+def test_thirteen_value_layout_round_trip():
+    """Hyperelasticity.jl's 13-value cell (rho u, rho F row-major, rho E) and the 14-value
+    layout: the round trip is exact and the density comes from det(rho F)."""
+    import hyperelasticsolver_gb300 as h
+    from hyperelasticsolver_gb300 import Hyperelasticity as H
+    rng = np.random.default_rng(1)
+    eos = h.Barton2009()
+    F = np.eye(3) + 0.05 * rng.standard_normal((3, 3))
+    rho = eos.rho0 / np.linalg.det(F)
+    q13 = np.concatenate([rho * rng.uniform(-1, 1, 3), (rho * F).reshape(-1), [rho * 0.7]])  # row-major rho F
+    q14 = H.q13_to_q14(eos, q13)
+    assert abs(q14[0] - rho) <= 1e-14 * rho
+    assert np.array_equal(q14[5:14].reshape(3, 3, order="F"), (rho * F))  # column-major 9-vector
+    assert np.array_equal(H.q14_to_q13(q14), q13)

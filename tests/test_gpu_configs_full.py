@@ -102,3 +102,29 @@ def test_adjoint_65536_cells_1000_steps():
     print(f"adjoint, 65536 cells x 1000 steps, checkpoints every 50: max rel vs central differences {rel.max():.2e}; "
           f"reverse pass {tm['ms_recompute'] + tm['ms_adjoint']:.1f} ms")
     assert rel.max() <= 1e-5, [(PARAM_NAMES[k], g[k], fd[k], rel[k]) for k in np.argsort(-rel)[:4]]
+
+
+def test_twophase_2p22_cells_300_steps_with_relaxation(hyp):
+    """The same two-phase workload with pressure relaxation after every step (an extension;
+    mixed relaxes in FP64): mixed against FP64, per-phase density L1 <= 1e-6."""
+    from hyperelasticsolver_gb300 import HyperelasticityMPh as HM
+    from hyperelasticsolver_gb300._cases import mph_interface_prims
+    eos = (hyp.Barton2009(), hyp.Barton2009(_b0=2.1 * np.sqrt(0.1)))
+    n, steps = 1 << 22, 300
+    Q0 = np.ascontiguousarray(HM.prim2cons_mph(eos, mph_interface_prims(eos[0], n)).T)
+    out = {}
+    for prec in ("mixed", "fp64"):
+        with hyp.Solver(eos, n, model="multi", flux="hll", precision=prec, cfl=0.5, relax="pressure") as s:
+            s.upload(Q0)
+            k, t = s.step(max_steps=steps)
+            assert k == steps
+            out[prec] = s.download()
+    errs = []
+    for p in range(2):
+        a, r = _phase_density(out["mixed"], p), _phase_density(out["fp64"], p)
+        errs.append(np.sum(np.abs(a - r)) / np.sum(np.abs(r)))
+    a1 = out["fp64"][0]
+    assert np.max(np.abs(out["fp64"][0] + out["fp64"][15] - 1.0)) <= 1e-12  # alpha1 + alpha2 = 1
+    print(f"two-phase 2^22 cells, {steps} HLL steps with relaxation: per-phase density L1 {errs[0]:.2e} / "
+          f"{errs[1]:.2e}; alpha1 range {a1.min():.3e} .. {a1.max():.3e}")
+    assert max(errs) <= L1_TARGET

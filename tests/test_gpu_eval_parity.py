@@ -243,3 +243,26 @@ def test_golden_function_forms_on_gpu(hyp, orc):
         sp = np.array(c["speeds"])
         got = H.get_eigvals(eos, np.array(c["Q"])[1:], c["n"])
         assert np.max(np.abs(got - sp)) <= RTOL_FP64 * np.max(np.abs(sp)), "golden get_eigvals along n"
+
+
+def test_thirteen_value_forms(hyp, orc):
+    """Hyperelasticity.jl's 13-value cons2prim / prim2cons / flux (:25-114) with the eos
+    passed in, against the oracle's per-phase functions at alpha = 1 (the 14-value model
+    the reference's solver runs), reordered to the 13-value layout."""
+    from hyperelasticsolver_gb300 import Hyperelasticity as H
+    rng = np.random.default_rng(18)
+    eos, pb = hyp.Barton2009(), orc.problem()
+    P14 = random_prims1(rng, 50)
+    Q14 = orc.prim2cons(pb, P14)
+    Q13 = H.q14_to_q13(Q14)
+    F = P14[:, 5:].reshape(-1, 3, 3).transpose(0, 2, 1)  # [i][j] = F[i, j]
+    assert_close(H.prim2cons13(eos, P14[:, 1:4], F, P14[:, 4]), Q13, RTOL_FP64, "prim2cons13")
+    den, vel, F13, e_int = H.cons2prim13(eos, Q13)
+    Po = orc.cons2prim(pb, Q14)
+    assert_close(den, Po[:, 0], RTOL_FP64, "den")
+    assert_close(vel, Po[:, 1:4], RTOL_FP64, "vel")
+    assert_close(F13, F, RTOL_FP64, "F")
+    f13 = H.flux13(eos, Q13)
+    fo = H.q14_to_q13(orc.flux(pb, Q14))
+    assert_close(f13, fo, RTOL_FP64, "flux13")
+    assert np.all(f13[:, 3:6] == 0.0)  # the rho F row-1 flux is identically zero (Hyperelasticity.jl:106)
