@@ -54,10 +54,15 @@ def initial_states(eos, testcase):
     return Ql, Qr
 
 
-def relax_pressure(eos, Q):
+def relax_pressure(eos, Q, velocity=False):
     """Instantaneous pressure relaxation of two-phase cells (hyp_eval_relax): volume
     fractions moved until both phases' mean-stress pressures agree, energies by
-    de = -p* dv, distortions scaled in their volumetric part. An extension (the
-    reference has no relaxation terms); cells with a phase below 1e-5 come back as they
-    are, a cell whose Newton iteration does not converge as NaN."""
-    return M.call("hyp_eval_relax", _cfg(eos), Q, 30, 30)
+    de = -p* dv, distortions scaled in their volumetric part; velocity=True relaxes the
+    velocities to the mixture velocity first. An extension (the reference has no
+    relaxation terms); cells with a phase below 1e-5 come back as they are, a cell whose
+    Newton iteration does not converge as NaN."""
+    x, n, single = L.soa(Q, 30)
+    out = np.empty((30, n))
+    mode = L.HYP_RELAX_MECHANICAL if velocity else L.HYP_RELAX_PRESSURE
+    L.check(L.load().hyp_eval_relax(_cfg(eos), mode, L.ptr(x), L.ptr(out), n), what="hyp_eval_relax")
+    return L.unsoa(out, single)

@@ -23,7 +23,7 @@ HYP_MODEL_SINGLE, HYP_MODEL_MULTI = 1, 2
 HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = 0, 1, 2
 HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = 0, 1
 HYP_PREC_FP64, HYP_PREC_MIXED = 0, 1
-HYP_RELAX_NONE, HYP_RELAX_PRESSURE = 0, 1
+HYP_RELAX_NONE, HYP_RELAX_PRESSURE, HYP_RELAX_MECHANICAL = 0, 1, 2
 HYP_BATCH_NUM_VARIANTS = 6
 
 
@@ -98,7 +98,7 @@ _SIGS = {
     "hyp_step_noalloc_f64": ([ctypes.POINTER(ConfigC), ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int,
                               ctypes.c_double, ctypes.c_void_p, _dp, ctypes.POINTER(ctypes.c_int64)], ctypes.c_int),
     "hyp_set_relaxation": ([ctypes.c_void_p, ctypes.c_int], ctypes.c_int),
-    "hyp_eval_relax": ([ctypes.POINTER(ConfigC), _dp, _dp, _i64], ctypes.c_int),
+    "hyp_eval_relax": ([ctypes.POINTER(ConfigC), ctypes.c_int, _dp, _dp, _i64], ctypes.c_int),
     "hyp_set_slab": ([ctypes.c_void_p, ctypes.c_double, ctypes.c_int, ctypes.c_int], ctypes.c_int),
     "hyp_slab_local_max": ([ctypes.c_void_p, _dp], ctypes.c_int),
     "hyp_slab_step": ([ctypes.c_void_p, ctypes.c_double, _dp], ctypes.c_int),

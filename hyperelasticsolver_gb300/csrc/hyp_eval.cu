@@ -517,22 +517,27 @@ extern "C" int hyp_eval_hll_eigvals(const hyp_config* cfg, const double* Ql, con
 
 // ---- two-phase pressure relaxation (hyp_relax.cuh) --------------------------
 namespace {
-__global__ void k_relax(ModelArg m, const double* Q, double* R, int64_t n) {
+struct RelaxArg {
+  ModelArg m;
+  int mode;
+};
+__global__ void k_relax(RelaxArg a, const double* Q, double* R, int64_t n) {
   IDX double q[30];
   LD(q, Q, 30);
-  if (relax_pressure2(m.e, q)) {
+  if (relax_cell2(a.m.e, a.mode, q)) {
     for (int c = 0; c < 30; ++c) q[c] = NAN;  // not converged
   }
   ST(R, q, 30);
 }
 }  // namespace
 
-extern "C" int hyp_eval_relax(const hyp_config* cfg, const double* Q, double* Q_out, int64_t n) {
+extern "C" int hyp_eval_relax(const hyp_config* cfg, int mode, const double* Q, double* Q_out, int64_t n) {
   if (!model_ok(cfg) || cfg->model != HYP_MODEL_MULTI) return HYP_ERR_INVALID;
-  ModelArg m = model_arg(cfg);
+  if (mode != HYP_RELAX_PRESSURE && mode != HYP_RELAX_MECHANICAL) return HYP_ERR_INVALID;
+  RelaxArg a{model_arg(cfg), mode};
   return run(n, {{Q, nullptr, 30}, {nullptr, Q_out, 30}},
-             [](int64_t n, double** d, const void* a) {
-               k_relax<<<grid(n), kBlock>>>(*(const ModelArg*)a, d[0], d[1], n);
+             [](int64_t n, double** d, const void* p) {
+               k_relax<<<grid(n), kBlock>>>(*(const RelaxArg*)p, d[0], d[1], n);
              },
-             &m);
+             &a);
 }

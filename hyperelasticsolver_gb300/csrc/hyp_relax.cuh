@@ -1,4 +1,5 @@
-// hyp_relax.cuh -- instantaneous pressure relaxation of a two-phase cell (FP64).
+// hyp_relax.cuh -- instantaneous pressure (and velocity) relaxation of a two-phase
+// cell (FP64).
 //
 // The reference's two-phase model (HyperelasticityMPh.jl) carries two volume
 // fractions, velocities and distortions per cell and has no relaxation terms; this
@@ -23,7 +24,10 @@
 // Conserved: each phase's mass and momentum, the mixture's total energy
 // (sum_k m_k (e_k' - e_k) = -p* sum_k (alpha_k' - alpha_k) = 0), alpha_1 + alpha_2.
 // A cell with a phase below kRelaxMinAlpha is left as it is (a vanishing phase has no
-// weight in the mixture and its relaxation is ill-conditioned).
+// weight in the mixture and its relaxation is ill-conditioned). HYP_RELAX_MECHANICAL
+// relaxes the velocities first (relax_velocity2): at a diffuse interface pressure
+// relaxation alone let the two velocities drift apart and the minority phase's
+// density collapse within 100 steps of the 8-cell smoothed interface.
 #pragma once
 #include "hyp_physics.cuh"
 
@@ -57,8 +61,44 @@ HYP_HD PhaseP relax_phase_pressure(const EosC& e, const double* A, double lam, d
   return r;
 }
 
+// Instantaneous velocity relaxation of one two-phase cell in place: both phases take
+// the mixture velocity u* = sum m_k u_k / sum m_k (m_k = alpha_k rho_k); a phase's
+// momentum becomes m_k u* and its total energy changes by m_k u* . (u* - u_k), which
+// keeps the mixture's momentum and total energy and adds |u_k - u*|^2 / 2 to each
+// phase's internal energy (the drag's dissipation). Applied before the pressure
+// relaxation, it brings the cell to mechanical equilibrium (one velocity, one
+// pressure), which the two-velocity model needs at a diffuse interface: pressure
+// relaxation alone lets the phases' velocities drift apart there.
+HYP_HD int relax_velocity2(const EosC* eos, double* Q) {
+  Prim P[2];
+  int st = 0;
+  for (int k = 0; k < 2; ++k) st |= cons_to_prim(eos[k], Q[15 * k], Q + 15 * k + 2, Q[15 * k + 5], Q + 15 * k + 6, P[k]);
+  if (st) return st;
+  if (!(Q[0] >= kRelaxMinAlpha && Q[15] >= kRelaxMinAlpha)) return 0;
+  const double m0 = P[0].den, m1 = P[1].den, im = 1.0 / (m0 + m1);
+  double us[3];
+  for (int c = 0; c < 3; ++c) us[c] = (m0 * P[0].u[c] + m1 * P[1].u[c]) * im;
+  for (int k = 0; k < 2; ++k) {
+    double* q = Q + 15 * k;
+    const double m = P[k].den;
+    const double w = us[0] * (us[0] - P[k].u[0]) + us[1] * (us[1] - P[k].u[1]) + us[2] * (us[2] - P[k].u[2]);
+    q[5] = q[5] + m * w;
+    for (int c = 0; c < 3; ++c) q[2 + c] = m * us[c];
+  }
+  return 0;
+}
+
 // Relax one two-phase cell in place (30 conservative values, HyperelasticityMPh.jl:80-84).
 // Returns HYP_CELL_* bits; 0 also when the cell is left as it is.
+HYP_HD int relax_pressure2(const EosC* eos, double* Q);
+// The relaxation of a hyp_set_relaxation mode: 1 pressure, 2 velocity then pressure.
+HYP_HD int relax_cell2(const EosC* eos, int mode, double* Q) {
+  if (mode == 2) {
+    const int st = relax_velocity2(eos, Q);
+    if (st) return st;
+  }
+  return relax_pressure2(eos, Q);
+}
 HYP_HD int relax_pressure2(const EosC* eos, double* Q) {
   Prim P[2];
   int st = 0;

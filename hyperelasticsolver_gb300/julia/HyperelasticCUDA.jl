@@ -34,6 +34,7 @@ const HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = Cint(0), Cint(1), Cint(2)
 const HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = Cint(0), Cint(1)
 const HYP_RELAX_NONE = Cint(0)
 const HYP_RELAX_PRESSURE = Cint(1)
+const HYP_RELAX_MECHANICAL = Cint(2)
 const HYP_PREC_FP64, HYP_PREC_MIXED = Cint(0), Cint(1)
 
 struct HypError <: Exception
@@ -313,14 +314,15 @@ initial_condition_tanh!(s::Solver, Ql::Vector{Float64}, Qr::Vector{Float64}, eps
         "hyp_init_tanh", s.h)
 
 # ---- two-phase pressure relaxation (an extension: the reference has none) ----
-"set_relaxation!(s, mode): HYP_RELAX_NONE (default) or HYP_RELAX_PRESSURE after each two-phase step"
+"set_relaxation!(s, mode): HYP_RELAX_NONE (default), HYP_RELAX_PRESSURE or HYP_RELAX_MECHANICAL after each two-phase step"
 set_relaxation!(s::Solver, mode::Integer) =
   check(ccall((:hyp_set_relaxation, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, mode), "hyp_set_relaxation", s.h)
-"relax_pressure(eos, Q): instantaneous pressure relaxation of two-phase cells (n, 30)"
-function relax_pressure(eos::Tuple, Q::Matrix{Float64})
+"relax_pressure(eos, Q; velocity=false): instantaneous (velocity and) pressure relaxation of two-phase cells (n, 30)"
+function relax_pressure(eos::Tuple, Q::Matrix{Float64}; velocity::Bool=false)
   out = similar(Q)
-  check(ccall((:hyp_eval_relax, libhyp), Cint, (Ref{ConfigC}, Ptr{Float64}, Ptr{Float64}, Int64),
-              Ref(config(eos, HYP_MODEL_MULTI)), Q, out, size(Q, 1)), "relax_pressure")
+  check(ccall((:hyp_eval_relax, libhyp), Cint, (Ref{ConfigC}, Cint, Ptr{Float64}, Ptr{Float64}, Int64),
+              Ref(config(eos, HYP_MODEL_MULTI)), velocity ? HYP_RELAX_MECHANICAL : HYP_RELAX_PRESSURE, Q, out,
+              size(Q, 1)), "relax_pressure")
   out
 end
 

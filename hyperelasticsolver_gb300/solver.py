@@ -36,9 +36,11 @@ class Solver:
             self.set_relaxation(relax)
 
     def set_relaxation(self, mode):
-        """Two-phase pressure relaxation after each step: "pressure", or None (the reference's
-        model, the default). An extension: the reference has no relaxation terms."""
-        m = {None: L.HYP_RELAX_NONE, "none": L.HYP_RELAX_NONE, "pressure": L.HYP_RELAX_PRESSURE}[mode]
+        """Two-phase relaxation after each step: "pressure", "mechanical" (velocity, then
+        pressure), or None (the reference's model, the default). An extension: the
+        reference has no relaxation terms."""
+        m = {None: L.HYP_RELAX_NONE, "none": L.HYP_RELAX_NONE, "pressure": L.HYP_RELAX_PRESSURE,
+             "mechanical": L.HYP_RELAX_MECHANICAL}[mode]
         L.check(L.load().hyp_set_relaxation(self._h, m), self._h, "hyp_set_relaxation")
 
     def close(self):

@@ -52,8 +52,9 @@ enum { HYP_BC_FROZEN = 0, HYP_BC_TRANSMISSIVE = 1 };
 /* arithmetic: plain FP64, or FP32 fluxes with a compensated hi/lo FP32 state */
 enum { HYP_PREC_FP64 = 0, HYP_PREC_MIXED = 1 };
 /* two-phase relaxation after each step (hyp_set_relaxation): none (the reference's
-   model), or instantaneous pressure relaxation */
-enum { HYP_RELAX_NONE = 0, HYP_RELAX_PRESSURE = 1 };
+   model), instantaneous pressure relaxation, or velocity then pressure relaxation
+   (mechanical equilibrium) */
+enum { HYP_RELAX_NONE = 0, HYP_RELAX_PRESSURE = 1, HYP_RELAX_MECHANICAL = 2 };
 
 /* Barton2009 primary parameters (EquationsOfState.jl:71-116); b0sq and k0 are derived.
    Defaults of the reference constructor: 8.93, 4.6, 3.9e-4, 300, 2.1, 1, 3, 2. */
@@ -109,13 +110,20 @@ int hyp_set_eos(hyp_ctx* ctx, int phase, const hyp_barton2009* eos);
    Favrie, Gavrilyuk & Saurel 2009 treat them: volume fractions move until both
    phases' mean-stress pressures agree, each phase's internal energy follows
    de = -p* dv and its distortion changes in its volumetric part only; each phase's
-   mass and momentum and the mixture's total energy are conserved. Cells with a phase
-   below 1e-5 are left as they are; with frozen ends the end cells too. Mixed
-   contexts relax in FP64. A cell that does not converge is left unrelaxed and the
-   step returns HYP_ERR_NONFINITE with its index. */
+   mass and momentum and the mixture's total energy are conserved.
+   HYP_RELAX_MECHANICAL first relaxes the velocities: both phases take the mixture
+   velocity, each phase's total energy changing by m u* . (u* - u) so that the
+   mixture's momentum and energy are kept; pressure relaxation alone lets the phases'
+   velocities drift apart at a diffuse interface (on the smoothed-interface workload
+   of 2^22 cells the minority phase's density then collapsed within 100 steps).
+   Cells with a phase below 1e-5 are left as they are; with frozen ends the end cells
+   too. Mixed contexts relax in FP64. A cell that does not converge is left
+   unrelaxed and the step returns HYP_ERR_NONFINITE with its index. */
 int hyp_set_relaxation(hyp_ctx* ctx, int mode);
-/* The same relaxation of n two-phase cells (function level).  Q, Q_out: [30][n] */
-int hyp_eval_relax(const hyp_config* cfg, const double* Q, double* Q_out, int64_t n);
+/* The same relaxation (mode HYP_RELAX_PRESSURE or HYP_RELAX_MECHANICAL) of n two-phase
+   cells (function level).  Q, Q_out: [30][n]; a cell that does not converge comes
+   back as NaN. */
+int hyp_eval_relax(const hyp_config* cfg, int mode, const double* Q, double* Q_out, int64_t n);
 /* hyp_step (max_steps >= 1) that also returns the time after every step taken,
    t_hist[0 .. *steps_done - 1] (host, max_steps entries): the Step / t / dt line
    main.jl:229-237 logs each step, read back once at the end rather than with a

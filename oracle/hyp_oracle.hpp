@@ -727,6 +727,26 @@ inline double relax_pressure_of(const Barton& e, const double* A, double lam, do
   stress(e, S, As, sig);
   return -(M3(sig, 0, 0) + M3(sig, 1, 1) + M3(sig, 2, 2)) / 3.0;
 }
+// Instantaneous velocity relaxation: both phases take the mixture velocity
+// u* = sum m_k u_k / sum m_k; each phase's momentum becomes m_k u*, its total energy
+// changes by m_k u* . (u* - u_k), so the mixture's momentum and energy are kept and
+// each phase's internal energy grows by |u_k - u*|^2 / 2.
+inline void relax_velocity2(const Barton* eos, double* Q) {
+  double P[2][15], m[2];
+  for (int k = 0; k < 2; ++k) {
+    cons2prim(eos[k], Q + 15 * k, P[k]);
+    m[k] = P[k][0] * P[k][1];
+  }
+  double us[3];
+  for (int c = 0; c < 3; ++c) us[c] = (m[0] * P[0][2 + c] + m[1] * P[1][2 + c]) / (m[0] + m[1]);
+  for (int k = 0; k < 2; ++k) {
+    double* q = Q + 15 * k;
+    double w = 0.0;
+    for (int c = 0; c < 3; ++c) w += us[c] * (us[c] - P[k][2 + c]);
+    q[5] = q[5] + m[k] * w;
+    for (int c = 0; c < 3; ++c) q[2 + c] = m[k] * us[c];
+  }
+}
 inline int relax_pressure2(const Barton* eos, double* Q) {
   constexpr double kMinAlpha = 1e-5;
   double P[2][15], m[2], v[2], a0[2] = {Q[0], Q[15]};
@@ -992,7 +1012,11 @@ template <class T, class PM> T step(const ProblemT<PM>& pb, std::vector<T>& Q, i
   if constexpr (std::is_same<T, double>::value) {
     if (pb.model == MODEL_MULTI && pb.relax) {
 #pragma omp parallel for num_threads(nthreads) schedule(dynamic, 64)
-      for (int i = i0; i <= i1; ++i) relax_pressure2(pb.eos, &Q1[(size_t)i * nv]);
+      for (int i = i0; i <= i1; ++i) {
+        double* q = &Q1[(size_t)i * nv];
+        if (pb.relax == 2 && q[0] >= 1e-5 && q[15] >= 1e-5) relax_velocity2(pb.eos, q);
+        relax_pressure2(pb.eos, q);
+      }
     }
   }
   Q.swap(Q1);

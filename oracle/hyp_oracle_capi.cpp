@@ -254,12 +254,14 @@ int hyo_speeds_dir(const hyo_problem* p, const double* Q, const double* dir, dou
   }
   return 0;
 }
-// The two-phase pressure relaxation of n cells (status per cell in st: 0 or 8).
+// The two-phase relaxation of n cells: pressure, after the velocities when
+// p->relax == 2 (status per cell in st: 0 or 8).
 int hyo_relax(const hyo_problem* p, const double* Q, double* R, int* st, int64_t n) {
   Problem pb = to_problem(p);
   for (int64_t i = 0; i < n; ++i) {
     double q[30];
     GATHER(q, Q, 30, n, i);
+    if (pb.relax == 2 && q[0] >= 1e-5 && q[15] >= 1e-5) relax_velocity2(pb.eos, q);
     st[i] = relax_pressure2(pb.eos, q);
     SCATTER(R, q, 30, n, i);
   }

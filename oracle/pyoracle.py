@@ -290,7 +290,8 @@ def speeds(pb, Q, n_dir=None):
 
 
 def relax(pb, Q):
-    """Two-phase pressure relaxation of cells (an extension; see hyp_oracle.hpp).
+    """Two-phase pressure relaxation of cells (an extension; see hyp_oracle.hpp), the
+    velocities relaxed first when pb.relax == 2.
     Returns (Q', status per cell: 0, or 8 when Newton did not converge)."""
     q, n, s = _soa(Q, 30)
     r = np.empty_like(q)

@@ -105,8 +105,8 @@ def test_adjoint_65536_cells_1000_steps():
 
 
 def test_twophase_2p22_cells_300_steps_with_relaxation(hyp):
-    """The same two-phase workload with pressure relaxation after every step (an extension;
-    mixed relaxes in FP64): mixed against FP64, per-phase density L1 <= 1e-6."""
+    """The same two-phase workload with velocity and pressure relaxation after every step
+    (an extension; mixed relaxes in FP64): mixed against FP64, per-phase density L1 <= 1e-6."""
     from hyperelasticsolver_gb300 import HyperelasticityMPh as HM
     from hyperelasticsolver_gb300._cases import mph_interface_prims
     eos = (hyp.Barton2009(), hyp.Barton2009(_b0=2.1 * np.sqrt(0.1)))
@@ -114,7 +114,7 @@ def test_twophase_2p22_cells_300_steps_with_relaxation(hyp):
     Q0 = np.ascontiguousarray(HM.prim2cons_mph(eos, mph_interface_prims(eos[0], n)).T)
     out = {}
     for prec in ("mixed", "fp64"):
-        with hyp.Solver(eos, n, model="multi", flux="hll", precision=prec, cfl=0.5, relax="pressure") as s:
+        with hyp.Solver(eos, n, model="multi", flux="hll", precision=prec, cfl=0.5, relax="mechanical") as s:
             s.upload(Q0)
             k, t = s.step(max_steps=steps)
             assert k == steps

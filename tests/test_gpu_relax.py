@@ -15,28 +15,31 @@ def eos_pair(hyp):
     return (hyp.Barton2009(), hyp.Barton2009(_b0=B0_SOFT))
 
 
-def test_relax_evaluator_matches_oracle(hyp, orc):
+@pytest.mark.parametrize("velocity", [False, True])
+def test_relax_evaluator_matches_oracle(hyp, orc, velocity):
     from hyperelasticsolver_gb300 import HyperelasticityMPh as HM
     Q = _states(orc, 64, seed=21)
-    got = HM.relax_pressure(eos_pair(hyp), Q)
-    ref, st = orc.relax(_pb(orc), Q)
+    got = HM.relax_pressure(eos_pair(hyp), Q, velocity=velocity)
+    pb = _pb(orc, relax=2 if velocity else 1)
+    ref, st = orc.relax(pb, Q)
     assert np.all(st == 0) and np.all(np.isfinite(got))
-    sens = ulp_sensitivity(lambda q: orc.relax(_pb(orc), q)[0], (Q,))
+    sens = ulp_sensitivity(lambda q: orc.relax(pb, q)[0], (Q,))
     assert_within_sensitivity(got, ref, sens, RTOL_FP64, "relaxed cells", axis=0)
     p = _pressures(orc, got)
     assert np.max(np.abs(p[:, 0] - p[:, 1]) / np.abs(p).max(axis=1).clip(1e-2)) <= 1e-10
 
 
+@pytest.mark.parametrize("mode", ["pressure", "mechanical"])
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
 @pytest.mark.parametrize("testcase", [4, 6])
-def test_step_with_relaxation(hyp, orc, precision, testcase):
+def test_step_with_relaxation(hyp, orc, precision, testcase, mode):
     """The reference's two-phase test cases smoothed over 8 cells (so that interface cells
     hold both phases), 30 HLL steps with relaxation after each: FP64 against the oracle
     run with the same relaxation, mixed against FP64 (density L1 per phase <= 1e-6)."""
     from hyperelasticsolver_gb300._cases import mph_case
     nx, steps = 128, 30
     Pl, Pr = mph_case(testcase)
-    pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, nx=nx, cfl=0.5, relax=1,
+    pb = orc.problem(model=orc.MODEL_MULTI, flux=orc.FLUX_HLL, nx=nx, cfl=0.5, relax=2 if mode == "mechanical" else 1,
                      eos=(orc.barton2009(), orc.barton2009(b0=B0_SOFT)))
     x = (np.arange(nx) + 0.5) / nx
     w = 0.5 * (1 - np.tanh((x - 0.5) * nx / 4))[:, None]
@@ -45,7 +48,7 @@ def test_step_with_relaxation(hyp, orc, precision, testcase):
     Q0 = np.ascontiguousarray(orc.prim2cons(pb, P).T)
     Qo, so, to, _ = orc.run(pb, Q0, max_steps=steps)
     with hyp.Solver(eos_pair(hyp), nx, model="multi", flux="hll", cfl=0.5, precision=precision,
-                    relax="pressure") as s:
+                    relax=mode) as s:
         s.upload(Q0)
         n, t = s.step(max_steps=steps)
         assert n == steps
