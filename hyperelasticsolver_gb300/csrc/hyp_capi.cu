@@ -120,6 +120,9 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
     // state [2 parities][30 hi + 30 lo rows][pitch] floats; a parity's block also stages
     // FP64 uploads and downloads (30 pitch doubles >= 30 n)
     c->mpitch = mixed_pitch(c->n);
+    // phases as packed FP32 pairs in the face kernels: 2.72 against 2.89 ms per HLL step
+    // (1.51 against 1.58 LxF) at 2^22 cells on GB300
+    c->mixed_kind = HYP_MIXED_PAIR;
     const size_t nf4 = (size_t)30 * (c->n + 1) * sizeof(float);
     if ((e = cudaMalloc(&c->mixed_base, (size_t)2 * 60 * c->mpitch * sizeof(float))) != cudaSuccess)
       fail(e, "cudaMalloc(mixed state)");
@@ -550,12 +553,14 @@ extern "C" int hyp_set_wait_limit(hyp_ctx* c, int tries) {
   return HYP_OK;
 }
 
-extern "C" int hyp_set_mixed_kernel(hyp_ctx* c, int tma) {
+extern "C" int hyp_set_mixed_kernel(hyp_ctx* c, int kind) {
   if (!c) return HYP_ERR_INVALID;
-  if (!mixed(c) || c->cfg.model != HYP_MODEL_SINGLE)
-    return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: single-phase mixed-precision contexts only");
-  if (tma && !c->tma_grid) return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: TMA is not available");
-  c->mixed_tma = tma ? 1 : 0;
+  if (!mixed(c)) return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: mixed-precision contexts only");
+  if (kind != HYP_MIXED_TILE && kind != HYP_MIXED_TMA && kind != HYP_MIXED_PAIR)
+    return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: unknown kernel kind");
+  if (kind == HYP_MIXED_TMA && (c->cfg.model != HYP_MODEL_SINGLE || !c->tma_grid))
+    return set_err(c, HYP_ERR_UNSUPPORTED, "hyp_set_mixed_kernel: TMA is not available");
+  c->mixed_kind = kind;
   for (auto& g : c->graph)  // graphs hold the previous kernel
     if (g) {
       cudaGraphExecDestroy(g);

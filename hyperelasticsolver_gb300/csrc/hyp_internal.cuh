@@ -148,7 +148,7 @@ struct hyp_ctx {
   float* mixed_base = nullptr;          // one allocation [2 parities][32 rows][mpitch] holding all of the above
   int64_t mpitch = 0;                   // row pitch (floats, a multiple of 4)
   CUtensorMap tmap;                     // TMA map over mixed_base (both parities)
-  int mixed_tma = 0;                    // step with the TMA-prefetched persistent kernel
+  int mixed_kind = HYP_MIXED_TILE;      // kernel family (hyp_set_mixed_kernel)
   int wait_tries = hyp::kWaitTries;     // poll budget of the TMA kernel's barrier waits
   int tma_grid = 0;
   hyp::EosMixed eos_mixed;

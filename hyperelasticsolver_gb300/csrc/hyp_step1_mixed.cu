@@ -14,14 +14,19 @@
 // The three max-lambda slots rotate (read k%3, write (k+1)%3, clear (k+2)%3)
 // so one launch per step needs no separate reset.
 //
-// Two kernels run the same tile body:
+// Three kernels run the same tile arithmetic:
 //   step1_mixed_kernel      one block per tile, each thread loading its cell;
+//   step1_mixed_pair_kernel one block per two adjacent tiles of 126 cells, thread j
+//                           holding local cell j of both in the lanes of packed
+//                           FP32 pairs (hyp_mixed_pair.cuh), so one instruction
+//                           advances two cells;
 //   step1_mixed_tma_kernel  a persistent grid; thread 0 of a block prefetches
 //                           the block's next tile (all 32 rows of its cells) with
 //                           2D TMA boxes into shared memory while the block
 //                           computes the current tile from its copy, so loads
 //                           overlap compute.
 #include "hyp_internal.cuh"
+#include "hyp_mixed_pair.cuh"
 #include "hyp_mixed_tile.cuh"
 
 namespace hyp {
@@ -65,6 +70,148 @@ __global__ void __launch_bounds__(kBlock, 4)
   const int64_t i = first - 1 + threadIdx.x;
   if (i < a.own_lo || i >= a.own_hi) l = 0.0f;  // a slab's ghost cells: their owner reports them
   const float m = mixed_block_max<kBlock>(l);
+  if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
+}
+
+// ---- two tiles per block in packed FP32 pairs ----------------------------------
+
+constexpr int kPairBlock = 128;
+
+// Tiles 2b (lane x) and 2b + 1 (lane y) of BLOCK - 2 cells each: the phases of
+// mixed_tile_run (cell fluxes from the cached islands, faces, compensated update,
+// islands and wave speed of the new state) with every value a pair. A lane whose
+// cell is held (frozen end, slab ghost) keeps its state, lambda and islands.
+template <int BLOCK>
+__global__ void __launch_bounds__(BLOCK, 4)
+    step1_mixed_pair_kernel(MixedArrays a, EosMixed em, MixedSlots sl, DevState* S, double t_end, double cfl,
+                            double dx, int flux, int bc) {
+  constexpr int M = BLOCK - 2;
+  __shared__ float2 sFF[14][BLOCK];  // cell fluxes (11 slots), then the face fluxes (14)
+  __shared__ float2 sQ[14][BLOCK];
+  __shared__ float2 sL[BLOCK];
+  const int64_t n = a.stride, hi = a.n;
+  const int j = threadIdx.x;
+  const int64_t firstA = (int64_t)blockIdx.x * (2 * M);
+  const int64_t iA = firstA - 1 + j, iB = iA + M;  // this thread's cells (halo at j = 0, BLOCK - 1)
+  const int64_t cA = iA < 0 ? 0 : (iA >= hi ? hi - 1 : iA), cB = iB >= hi ? hi - 1 : iB;
+  float2 qh[14], ql[14];
+#pragma unroll
+  for (int v = 0; v < 14; ++v) {
+    qh[v] = make_float2(a.Qh[v * n + cA], a.Qh[v * n + cB]);
+    ql[v] = make_float2(a.Ql[v * n + cA], a.Ql[v * n + cB]);
+  }
+  const float2 li = make_float2(a.lam[cA], a.lam[cB]);
+  IslandsP I0;
+  I0.ir = make_float2(a.isl[cA], a.isl[cB]);
+  I0.e_int = make_float2(a.isl[n + cA], a.isl[n + cB]);
+  I0.sm1 = make_float2(a.isl[2 * n + cA], a.isl[2 * n + cB]);
+  float dtdx;
+  if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
+  const bool inner = j > 0 && j < BLOCK - 1;
+  float2 f11[kNFlux1];
+  {
+    PrimP P;
+    const int st = prim_from_islands_pair(em, qh, ql, I0, P);
+    const CoefP sc = stress_coeffs_pair(em.f, P);
+    flux_pair(qh, P, sc, f11);
+#pragma unroll
+    for (int s = 0; s < kNFlux1; ++s) sFF[s][j] = f11[s];
+#pragma unroll
+    for (int v = 0; v < 14; ++v) sQ[v][j] = qh[v];
+    sL[j] = li;
+    if (inner && (st & 0xff) && iA == cA) mixed_record_err(S, st & 0xff, iA);
+    if (inner && (st >> 8) && iB == cB) mixed_record_err(S, st >> 8, iB);
+  }
+  __syncthreads();
+  // face j + 1/2 between local cells j (registers) and j + 1 (shared memory)
+  float2 fv[14];
+  if (j < BLOCK - 1) {
+    const float2 lr = sL[j + 1];
+    const float2 lf = flux == HYP_FLUX_LXF ? f2s(1.0f / dtdx) : f2max(li, lr);
+    const float2 nhl = f2mul(f2s(-0.5f), lf);
+#pragma unroll
+    for (int v = 0; v < 14; ++v) {
+      const int s = flux_slot1(v);
+      const float2 sum = s >= 0 ? f2add(f11[s], sFF[s][j + 1]) : f2s(0.0f);
+      fv[v] = f2fma(nhl, f2sub(sQ[v][j + 1], qh[v]), f2mul(f2s(0.5f), sum));
+    }
+  }
+  __syncthreads();
+  if (j < BLOCK - 1) {
+#pragma unroll
+    for (int v = 0; v < 14; ++v) sFF[v][j] = fv[v];
+  }
+  __syncthreads();
+  float lA = 0.0f, lB = 0.0f;
+  const bool ownA = inner && iA < hi, ownB = inner && iB < hi;
+  if (ownA || ownB) {
+    const bool holdA = bc_holds(bc, iA == 0, iA == hi - 1), holdB = !ownB || bc_holds(bc, false, iB == hi - 1);
+    const float2 ndt = f2s(-dtdx);
+#pragma unroll
+    for (int v = 0; v < 14; ++v) {
+      const float2 delta = f2mul(ndt, f2sub(fv[v], sFF[v][j - 1]));  // F_{j+1/2} - F_{j-1/2}
+      const ff2 q = ff2_add_f(ff2{qh[v], ql[v]}, delta);
+      if (!holdA) {
+        qh[v].x = q.hi.x;
+        ql[v].x = q.lo.x;
+      }
+      if (!holdB) {
+        qh[v].y = q.hi.y;
+        ql[v].y = q.lo.y;
+      }
+    }
+    IslandsP I;
+    int st = islands_pair(em, qh, ql, I);
+    PrimP P;
+    st |= prim_from_islands_pair(em, qh, ql, I, P);
+    const CoefP sc = stress_coeffs_pair(em.f, P);
+    const float2 lnew = lambda_pair(em, P, sc);
+    st |= lane_status(!(lnew.x <= 3.0e38f), !(lnew.y <= 3.0e38f), HYP_CELL_NONFINITE);
+    if (holdA) {
+      lA = li.x;
+      I.ir.x = I0.ir.x;
+      I.e_int.x = I0.e_int.x;
+      I.sm1.x = I0.sm1.x;
+    } else {
+      lA = lnew.x;
+      if (ownA && (st & 0xff)) mixed_record_err(S, st & 0xff, iA);
+    }
+    if (holdB) {
+      lB = li.y;
+      I.ir.y = I0.ir.y;
+      I.e_int.y = I0.e_int.y;
+      I.sm1.y = I0.sm1.y;
+    } else {
+      lB = lnew.y;
+      if (st >> 8) mixed_record_err(S, st >> 8, iB);
+    }
+    if (ownA) {
+#pragma unroll
+      for (int v = 0; v < 14; ++v) {
+        a.Qh_out[v * n + iA] = qh[v].x;
+        a.Ql_out[v * n + iA] = ql[v].x;
+      }
+      a.lam_out[iA] = lA;
+      a.isl_out[iA] = I.ir.x;
+      a.isl_out[n + iA] = I.e_int.x;
+      a.isl_out[2 * n + iA] = I.sm1.x;
+    }
+    if (ownB) {
+#pragma unroll
+      for (int v = 0; v < 14; ++v) {
+        a.Qh_out[v * n + iB] = qh[v].y;
+        a.Ql_out[v * n + iB] = ql[v].y;
+      }
+      a.lam_out[iB] = lB;
+      a.isl_out[iB] = I.ir.y;
+      a.isl_out[n + iB] = I.e_int.y;
+      a.isl_out[2 * n + iB] = I.sm1.y;
+    }
+  }
+  // a slab's ghost cells: their owner reports them
+  if (!ownA || iA < a.own_lo || iA >= a.own_hi) lA = 0.0f;
+  if (!ownB || iB < a.own_lo || iB >= a.own_hi) lB = 0.0f;
+  const float m = mixed_block_max<BLOCK>(fmaxf(lA, lB));
   if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
 }
 
@@ -311,11 +458,15 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   sl.wr = (int)((k + 1) % 3);
   sl.clr = (int)((k + 2) % 3);
   const double dx = ctx_dx(c);
-  if (c->mixed_tma && !c->slab) {
+  if (c->mixed_kind == HYP_MIXED_TMA && !c->slab) {
     const int ntiles = (int)((c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2));
     step1_mixed_tma_kernel<kTmaBlock, kTmaMinB><<<c->tma_grid, kTmaBlock, TmaTile<kTmaBlock>::kSmem, c->stream>>>(
         c->tmap, arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc, ntiles,
         c->wait_tries);
+  } else if (c->mixed_kind == HYP_MIXED_PAIR) {
+    const int64_t ntiles = (c->n + (kPairBlock - 2) - 1) / (kPairBlock - 2);
+    step1_mixed_pair_kernel<kPairBlock><<<(unsigned)((ntiles + 1) / 2), kPairBlock, 0, c->stream>>>(
+        arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, ctx_bc(c));
   } else {
     const unsigned grid = (unsigned)((c->n + kTileM - 1) / kTileM);
     step1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl,

@@ -15,6 +15,7 @@
 #include "hyp_internal.cuh"
 #include "hyp_mixed_tile.cuh"
 #include "hyp_physics_mph_mixed.cuh"
+#include "hyp_physics_mph_pair.cuh"
 
 namespace hyp {
 
@@ -119,6 +120,71 @@ __global__ void __launch_bounds__(kFaceBlockM, 8) face2_lxf_mixed_kernel(
   }
 }
 
+// The face kernels with the phases as the lanes of packed FP32 pairs
+// (hyp_physics_mph_pair.cuh): pair k holds variable k of phase 1 and phase 2.
+__device__ __forceinline__ void load_face_pairs(const float* Qh, int64_t pitch, const float* F, int64_t fpitch,
+                                                int64_t L, int64_t R, float2* QL, float2* QR, float2* fl,
+                                                float2* fr) {
+  for (int k = 0; k < 15; ++k) {
+    QL[k] = make_float2(Qh[k * pitch + L], Qh[(15 + k) * pitch + L]);
+    QR[k] = make_float2(Qh[k * pitch + R], Qh[(15 + k) * pitch + R]);
+    fl[k] = make_float2(F[k * fpitch + L], F[(15 + k) * fpitch + L]);
+    fr[k] = make_float2(F[k * fpitch + R], F[(15 + k) * fpitch + R]);
+  }
+}
+
+__device__ __forceinline__ void store_face_pairs(float* D, int64_t nf, int64_t f, const float2* d) {
+  for (int k = 0; k < 15; ++k) {
+    D[k * nf + f] = d[k].x;
+    D[(15 + k) * nf + f] = d[k].y;
+  }
+}
+
+template <int kDef>
+__global__ void __launch_bounds__(kFaceBlockM) face2_hll_pair_kernel(
+    const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, EosPair ep, Quad6F qd,
+    const float* __restrict__ F, int64_t fpitch, const float* __restrict__ smin, const float* __restrict__ smax,
+    float* __restrict__ DM, float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
+  if (!(*t_now < t_end)) return;
+  const int64_t f = (int64_t)blockIdx.x * kFaceBlockM + threadIdx.x;  // face between cells f-1 and f
+  if (f > n) return;
+  const int64_t nf = n + 1;
+  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+  float2 dm[15], dp[15];
+  if (L == R) {  // boundary face with a zero-gradient ghost: no jump, no fluctuation
+    for (int k = 0; k < 15; ++k) dm[k] = dp[k] = f2s(0.0f);
+  } else {
+    float2 QL[15], QR[15], fl[15], fr[15];
+    load_face_pairs(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
+    for (int k = 0; k < 15; ++k) fr[k] = f2sub(fr[k], fl[k]);  // f(Q_r) - f(Q_l)
+    const int st = hll_face2_pair<kDef>(E, ep, qd, QL, QR, fr, smin[L], smax[R], dm, dp);
+    if (st) record_err2m(S, st, R);
+  }
+  store_face_pairs(DM, nf, f, dm);
+  store_face_pairs(DP, nf, f, dp);
+}
+
+template <int kDef>
+__global__ void __launch_bounds__(kFaceBlockM, 8) face2_lxf_pair_kernel(
+    const float* __restrict__ Qh, int64_t pitch, int64_t n, EosPair ep, Quad6F lobatto, const float* __restrict__ F,
+    int64_t fpitch, const unsigned long long* lam_now, double cfl, float* __restrict__ FF,
+    float* __restrict__ DM, float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
+  if (!(*t_now < t_end)) return;
+  const int64_t f = (int64_t)blockIdx.x * kFaceBlockM + threadIdx.x;
+  if (f > n) return;
+  const int64_t nf = n + 1;
+  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+  const double lmax = __longlong_as_double((long long)*lam_now);
+  const float lam = (float)lmax / (float)cfl;  // lambda = dx/dt = lmax/cfl (main.jl:223), in FP32
+  float2 QL[15], QR[15], fl[15], fr[15], ff_[15], dm[15], dp[15];
+  load_face_pairs(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
+  const int st = lxf_face2_pair<kDef>(ep, lobatto, QL, QR, fl, fr, lam, ff_, dm, dp);
+  if (st) record_err2m(S, st, R);
+  store_face_pairs(FF, nf, f, ff_);
+  store_face_pairs(DM, nf, f, dm);
+  store_face_pairs(DP, nf, f, dp);
+}
+
 __global__ void __launch_bounds__(kBlock) update2_mixed_kernel(
     const float* __restrict__ Qh, const float* __restrict__ Ql, float* __restrict__ Qh_out, float* __restrict__ Ql_out,
     int64_t pitch, int64_t n, const float* __restrict__ FF, const float* __restrict__ DM, const float* __restrict__ DP,
@@ -199,16 +265,30 @@ cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, 
 }
 
 cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
+  const bool def = default_exps(c), pair = c->mixed_kind == HYP_MIXED_PAIR;
+  const unsigned grid = grid_m(c->n + 1, kFaceBlockM);
   if (c->cfg.flux == HYP_FLUX_LXF) {
-    auto kern = default_exps(c) ? face2_lxf_mixed_kernel<1> : face2_lxf_mixed_kernel<-1>;
-    kern<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
-        c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->lobatto), c->F32, c->n, &c->st->lam_bits[p], c->cfg.cfl,
-        c->FF32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
+    if (pair) {
+      auto kern = def ? face2_lxf_pair_kernel<1> : face2_lxf_pair_kernel<-1>;
+      kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, make_eos_pair(eos2m(c)),
+                                                to_f(c->lobatto), c->F32, c->n, &c->st->lam_bits[p], c->cfg.cfl,
+                                                c->FF32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
+    } else {
+      auto kern = def ? face2_lxf_mixed_kernel<1> : face2_lxf_mixed_kernel<-1>;
+      kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->lobatto), c->F32,
+                                                c->n, &c->st->lam_bits[p], c->cfg.cfl, c->FF32, c->DM32, c->DP32,
+                                                &c->st->t[p], t_end, c->st);
+    }
+  } else if (pair) {
+    auto kern = def ? face2_hll_pair_kernel<1> : face2_hll_pair_kernel<-1>;
+    const Eos2M E = eos2m(c);
+    kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, E, make_eos_pair(E), to_f(c->quad),
+                                              c->F32, c->n, c->smin32, c->smax32, c->DM32, c->DP32, &c->st->t[p],
+                                              t_end, c->st);
   } else {
-    auto kern = default_exps(c) ? face2_hll_mixed_kernel<1> : face2_hll_mixed_kernel<-1>;
-    kern<<<grid_m(c->n + 1, kFaceBlockM), kFaceBlockM, 0, c->stream>>>(
-        c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n, c->smin32, c->smax32, c->DM32, c->DP32,
-        &c->st->t[p], t_end, c->st);
+    auto kern = def ? face2_hll_mixed_kernel<1> : face2_hll_mixed_kernel<-1>;
+    kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n,
+                                              c->smin32, c->smax32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
   }
   return cudaGetLastError();
 }

@@ -283,9 +283,11 @@ function last_timing(s::Solver)
         "hyp_last_timing", s.h)
   (ms_total=tot[], ms_cell=mc[], n_cell=nc[], ms_update=mu[], n_update=nu[])
 end
-"set_mixed_kernel!(s, tma): single-phase mixed precision on the TMA-prefetched persistent kernel (true) or one block per tile"
-set_mixed_kernel!(s::Solver, tma::Bool) =
-  check(ccall((:hyp_set_mixed_kernel, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, tma), "hyp_set_mixed_kernel", s.h)
+"set_mixed_kernel!(s, kind): mixed-precision kernel family, :tile (0), :tma (1, single-phase) or :pair (2, packed FP32 pairs)"
+function set_mixed_kernel!(s::Solver, kind::Symbol)
+  k = Dict(:tile => 0, :tma => 1, :pair => 2)[kind]
+  check(ccall((:hyp_set_mixed_kernel, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, k), "hyp_set_mixed_kernel", s.h)
+end
 "set_wait_limit!(s, tries): poll budget of the persistent kernel's device waits (0: every wait times out)"
 set_wait_limit!(s::Solver, tries::Integer) =
   check(ccall((:hyp_set_wait_limit, libhyp), Cint, (Ptr{Cvoid}, Cint), s.h, tries), "hyp_set_wait_limit", s.h)

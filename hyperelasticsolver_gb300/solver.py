@@ -111,11 +111,16 @@ class Solver:
         L.check(L.load().hyp_get_time(self._h, ctypes.byref(t), ctypes.byref(s)), self._h, "hyp_get_time")
         return t.value, s.value
 
+    MIXED_KERNELS = {"tile": 0, "tma": 1, "pair": 2}
+
     def set_mixed_kernel(self, kernel):
-        """Mixed precision: "tma" (persistent, TMA-prefetched tiles) or "tile" (one block per tile)."""
-        if kernel not in ("tma", "tile"):
-            raise ValueError("kernel must be 'tma' or 'tile'")
-        L.check(L.load().hyp_set_mixed_kernel(self._h, int(kernel == "tma")), self._h, "hyp_set_mixed_kernel")
+        """Mixed precision kernel family: "tile" (one block per tile, the single-phase
+        default; two-phase: scalar FP32 faces), "tma" (single-phase: persistent,
+        TMA-prefetched tiles) or "pair" (two cells -- two-phase: the two phases, the
+        two-phase default -- in the lanes of packed FP32 pairs)."""
+        if kernel not in self.MIXED_KERNELS:
+            raise ValueError("kernel must be one of " + ", ".join(self.MIXED_KERNELS))
+        L.check(L.load().hyp_set_mixed_kernel(self._h, self.MIXED_KERNELS[kernel]), self._h, "hyp_set_mixed_kernel")
 
     def set_wait_limit(self, tries):
         """Poll budget of the TMA kernel's device waits; 0 makes each wait time out at once."""

@@ -167,10 +167,21 @@ int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel
 int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_Q_out, int64_t n_cells, int n_steps,
                          double t0, void* stream, double* t_out, int64_t* err_cell);
 
-/* Single-phase mixed precision: step with the persistent kernel whose tiles are
-   prefetched by TMA (tma = 1) or with one block per tile loading its own cells
-   (tma = 0, the default, faster on GB300). Both run the same tile arithmetic. */
-int hyp_set_mixed_kernel(hyp_ctx* ctx, int tma);
+/* Kernel family of a mixed-precision context.
+   Single-phase: HYP_MIXED_TILE, one block per tile loading its own cells (the
+   default, the fastest on GB300); HYP_MIXED_TMA, a persistent kernel whose tiles are prefetched by TMA;
+   HYP_MIXED_PAIR, one block per two tiles, each thread stepping one cell of each
+   in the lanes of packed FP32 pairs (f32x2 instructions). All three run the same
+   tile arithmetic; the pair kernel's fused multiply-adds are written out, so its
+   results differ from the others' in the last bits (within the mixed step's own
+   error).
+   Two-phase: HYP_MIXED_TILE, the face kernels with both phases in scalar FP32;
+   HYP_MIXED_PAIR (the default), the face kernels with the two phases as the lanes
+   of packed FP32 pairs. HYP_MIXED_TMA is single-phase only.
+   Returns HYP_ERR_UNSUPPORTED for FP64 contexts, an unknown kind, or TMA where it
+   is not available; the CUDA graphs of the previous kernel are dropped. */
+enum { HYP_MIXED_TILE = 0, HYP_MIXED_TMA = 1, HYP_MIXED_PAIR = 2 };
+int hyp_set_mixed_kernel(hyp_ctx* ctx, int kind);
 
 /* Poll budget of the TMA kernel's device-side barrier waits (default 2^20). A wait
    that runs out records HYP_CELL_TIMEOUT, lets its in-flight copy land and ends the

@@ -20,9 +20,12 @@ def mirror(Q):
     return np.ascontiguousarray(M)
 
 
-@pytest.mark.parametrize("precision,bc,n", [("fp64", "frozen", 1 << 20), ("mixed", "frozen", 1 << 24),
-                                            ("mixed", "transmissive", 1 << 20), ("fp64", "transmissive", 4097)])
-def test_mirrored_run_is_the_mirror_of_the_run(hyp, precision, bc, n):
+@pytest.mark.parametrize("precision,bc,n,kernel", [("fp64", "frozen", 1 << 20, None),
+                                                   ("mixed", "frozen", 1 << 24, "tile"),
+                                                   ("mixed", "transmissive", 1 << 20, "tile"),
+                                                   ("mixed", "frozen", 1 << 22, "pair"),
+                                                   ("fp64", "transmissive", 4097, None)])
+def test_mirrored_run_is_the_mirror_of_the_run(hyp, precision, bc, n, kernel):
     from hyperelasticsolver_gb300._cases import segment_states, segment_fill
     from hyperelasticsolver_gb300 import Hyperelasticity as H
     eos = hyp.Barton2009()
@@ -30,6 +33,8 @@ def test_mirrored_run_is_the_mirror_of_the_run(hyp, precision, bc, n):
     out = []
     for q in (Q0, mirror(Q0)):
         with hyp.Solver(eos, n, precision=precision, bc=bc) as s:
+            if kernel:
+                s.set_mixed_kernel(kernel)
             s.upload(q)
             k, t = s.step(max_steps=40)
             out.append((s.download(), t))
@@ -37,7 +42,7 @@ def test_mirrored_run_is_the_mirror_of_the_run(hyp, precision, bc, n):
     assert ta == tb
     d = np.abs(mirror(Qa) - Qb)
     scale = np.maximum(np.max(np.abs(Qa), axis=1, keepdims=True), 1e-30)
-    print(f"mirror {precision} {bc} {n}: max rel {np.max(d / scale):.1e}, bitwise {np.array_equal(mirror(Qa), Qb)}")
+    print(f"mirror {precision} {kernel} {bc} {n}: max rel {np.max(d / scale):.1e}, bitwise {np.array_equal(mirror(Qa), Qb)}")
     assert np.array_equal(mirror(Qa), Qb)
 
 
@@ -51,9 +56,10 @@ def mirror2(Q):
 
 
 # observed: FP64 3.4e-15; mixed 1.7e-7 (HLL) and 6.8e-7 (LxF) of each variable's scale
-@pytest.mark.parametrize("precision,flux,tol", [("fp64", "hll", 1e-13), ("mixed", "hll", 5e-6),
-                                                ("mixed", "lxf", 5e-6)])
-def test_twophase_mirrored_run_at_full_size(hyp, precision, flux, tol):
+@pytest.mark.parametrize("precision,flux,tol,kernel", [("fp64", "hll", 1e-13, None), ("mixed", "hll", 5e-6, "tile"),
+                                                       ("mixed", "lxf", 5e-6, "tile"), ("mixed", "hll", 5e-6, "pair"),
+                                                       ("mixed", "lxf", 5e-6, "pair")])
+def test_twophase_mirrored_run_at_full_size(hyp, precision, flux, tol, kernel):
     """The two-phase step at the 2^22-cell interface workload also commutes with
     x -> -x, to rounding rather than bitwise: the HLL state Q_hll = (s_R Q_R - s_L Q_L
     - ...)/(s_R - s_L) and the path integrals evaluate their mirrored operands in a
@@ -66,6 +72,8 @@ def test_twophase_mirrored_run_at_full_size(hyp, precision, flux, tol):
     out = []
     for q in (Q0, mirror2(Q0)):
         with hyp.Solver(eos, n, model="multi", flux=flux, precision=precision) as s:
+            if kernel:
+                s.set_mixed_kernel(kernel)
             s.upload(q)
             k, t = s.step(max_steps=40)
             assert k == 40
@@ -75,5 +83,5 @@ def test_twophase_mirrored_run_at_full_size(hyp, precision, flux, tol):
     assert abs(ta - tb) <= (1e-14 if precision == "fp64" else 1e-6) * ta
     scale = np.maximum(np.max(np.abs(Qa), axis=1, keepdims=True), 1e-30)
     err = np.max(np.abs(mirror2(Qa) - Qb) / scale)
-    print(f"two-phase mirror {precision} {flux} 2^22: max rel {err:.1e}")
+    print(f"two-phase mirror {precision} {kernel} {flux} 2^22: max rel {err:.1e}")
     assert err <= tol

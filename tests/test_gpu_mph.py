@@ -164,9 +164,18 @@ def l1_linf(a, b):
     return np.sum(np.abs(a - b)) / np.sum(np.abs(b)), np.max(np.abs(a - b)) / np.max(np.abs(b))
 
 
+KERNELS = ["tile", "pair"]  # face kernels with the phases in scalar FP32 / as packed FP32 pairs
+
+
+def _mixed_kernel(s, prec, kernel):
+    if prec == "mixed":
+        s.set_mixed_kernel(kernel)
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("flux", ["hll", "lxf"])
 @pytest.mark.parametrize("testcase", [4, 6, 7])
-def test_mixed_twophase_vs_fp64(hyp, orc, testcase, flux):
+def test_mixed_twophase_vs_fp64(hyp, orc, testcase, flux, kernel):
     """Mixed-precision two-phase step (FP32 physics, compensated state, float-float
     cons2prim islands) against the FP64 two-phase step: relative L1 error of each
     phase's density <= 1e-6 after 100 steps of the reference's test cases."""
@@ -178,19 +187,21 @@ def test_mixed_twophase_vs_fp64(hyp, orc, testcase, flux):
     out = {}
     for prec in ("fp64", "mixed"):
         with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, precision=prec, cfl=0.6) as s:
+            _mixed_kernel(s, prec, kernel)
             s.upload(Q0)
             n, t = s.step(max_steps=steps)
             assert n == steps
             out[prec] = (s.download(), t)
     assert abs(out["mixed"][1] - out["fp64"][1]) <= 1e-6 * out["fp64"][1]
     errs = [l1_linf(a, b) for a, b in zip(phase_densities(out["mixed"][0]), phase_densities(out["fp64"][0]))]
-    print(f"mixed two-phase test case {testcase} ({flux}), {steps} steps: density L1/Linf per phase "
+    print(f"mixed ({kernel}) two-phase test case {testcase} ({flux}), {steps} steps: density L1/Linf per phase "
           + ", ".join(f"{l1:.1e}/{li:.1e}" for l1, li in errs))
     assert max(e[0] for e in errs) <= 1e-6
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("flux", ["hll", "lxf"])
-def test_mixed_twophase_smoothed_interface(hyp, orc, flux):
+def test_mixed_twophase_smoothed_interface(hyp, orc, flux, kernel):
     from hyperelasticsolver_gb300._cases import mph_interface_prims
     nx, steps = 2048, 100
     P = mph_interface_prims(hyp.Barton2009(), nx)
@@ -198,20 +209,23 @@ def test_mixed_twophase_smoothed_interface(hyp, orc, flux):
     out = {}
     for prec in ("fp64", "mixed"):
         with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, precision=prec, cfl=0.5) as s:
+            _mixed_kernel(s, prec, kernel)
             s.upload(Q0)
             s.step(max_steps=steps)
             out[prec] = s.download()
     errs = [l1_linf(a, b) for a, b in zip(phase_densities(out["mixed"]), phase_densities(out["fp64"]))]
-    print(f"mixed two-phase smoothed interface ({flux}), {steps} steps: density L1/Linf per phase "
+    print(f"mixed ({kernel}) two-phase smoothed interface ({flux}), {steps} steps: density L1/Linf per phase "
           + ", ".join(f"{l1:.1e}/{li:.1e}" for l1, li in errs))
     assert max(e[0] for e in errs) <= 1e-6
 
 
-def test_mixed_twophase_uniform_state_preserved(hyp, orc):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_mixed_twophase_uniform_state_preserved(hyp, orc, kernel):
     rng = np.random.default_rng(8)
     q = random_mph(orc, 1, rng)[0]
     Q0 = np.ascontiguousarray(np.repeat(q[:, None], 1000, axis=1))
     with hyp.Solver(eos_pair(hyp), 1000, model="multi", flux="hll", precision="mixed", bc="transmissive") as s:
+        s.set_mixed_kernel(kernel)
         s.upload(Q0)
         Qa = s.download()  # the compensated pair holds the FP64 input to ~48 bits
         s.step(max_steps=3)
@@ -223,8 +237,9 @@ def test_mixed_twophase_uniform_state_preserved(hyp, orc):
     assert np.max(np.abs(Qb - Qa) / np.maximum(scale, 1e-30)) < 1e-9
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("flux", ["hll", "lxf"])
-def test_nondefault_exponents_twophase(hyp, orc, flux):
+def test_nondefault_exponents_twophase(hyp, orc, flux, kernel):
     """Phase 1 with non-integer beta, gamma (the alternative Barton2009 parameters of
     main.jl:133): the step runs the kernels' general-exponent instances (powers through
     exp/log), which the default parameters never reach. FP64 against the oracle at
@@ -246,10 +261,11 @@ def test_nondefault_exponents_twophase(hyp, orc, flux):
     out = {}
     for prec in ("fp64", "mixed"):
         with hyp.Solver(eos, nx, model="multi", flux=flux, precision=prec, cfl=0.6) as s:
+            _mixed_kernel(s, prec, kernel)
             s.upload(Q0)
             assert s.step(max_steps=100)[0] == 100
             out[prec] = s.download()
     errs = [l1_linf(a, b) for a, b in zip(phase_densities(out["mixed"]), phase_densities(out["fp64"]))]
-    print(f"two-phase non-default exponents ({flux}): FP64 vs oracle {err:.1e}; mixed density L1/Linf "
+    print(f"two-phase non-default exponents ({flux}, {kernel}): FP64 vs oracle {err:.1e}; mixed density L1/Linf "
           + ", ".join(f"{l1:.1e}/{li:.1e}" for l1, li in errs))
     assert max(e[0] for e in errs) <= 1e-6

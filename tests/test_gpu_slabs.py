@@ -20,13 +20,15 @@ def _state(hyp):
     return eos, segment_fill(H.prim2cons(eos, segment_states(eos, 16)), N)
 
 
-@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+@pytest.mark.parametrize("precision,kernel", [("fp64", None), ("mixed", "tile"), ("mixed", "pair")])
 @pytest.mark.parametrize("flux,bc", [("rusanov", "frozen"), ("lxf", "transmissive")])
 @pytest.mark.parametrize("world", [2, 5])
-def test_slabs_equal_single_domain_bitwise(hyp, precision, flux, bc, world):
+def test_slabs_equal_single_domain_bitwise(hyp, precision, kernel, flux, bc, world):
     from hyperelasticsolver_gb300.domain import GpuSlab, step_all
     eos, Q0 = _state(hyp)
     with hyp.Solver(eos, N, flux=flux, bc=bc, precision=precision) as s:
+        if kernel:
+            s.set_mixed_kernel(kernel)
         s.upload(Q0)
         n, tref = s.step(max_steps=STEPS)
         assert n == STEPS
@@ -34,6 +36,8 @@ def test_slabs_equal_single_domain_bitwise(hyp, precision, flux, bc, world):
     slabs = [GpuSlab(eos, N, world, r, flux=flux, bc=bc, precision=precision) for r in range(world)]
     try:
         for sl in slabs:
+            if kernel:
+                sl.solver.set_mixed_kernel(kernel)
             sl.upload(Q0)
         for _ in range(STEPS):
             ts = step_all(slabs)
