@@ -84,18 +84,9 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     MixedCellIn c;
     mixed_tile_load(d.first, d.lo, d.hi, ld, c);
     if (!k.active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
-      const int64_t n = a.stride;
       const int64_t i = d.first - 1 + threadIdx.x;
-      if (threadIdx.x > 0 && threadIdx.x < BLOCK - 1 && i < d.hi) {
-        for (int v = 0; v < 14; ++v) {
-          a.Qh_out[v * n + i] = c.qh[v];
-          a.Ql_out[v * n + i] = c.ql[v];
-        }
-        a.lam_out[i] = c.li;
-        a.isl_out[i] = c.I0.ir;
-        a.isl_out[n + i] = c.I0.e_int;
-        a.isl_out[2 * n + i] = c.I0.sm1;
-      }
+      if (threadIdx.x > 0 && threadIdx.x < BLOCK - 1 && i < d.hi)
+        mixed_store_cell(a.out + i, a.rstride, c.qh, c.ql, c.li, c.I0);
       continue;
     }
     // faces from shared memory: the batch variants at 64 registers spill more otherwise
@@ -114,7 +105,7 @@ __global__ void __launch_bounds__(kBlock) batch_mixed_lam_kernel(MixedArrays a, 
     const TileDesc d = tiles[tix];
     float m = 0.0f;
     for (int64_t i = d.first + threadIdx.x; i < d.first + tile_cells && i < d.hi; i += kBlock)
-      m = fmaxf(m, mixed_cell_lambda(a, em, i, S, a.lam_out, a.isl_out));
+      m = fmaxf(m, mixed_cell_lambda<false>(a, em, i, S));
     m = mixed_block_max<kBlock>(m);
     if (threadIdx.x == 0) atomicMax(&b.slots[d.problem], (unsigned long long)__float_as_uint(m));
     __syncthreads();
@@ -261,8 +252,6 @@ struct hyp_batch {
   int64_t mpitch = 0;
   float* Qh[2] = {nullptr, nullptr};
   float* Ql[2] = {nullptr, nullptr};
-  float* lamf[2] = {nullptr, nullptr};
-  float* isl[2] = {nullptr, nullptr};
   // FP64 state
   double* Q[2] = {nullptr, nullptr};
   double* F = nullptr;
@@ -343,15 +332,9 @@ static int select_variant(hyp_batch* b, int v) {
 
 static MixedArrays batch_arrays(hyp_batch* b, int p) {
   MixedArrays a;
-  a.Qh = b->Qh[p];
-  a.Ql = b->Ql[p];
-  a.lam = b->lamf[p];
-  a.isl = b->isl[p];
-  a.Qh_out = b->Qh[1 - p];
-  a.Ql_out = b->Ql[1 - p];
-  a.lam_out = b->lamf[1 - p];
-  a.isl_out = b->isl[1 - p];
-  a.stride = b->mpitch;
+  a.in = b->Qh[p];
+  a.out = b->Qh[1 - p];
+  a.rstride = b->mpitch;
   a.n = b->total;
   a.own_lo = 0;
   a.own_hi = b->total;
@@ -449,8 +432,6 @@ extern "C" int hyp_batch_create(const hyp_config* cfg, const int64_t* offsets, i
     for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
       b->Qh[p] = b->mixed_base + (size_t)p * kMixedRows * b->mpitch;
       b->Ql[p] = b->Qh[p] + (size_t)14 * b->mpitch;
-      b->lamf[p] = b->Qh[p] + (size_t)28 * b->mpitch;
-      b->isl[p] = b->Qh[p] + (size_t)29 * b->mpitch;
     }
   } else {
     for (int p = 0; p < 2 && rc == HYP_OK; ++p) ck(cudaMalloc(&b->Q[p], nq * sizeof(double)));
@@ -512,9 +493,7 @@ extern "C" int hyp_batch_upload(hyp_batch* b, const double* Q, double t0) {
     double* stage = (double*)b->Qh[1];
     BCK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, b->stream));
     BCK(launch_split_n(b->stream, stage, b->Qh[0], b->Ql[0], 14, b->total, b->mpitch));
-    MixedArrays a = batch_arrays(b, 0);
-    a.lam_out = b->lamf[0];
-    a.isl_out = b->isl[0];
+    const MixedArrays a = batch_arrays(b, 0);  // lambda and islands into the uploaded block itself
     batch_mixed_lam_kernel<<<b->sms * 8, kBlock, 0, b->stream>>>(a, b->eos_mixed, b->tiles, b->ntiles, b->tile_cells,
                                                                   b->b, b->st);
     BCK(cudaGetLastError());

@@ -157,17 +157,12 @@ extern "C" int hyp_create(const hyp_config* cfg, hyp_ctx** out) {
     if (rc == HYP_OK && (e = cudaMalloc(&c->lam, (size_t)c->n * sizeof(double))) != cudaSuccess)
       fail(e, "cudaMalloc(lam)");
   } else {
-    // one block [2][32][pitch] floats: per parity 14 hi rows, 14 lo rows, lambda, 3 island rows
-    // (hyp_mixed_tile.cuh); a parity's block also stages FP64 uploads and downloads (16 pitch >= 14 n doubles)
-    c->mpitch = mixed_pitch(c->n);
-    if ((e = cudaMalloc(&c->mixed_base, (size_t)2 * kMixedRows * c->mpitch * sizeof(float))) != cudaSuccess)
-      fail(e, "cudaMalloc(mixed state)");
-    for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
-      c->Qh[p] = c->mixed_base + (size_t)p * kMixedRows * c->mpitch;
-      c->Ql[p] = c->Qh[p] + (size_t)14 * c->mpitch;
-      c->lamf[p] = c->Qh[p] + (size_t)28 * c->mpitch;
-      c->isl[p] = c->Qh[p] + (size_t)29 * c->mpitch;
-    }
+    // per parity one tile-major block of mixed_tiles(n) tiles x 32 rows (hi, lo, lambda,
+    // islands: hyp_internal.cuh); a parity's block also stages FP64 uploads and downloads
+    // (32 x 254 floats per 254 cells >= 14 doubles per cell)
+    const size_t block = (size_t)mixed_tiles(c->n) * kTileFloats;
+    if ((e = cudaMalloc(&c->mixed_base, 2 * block * sizeof(float))) != cudaSuccess) fail(e, "cudaMalloc(mixed state)");
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p) c->Qh[p] = c->mixed_base + (size_t)p * block;
     if (rc == HYP_OK && setup_mixed_tma(c) != 0) c->tma_grid = 0;  // TMA kernel unavailable
   }
   if (rc == HYP_OK && (e = cudaMalloc(&c->st, sizeof(DevState))) != cudaSuccess) fail(e, "cudaMalloc(state)");
@@ -287,7 +282,7 @@ extern "C" int hyp_download(hyp_ctx* c, double* Q, int64_t n_cells, int n_vars) 
     CK(cudaMemcpyAsync(Q, c->Q[c->cur], bytes, cudaMemcpyDeviceToHost, c->stream));
   } else if (bytes < ((size_t)64 << 20)) {
     double* stage = (double*)c->Qh[1 - c->cur];  // the other parity's block is free between steps
-    CK(launch_join(c, c->Qh[c->cur], c->Ql[c->cur], stage));
+    CK(launch_join(c, c->cur, stage));
     CK(cudaMemcpyAsync(Q, stage, bytes, cudaMemcpyDeviceToHost, c->stream));
   } else {
     // large states: join one variable row at a time on the context stream and copy each
@@ -296,8 +291,7 @@ extern "C" int hyp_download(hyp_ctx* c, double* Q, int64_t n_cells, int n_vars) 
     double* stage = (double*)c->Qh[1 - c->cur];
     const size_t row = (size_t)n_cells * sizeof(double);
     for (int v = 0; v < n_vars; ++v) {
-      CK(launch_join_n(c->stream, c->Qh[c->cur] + (size_t)v * c->mpitch, c->Ql[c->cur] + (size_t)v * c->mpitch,
-                       stage + (size_t)v * n_cells, 1, n_cells, c->mpitch));
+      CK(launch_join_rows(c, c->cur, stage + (size_t)v * n_cells, v, 1));
       CK(cudaEventRecord(c->row_ev[v], c->stream));
       CK(cudaStreamWaitEvent(c->copy_stream, c->row_ev[v], 0));
       CK(cudaMemcpyAsync(Q + (size_t)v * n_cells, stage + (size_t)v * n_cells, row, cudaMemcpyDeviceToHost,

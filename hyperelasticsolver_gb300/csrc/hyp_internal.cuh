@@ -118,12 +118,23 @@ struct StepTiming {
 namespace hyp {
 struct AdjTape;
 struct SnapBuf;
-// Mixed-precision state of one parity: kMixedRows rows of a pitch of floats,
-// rows 0-13 hi parts, 14-27 lo parts, 28 the cell's wave speed, 29-31 its
-// island outputs. The two parities are consecutive blocks of one allocation, so
-// the whole state is one 2D array [2 x 32][pitch] that a TMA tensor map can box.
+// Mixed-precision state of one parity: kMixedRows rows per cell, rows 0-13 hi
+// parts, 14-27 lo parts, 28 the cell's wave speed, 29-31 its island outputs.
+// Row-major blocks (the batch solver, the two-phase step's 60 rows): row r of cell
+// i at r * pitch + i. Tile-major blocks (the single-phase step): cells in tiles of
+// kTileCells, each tile's 32 rows of kTileCells floats contiguous (32,512 bytes), so
+// that the block that steps a tile reads and writes one contiguous span.
 constexpr int kMixedRows = 32;
+constexpr int kRowLo = 14, kRowLam = 28, kRowIsl = 29;
+constexpr int kTileCells = 254;  // owned cells of a 256-thread tile
+constexpr int kTileFloats = kMixedRows * kTileCells;
 __host__ __device__ __forceinline__ int64_t mixed_pitch(int64_t n) { return (n + 3) & ~int64_t(3); }
+__host__ __device__ __forceinline__ int64_t mixed_tiles(int64_t n) { return (n + kTileCells - 1) / kTileCells; }
+// Offset of cell i's row 0 in a tile-major block (row r at + r * kTileCells).
+__host__ __device__ __forceinline__ int64_t tile_cell_off(int64_t i) {
+  const unsigned t = (unsigned)i / kTileCells;  // cells < 2^31: the state of 2^31 cells exceeds the device
+  return (int64_t)t * kTileFloats + (int64_t)((unsigned)i - t * kTileCells);
+}
 }
 
 struct hyp_ctx {
@@ -139,15 +150,14 @@ struct hyp_ctx {
   double* Q[2] = {nullptr, nullptr};
   double* F = nullptr;     // per-cell fluxes (scratch)
   double* lam = nullptr;   // per-cell max wave speed (scratch)
-  // mixed precision: per parity one block of 2 x 14 x n floats (hi then lo), which
-  // also serves as the FP64 staging buffer of uploads and downloads; per-cell FP32 lambda
+  // mixed precision: per parity one block of floats, which also serves as the FP64
+  // staging buffer of uploads and downloads. Single-phase: Qh[p] is a tile-major
+  // block of the 32 rows (hi, lo, lambda, islands) of mixed_tiles(n) tiles; Ql is not
+  // used. Two-phase: Qh[p] / Ql[p] the row-major hi / lo rows [30][mpitch].
   float* Qh[2] = {nullptr, nullptr};
   float* Ql[2] = {nullptr, nullptr};
-  float* lamf[2] = {nullptr, nullptr};
-  float* isl[2] = {nullptr, nullptr};  // cached float-float island outputs [3][n] (1/rho, e_int, rho/rho0 - 1)
-  float* mixed_base = nullptr;          // one allocation [2 parities][32 rows][mpitch] holding all of the above
-  int64_t mpitch = 0;                   // row pitch (floats, a multiple of 4)
-  CUtensorMap tmap;                     // TMA map over mixed_base (both parities)
+  float* mixed_base = nullptr;          // one allocation holding both parities' blocks
+  int64_t mpitch = 0;                   // two-phase: row pitch (floats, a multiple of 4)
   int mixed_kind = HYP_MIXED_TILE;      // kernel family (hyp_set_mixed_kernel)
   int wait_tries = hyp::kWaitTries;     // poll budget of the TMA kernel's barrier waits
   int tma_grid = 0;
@@ -247,7 +257,8 @@ cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, 
 cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end);
 cudaError_t launch_update2_mixed(hyp_ctx* c, int p, double t_end);
 int setup_mixed_tma(hyp_ctx* c);
-cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q);
+cudaError_t launch_join(hyp_ctx* c, int p, double* q);
+cudaError_t launch_join_rows(hyp_ctx* c, int p, double* q, int v0, int rows);
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot);
 cudaError_t launch_install1_mixed(hyp_ctx* c, const double* q, unsigned long long* slot);
 cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end);

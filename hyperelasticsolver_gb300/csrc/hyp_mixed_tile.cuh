@@ -12,24 +12,35 @@
 //   3. Q += -dt/dx (F_{i+1/2} - F_{i-1/2}) accumulated into (hi, lo) (main.jl:43-60);
 //   4. islands, cons2prim and wave speed of the NEW state, stored per cell.
 // Returns the thread's new wave speed; the caller reduces the block max.
+// Phases 2 and 3 treat the 14 variables as 7 pairs (2k, 2k+1) in packed FP32
+// instructions (hyp_pair.cuh) and keep them in shared memory as float2: the same
+// operations in the same order, half the instructions and shared-memory accesses.
 #pragma once
 #include "hyp_internal.cuh"
+#include "hyp_pair.cuh"
 
 namespace hyp {
 
+// A step's input and output state blocks (32 rows per cell: kRowLo, kRowLam,
+// kRowIsl), row-major (row r of cell i at r * rstride + i) or tile-major (at
+// tile_cell_off(i) + r * kTileCells).
 struct MixedArrays {
-  const float* Qh;  // [14][stride] hi parts
-  const float* Ql;  // [14][stride] lo parts
-  const float* lam; // [stride] wave speed of the state
-  const float* isl; // [3][stride] island outputs of the state
-  float* Qh_out;
-  float* Ql_out;
-  float* lam_out;
-  float* isl_out;
-  int64_t stride;   // floats between rows (a multiple of 4)
+  const float* in;
+  float* out;
+  int64_t rstride;  // row-major blocks: the pitch
   int64_t n;        // cells
   int64_t own_lo, own_hi;  // cells whose new wave speed enters the step's max (a slab's ghosts do not)
 };
+// kTiled: tile-major blocks, whose row stride is known at compile time, so that a
+// cell's 32 rows are immediate offsets from one address; else row-major.
+template <bool kTiled>
+__device__ __forceinline__ int64_t rows_apart(const MixedArrays& a) {
+  return kTiled ? (int64_t)kTileCells : a.rstride;
+}
+template <bool kTiled>
+__device__ __forceinline__ int64_t cell_at(int64_t i) {
+  return kTiled ? tile_cell_off(i) : i;
+}
 
 // One cell's inputs to a tile.
 struct MixedCellIn {
@@ -38,38 +49,67 @@ struct MixedCellIn {
   Islands I0;
 };
 
+__device__ __forceinline__ float2 pair_of(const float* v, int k) { return make_float2(v[2 * k], v[2 * k + 1]); }
+
 // Loads the cell's inputs straight from the state arrays and keeps the hi parts
 // the face phase reads in shared memory.
 // Loader interface used by mixed_tile: operator()(j, ic, c) fills cell ic's
-// inputs for local index j; keep(j, c) stores what face_q needs; face_q(v, j, ic)
-// returns the hi part of variable v of local cell j (cell ic); release() runs
-// once the face phase has read its inputs.
-template <int BLOCK>
+// inputs for local index j; keep(j, c) stores what face_q2 needs; face_q2(k, j, ic)
+// returns the hi parts of variables 2k, 2k+1 of local cell j (cell ic); release()
+// runs once the face phase has read its inputs.
+template <int BLOCK, bool kTiled = false>
 struct MixedGlobalLoader {
   const MixedArrays& a;
-  __device__ __forceinline__ static float (&sQ())[14][BLOCK] {
-    __shared__ float q[14][BLOCK];
+  __device__ __forceinline__ static float2 (&sQ())[7][BLOCK] {
+    __shared__ float2 q[7][BLOCK];
     return q;
   }
   __device__ __forceinline__ void operator()(int, int64_t ic, MixedCellIn& c) const {
-    const int64_t n = a.stride;
+    const int64_t r = rows_apart<kTiled>(a);
+    const float* q = a.in + cell_at<kTiled>(ic);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
-      c.qh[v] = a.Qh[v * n + ic];
-      c.ql[v] = a.Ql[v * n + ic];
+      c.qh[v] = q[v * r];
+      c.ql[v] = q[(kRowLo + v) * r];
     }
-    c.li = a.lam[ic];
-    c.I0.ir = a.isl[ic];
-    c.I0.e_int = a.isl[n + ic];
-    c.I0.sm1 = a.isl[2 * n + ic];
+    c.li = q[kRowLam * r];
+    c.I0.ir = q[kRowIsl * r];
+    c.I0.e_int = q[(kRowIsl + 1) * r];
+    c.I0.sm1 = q[(kRowIsl + 2) * r];
   }
   __device__ __forceinline__ void keep(int j, const MixedCellIn& c) const {
 #pragma unroll
-    for (int v = 0; v < 14; ++v) sQ()[v][j] = c.qh[v];
+    for (int k = 0; k < 7; ++k) sQ()[k][j] = pair_of(c.qh, k);
   }
-  __device__ __forceinline__ float face_q(int v, int j, int64_t) const { return sQ()[v][j]; }
+  __device__ __forceinline__ float2 face_q2(int k, int j, int64_t) const { return sQ()[k][j]; }
   __device__ __forceinline__ void release() const {}
 };
+
+// A cell's 11 flux components (flux_slot1 order) as 7 pairs of variables, zero
+// where a variable of rho A has no x-flux (row 1 of rho A: variables 5, 8, 11).
+__device__ __forceinline__ void flux_pairs(const float* f11, float2* f2) {
+  f2[0] = make_float2(f11[0], f11[1]);
+  f2[1] = make_float2(f11[2], f11[3]);
+  f2[2] = make_float2(f11[4], 0.0f);
+  f2[3] = make_float2(f11[5], f11[6]);
+  f2[4] = make_float2(0.0f, f11[7]);
+  f2[5] = make_float2(f11[8], 0.0f);
+  f2[6] = make_float2(f11[9], f11[10]);
+}
+
+// A cell's 32 rows into a state block (q: the cell's row 0, rows rstride apart).
+__device__ __forceinline__ void mixed_store_cell(float* q, int64_t rstride, const float* qh, const float* ql,
+                                                 float lam, const Islands& I) {
+#pragma unroll
+  for (int v = 0; v < 14; ++v) {
+    q[v * rstride] = qh[v];
+    q[(kRowLo + v) * rstride] = ql[v];
+  }
+  q[kRowLam * rstride] = lam;
+  q[kRowIsl * rstride] = I.ir;
+  q[(kRowIsl + 1) * rstride] = I.e_int;
+  q[(kRowIsl + 2) * rstride] = I.sm1;
+}
 
 __device__ __forceinline__ void mixed_record_err(DevState* S, int code, long long cell) {
   if (atomicCAS(&S->err_code, 0, code) == 0) S->err_cell = cell;
@@ -106,47 +146,48 @@ __device__ __forceinline__ void mixed_tile_load(int64_t first, int64_t lo, int64
 // kOwnRegs: a face reads its left cell (this thread's) and an update its right face
 // (this thread's) from registers instead of shared memory -- 39 fewer shared loads
 // per cell, at 11 more registers live across a barrier (the same values either way).
-template <int BLOCK, bool kOwnRegs = true, class Loader>
+template <int BLOCK, bool kOwnRegs = true, bool kTiled = false, class Loader>
 __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
                                                 int64_t hi, float dtdx, int flux, int bc, DevState* S,
                                                 const Loader& load, MixedCellIn& c) {
-  __shared__ float sFF[14][BLOCK];  // cell fluxes (11 slots), then the face fluxes (14)
+  __shared__ float2 sF[7][BLOCK];  // per variable pair: cell fluxes, then the face fluxes
   __shared__ float sL[BLOCK];
-  const int64_t n = a.stride;
   const int j = threadIdx.x;
   const int64_t i = first - 1 + j;
   const int64_t ic = tile_cell(first, lo, hi);
-  float f11[kNFlux1];  // this cell's flux: its own face reads it from registers
+  float2 fc[7];  // this cell's flux: its own face reads it from registers
   {
     PrimM P;
     int st = prim_from_islands(em, c.qh, c.ql, c.I0, P);
     StressCT<float> sc = stress_coeffs<float>(em.f, P.k, P.w, P.xm1);
+    float f11[kNFlux1];
     flux_mixed(em, c.qh, P, sc, f11);
+    flux_pairs(f11, fc);
 #pragma unroll
-    for (int s = 0; s < kNFlux1; ++s) sFF[s][j] = f11[s];
+    for (int k = 0; k < 7; ++k) sF[k][j] = fc[k];
     load.keep(j, c);
     sL[j] = c.li;
     if (st && i == ic && j > 0 && j < BLOCK - 1) mixed_record_err(S, st, i);
   }
   __syncthreads();
   // face j + 1/2 between local cells j (this thread: registers) and j + 1 (shared memory)
-  float fv[14];
+  float2 fv[7];
   if (j < BLOCK - 1) {
     const float lf = flux == HYP_FLUX_LXF ? 1.0f / dtdx : fmaxf(kOwnRegs ? c.li : sL[j], sL[j + 1]);
-    const float hl = 0.5f * lf;
+    const float2 nhl = f2s(-0.5f * lf), half = f2s(0.5f);
     const int64_t i1 = i + 1, ic1 = i1 < lo ? lo : (i1 >= hi ? hi - 1 : i1);
 #pragma unroll
-    for (int v = 0; v < 14; ++v) {
-      const int s = flux_slot1(v);
-      const float fl = s >= 0 ? (kOwnRegs ? f11[s] : sFF[s][j]) : 0.0f, fr = s >= 0 ? sFF[s][j + 1] : 0.0f;
-      fv[v] = 0.5f * (fl + fr) - hl * (load.face_q(v, j + 1, ic1) - (kOwnRegs ? c.qh[v] : load.face_q(v, j, ic)));
+    for (int k = 0; k < 7; ++k) {
+      const float2 fl = kOwnRegs ? fc[k] : sF[k][j], fr = sF[k][j + 1];
+      const float2 ql = kOwnRegs ? pair_of(c.qh, k) : load.face_q2(k, j, ic);
+      fv[k] = f2fma(nhl, f2sub(load.face_q2(k, j + 1, ic1), ql), f2mul(half, f2add(fl, fr)));
     }
   }
   __syncthreads();
   load.release();
   if (j < BLOCK - 1) {
 #pragma unroll
-    for (int v = 0; v < 14; ++v) sFF[v][j] = fv[v];
+    for (int k = 0; k < 7; ++k) sF[k][j] = fv[k];
   }
   __syncthreads();
   float lnew = 0.0f;
@@ -157,12 +198,15 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
     if (frozen) {
       lnew = c.li;
     } else {
+      const float2 ndt = f2s(-dtdx);
 #pragma unroll
-      for (int v = 0; v < 14; ++v) {
-        const float delta = -dtdx * ((kOwnRegs ? fv[v] : sFF[v][j]) - sFF[v][j - 1]);  // F_{j+1/2} - F_{j-1/2}
-        ff q = ff_add_f(ff{c.qh[v], c.ql[v]}, delta);
-        c.qh[v] = q.hi;
-        c.ql[v] = q.lo;
+      for (int k = 0; k < 7; ++k) {
+        const float2 delta = f2mul(ndt, f2sub(kOwnRegs ? fv[k] : sF[k][j], sF[k][j - 1]));  // F_{j+1/2} - F_{j-1/2}
+        const ff2 q = ff2_add_f(ff2{pair_of(c.qh, k), pair_of(c.ql, k)}, delta);
+        c.qh[2 * k] = q.hi.x;
+        c.qh[2 * k + 1] = q.hi.y;
+        c.ql[2 * k] = q.lo.x;
+        c.ql[2 * k + 1] = q.lo.y;
       }
       PrimM P;
       int st = prim_mixed(em, c.qh, c.ql, P, I);
@@ -171,31 +215,24 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
       if (!(lnew <= 3.0e38f)) st |= HYP_CELL_NONFINITE;
       if (st) mixed_record_err(S, st, i);
     }
-#pragma unroll
-    for (int v = 0; v < 14; ++v) {
-      a.Qh_out[v * n + i] = c.qh[v];
-      a.Ql_out[v * n + i] = c.ql[v];
-    }
-    a.lam_out[i] = lnew;
-    a.isl_out[i] = I.ir;
-    a.isl_out[n + i] = I.e_int;
-    a.isl_out[2 * n + i] = I.sm1;
+    mixed_store_cell(a.out + cell_at<kTiled>(i), rows_apart<kTiled>(a), c.qh, c.ql, lnew, I);
   }
   __syncthreads();  // the shared arrays are reused by the block's next tile
   return lnew;
 }
-template <int BLOCK, class Loader>
+template <int BLOCK, bool kTiled = false, class Loader>
 __device__ __forceinline__ float mixed_tile(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
                                             int64_t hi, float dtdx, int flux, int bc, DevState* S,
                                             const Loader& load) {
   MixedCellIn c;
   mixed_tile_load(first, lo, hi, load, c);
-  return mixed_tile_run<BLOCK>(a, em, first, lo, hi, dtdx, flux, bc, S, load, c);
+  return mixed_tile_run<BLOCK, true, kTiled>(a, em, first, lo, hi, dtdx, flux, bc, S, load, c);
 }
 
-// Wave speed and island outputs of one cell of a freshly uploaded state.
+// Wave speed and island outputs of one cell of a freshly uploaded state, into rows
+// kRowLam.. of the cell at q (rows rstride apart).
 __device__ __forceinline__ float mixed_cell_lambda_of(const EosMixed& em, const float* qh, const float* ql, int64_t i,
-                                                      int64_t n, DevState* S, float* lam_out, float* isl_out) {
+                                                      DevState* S, float* q, int64_t rstride) {
   PrimM P;
   Islands I;
   int st = prim_mixed(em, qh, ql, P, I);
@@ -203,22 +240,24 @@ __device__ __forceinline__ float mixed_cell_lambda_of(const EosMixed& em, const 
   const float l = lambda_mixed(em, P, c);
   if (!(l <= 3.0e38f)) st |= HYP_CELL_NONFINITE;
   if (st) mixed_record_err(S, st, i);
-  lam_out[i] = l;
-  isl_out[i] = I.ir;
-  isl_out[n + i] = I.e_int;
-  isl_out[2 * n + i] = I.sm1;
+  q[kRowLam * rstride] = l;
+  q[kRowIsl * rstride] = I.ir;
+  q[(kRowIsl + 1) * rstride] = I.e_int;
+  q[(kRowIsl + 2) * rstride] = I.sm1;
   return l;
 }
-__device__ __forceinline__ float mixed_cell_lambda(const MixedArrays& a, const EosMixed& em, int64_t i, DevState* S,
-                                                   float* lam_out, float* isl_out) {
-  const int64_t n = a.stride;
+// The same for cell i of a.in, written into a.in's own block (an upload's state).
+template <bool kTiled>
+__device__ __forceinline__ float mixed_cell_lambda(const MixedArrays& a, const EosMixed& em, int64_t i, DevState* S) {
+  const int64_t r = rows_apart<kTiled>(a);
+  float* q = const_cast<float*>(a.in) + cell_at<kTiled>(i);
   float qh[14], ql[14];
 #pragma unroll
   for (int v = 0; v < 14; ++v) {
-    qh[v] = a.Qh[v * n + i];
-    ql[v] = a.Ql[v * n + i];
+    qh[v] = q[v * r];
+    ql[v] = q[(kRowLo + v) * r];
   }
-  return mixed_cell_lambda_of(em, qh, ql, i, n, S, lam_out, isl_out);
+  return mixed_cell_lambda_of(em, qh, ql, i, S, q, r);
 }
 
 }  // namespace hyp

@@ -20,6 +20,7 @@
 #include <cmath>
 #include <cstring>
 #include <string>
+#include <algorithm>
 #include "hyp_internal.cuh"
 
 using namespace hyp;
@@ -60,37 +61,40 @@ extern "C" int hyp_cell_record_size(const hyp_ctx* c, int* bytes) {
   return HYP_OK;
 }
 
-// Rows of the current state's records: base, pitch (bytes), element size, row count.
-static void record_rows(hyp_ctx* c, char** base, size_t* pitch, size_t* elem, int* rows) {
-  if (c->cfg.precision == HYP_PREC_MIXED) {
-    *base = (char*)c->Qh[c->cur];  // rows 0-31 of the parity's block: hi, lo, lambda, islands
-    *pitch = (size_t)c->mpitch * sizeof(float);
-    *elem = sizeof(float);
-    *rows = kMixedRows;
-  } else {
-    *base = (char*)c->Q[c->cur];
-    *pitch = (size_t)c->n * sizeof(double);
-    *elem = sizeof(double);
-    *rows = 14;
-  }
-}
-
+// Copies the records of cells [first, first + count) between the current state and
+// rec ([rows][count], host or device memory: cudaMemcpyDefault resolves which). FP64:
+// 14 rows of the row-major [14][n] state. Mixed: the 32 rows of the tile-major block,
+// one 2D copy per tile the range touches.
 static int cells_copy(hyp_ctx* c, int64_t first, int64_t count, void* rec, bool to_ctx) {
   if (!c || !rec || count <= 0 || first < 0 || first + count > c->n) return HYP_ERR_INVALID;
   if (c->cfg.model != HYP_MODEL_SINGLE) return ctx_set_err(c, HYP_ERR_UNSUPPORTED, "cell records: single phase only");
   if (!c->has_state) return ctx_set_err(c, HYP_ERR_INVALID, "cell records: no state uploaded");
   SCK(cudaSetDevice(c->device));
-  char* base;
-  size_t pitch, elem;
-  int rows;
-  record_rows(c, &base, &pitch, &elem, &rows);
-  char* dev = base + (size_t)first * elem;
-  const size_t w = (size_t)count * elem;
-  // rec is [rows][count], host or device memory (cudaMemcpyDefault resolves which)
-  if (to_ctx)
-    SCK(cudaMemcpy2DAsync(dev, pitch, rec, w, w, rows, cudaMemcpyDefault, c->stream));
-  else
-    SCK(cudaMemcpy2DAsync(rec, w, dev, pitch, w, rows, cudaMemcpyDefault, c->stream));
+  const bool mixed = c->cfg.precision == HYP_PREC_MIXED;
+  const size_t elem = mixed ? sizeof(float) : sizeof(double);
+  const int rows = mixed ? kMixedRows : 14;
+  const size_t rec_pitch = (size_t)count * elem;
+  for (int64_t i = first; i < first + count;) {
+    char* dev;
+    size_t pitch;
+    int64_t run;
+    if (mixed) {  // the rest of cell i's tile
+      run = std::min<int64_t>(first + count - i, kTileCells - i % kTileCells);
+      dev = (char*)(c->Qh[c->cur] + tile_cell_off(i));
+      pitch = (size_t)kTileCells * sizeof(float);
+    } else {
+      run = first + count - i;
+      dev = (char*)(c->Q[c->cur] + i);
+      pitch = (size_t)c->n * sizeof(double);
+    }
+    char* host = (char*)rec + (size_t)(i - first) * elem;
+    const size_t w = (size_t)run * elem;
+    if (to_ctx)
+      SCK(cudaMemcpy2DAsync(dev, pitch, host, rec_pitch, w, rows, cudaMemcpyDefault, c->stream));
+    else
+      SCK(cudaMemcpy2DAsync(host, rec_pitch, dev, pitch, w, rows, cudaMemcpyDefault, c->stream));
+    i += run;
+  }
   SCK(cudaStreamSynchronize(c->stream));
   if (to_ctx) c->slab_cell_pass = -1;  // a changed cell invalidates an FP64 cell pass
   return HYP_OK;

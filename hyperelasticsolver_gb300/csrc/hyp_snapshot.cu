@@ -290,7 +290,7 @@ static int enqueue_snapshot(hyp_ctx* c, int slot) {
   const double* src = c->Q[c->cur];
   if (c->cfg.precision == HYP_PREC_MIXED) {  // (hi, lo) -> FP64 in the other parity's block
     double* stage = (double*)c->Qh[1 - c->cur];
-    SCK(launch_join(c, c->Qh[c->cur], c->Ql[c->cur], stage));
+    SCK(launch_join(c, c->cur, stage));
     src = stage;
   }
   snapshot_prims_kernel<<<(unsigned)((c->n + 127) / 128), 128, 0, c->stream>>>(snap_arg(c), src, s->dev[slot], c->n);

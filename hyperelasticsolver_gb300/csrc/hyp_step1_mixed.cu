@@ -21,10 +21,16 @@
 //                           FP32 pairs (hyp_mixed_pair.cuh), so one instruction
 //                           advances two cells;
 //   step1_mixed_tma_kernel  a persistent grid; thread 0 of a block prefetches
-//                           the block's next tile (all 32 rows of its cells) with
-//                           2D TMA boxes into shared memory while the block
-//                           computes the current tile from its copy, so loads
-//                           overlap compute.
+//                           the block's next tile (the tile's contiguous span of
+//                           the tile-major block) with one TMA bulk copy into
+//                           shared memory while the block computes the current
+//                           tile from its copy, so loads overlap compute.
+// The state blocks are tile-major (hyp_internal.cuh): a tile's 32 rows are one
+// contiguous 32,512-byte span, which the block reads and writes whole (the halo
+// cells come from the neighbouring spans). Against row-major blocks (each row a
+// separate 1 KB piece 64 MB from the next at 2^24 cells) this measured 0.771
+// against 0.845 ms per step at 2^24 cells; a copy of the same bytes in the two
+// patterns, without the physics: 0.60 against 0.68 ms.
 #include "hyp_internal.cuh"
 #include "hyp_mixed_pair.cuh"
 #include "hyp_mixed_tile.cuh"
@@ -39,7 +45,9 @@ struct MixedSlots {
 };
 
 // t, the step count and the max-lambda slots (block 0, thread 0); returns
-// whether the step is active and dt/dx.
+// whether the step is active and dt/dx. Every thread reads the control itself: a
+// lane-0 read broadcast by shuffles measured 0.939 against 0.847 ms per step at
+// 2^24 cells (the cell loads issued ahead of it no longer overlap it).
 __device__ __forceinline__ bool mixed_step_prologue(const MixedSlots& sl, DevState* S, double t_end, double cfl,
                                                     double dx, float& dtdx) {
   const double tn = S->t[sl.p];
@@ -61,12 +69,12 @@ __global__ void __launch_bounds__(kBlock, 4)
     step1_mixed_kernel(MixedArrays a, EosMixed em, MixedSlots sl, DevState* S, double t_end, double cfl, double dx,
                        int flux, int bc) {
   const int64_t first = (int64_t)blockIdx.x * kTileM;
-  const MixedGlobalLoader<kBlock> ld{a};
+  const MixedGlobalLoader<kBlock, true> ld{a};
   MixedCellIn c;
   mixed_tile_load(first, 0, a.n, ld, c);  // issued before the control reads below
   float dtdx;
   if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
-  float l = mixed_tile_run<kBlock>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld, c);
+  float l = mixed_tile_run<kBlock, true, true>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld, c);
   const int64_t i = first - 1 + threadIdx.x;
   if (i < a.own_lo || i >= a.own_hi) l = 0.0f;  // a slab's ghost cells: their owner reports them
   const float m = mixed_block_max<kBlock>(l);
@@ -89,22 +97,25 @@ __global__ void __launch_bounds__(BLOCK, 4)
   __shared__ float2 sFF[14][BLOCK];  // cell fluxes (11 slots), then the face fluxes (14)
   __shared__ float2 sQ[14][BLOCK];
   __shared__ float2 sL[BLOCK];
-  const int64_t n = a.stride, hi = a.n;
+  constexpr int64_t r = kTileCells;
+  const int64_t hi = a.n;
   const int j = threadIdx.x;
   const int64_t firstA = (int64_t)blockIdx.x * (2 * M);
   const int64_t iA = firstA - 1 + j, iB = iA + M;  // this thread's cells (halo at j = 0, BLOCK - 1)
   const int64_t cA = iA < 0 ? 0 : (iA >= hi ? hi - 1 : iA), cB = iB >= hi ? hi - 1 : iB;
+  const float* qA = a.in + tile_cell_off(cA);
+  const float* qB = a.in + tile_cell_off(cB);
   float2 qh[14], ql[14];
 #pragma unroll
   for (int v = 0; v < 14; ++v) {
-    qh[v] = make_float2(a.Qh[v * n + cA], a.Qh[v * n + cB]);
-    ql[v] = make_float2(a.Ql[v * n + cA], a.Ql[v * n + cB]);
+    qh[v] = make_float2(qA[v * r], qB[v * r]);
+    ql[v] = make_float2(qA[(kRowLo + v) * r], qB[(kRowLo + v) * r]);
   }
-  const float2 li = make_float2(a.lam[cA], a.lam[cB]);
+  const float2 li = make_float2(qA[kRowLam * r], qB[kRowLam * r]);
   IslandsP I0;
-  I0.ir = make_float2(a.isl[cA], a.isl[cB]);
-  I0.e_int = make_float2(a.isl[n + cA], a.isl[n + cB]);
-  I0.sm1 = make_float2(a.isl[2 * n + cA], a.isl[2 * n + cB]);
+  I0.ir = make_float2(qA[kRowIsl * r], qB[kRowIsl * r]);
+  I0.e_int = make_float2(qA[(kRowIsl + 1) * r], qB[(kRowIsl + 1) * r]);
+  I0.sm1 = make_float2(qA[(kRowIsl + 2) * r], qB[(kRowIsl + 2) * r]);
   float dtdx;
   if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
   const bool inner = j > 0 && j < BLOCK - 1;
@@ -186,26 +197,28 @@ __global__ void __launch_bounds__(BLOCK, 4)
       if (st >> 8) mixed_record_err(S, st >> 8, iB);
     }
     if (ownA) {
+      float* q = a.out + tile_cell_off(iA);
 #pragma unroll
       for (int v = 0; v < 14; ++v) {
-        a.Qh_out[v * n + iA] = qh[v].x;
-        a.Ql_out[v * n + iA] = ql[v].x;
+        q[v * r] = qh[v].x;
+        q[(kRowLo + v) * r] = ql[v].x;
       }
-      a.lam_out[iA] = lA;
-      a.isl_out[iA] = I.ir.x;
-      a.isl_out[n + iA] = I.e_int.x;
-      a.isl_out[2 * n + iA] = I.sm1.x;
+      q[kRowLam * r] = lA;
+      q[kRowIsl * r] = I.ir.x;
+      q[(kRowIsl + 1) * r] = I.e_int.x;
+      q[(kRowIsl + 2) * r] = I.sm1.x;
     }
     if (ownB) {
+      float* q = a.out + tile_cell_off(iB);
 #pragma unroll
       for (int v = 0; v < 14; ++v) {
-        a.Qh_out[v * n + iB] = qh[v].y;
-        a.Ql_out[v * n + iB] = ql[v].y;
+        q[v * r] = qh[v].y;
+        q[(kRowLo + v) * r] = ql[v].y;
       }
-      a.lam_out[iB] = lB;
-      a.isl_out[iB] = I.ir.y;
-      a.isl_out[n + iB] = I.e_int.y;
-      a.isl_out[2 * n + iB] = I.sm1.y;
+      q[kRowLam * r] = lB;
+      q[kRowIsl * r] = I.ir.y;
+      q[(kRowIsl + 1) * r] = I.e_int.y;
+      q[(kRowIsl + 2) * r] = I.sm1.y;
     }
   }
   // a slab's ghost cells: their owner reports them
@@ -217,84 +230,75 @@ __global__ void __launch_bounds__(BLOCK, 4)
 
 // ---- TMA-prefetched persistent kernel ----------------------------------------
 
-constexpr int kBoxW = 132;  // box width: 128 cells + 4 so that a box starting at the
-                            // 16-byte boundary below the tile's first cell covers it
-template <int BLOCK>
-struct TmaTile {
-  // boxes at 128-column steps; a tile needs BLOCK + 3 columns: 128 (kBoxes - 1) + kBoxW >= BLOCK + 3
-  static constexpr int kBoxes = (BLOCK - 2) / 128 + 1;
-  static_assert(128 * (kBoxes - 1) + kBoxW >= BLOCK + 3, "boxes cover the tile");
-  static constexpr int kStageFloats = kBoxes * kMixedRows * kBoxW;
-  static constexpr unsigned kBytes = kStageFloats * 4u;  // bytes one tile load delivers
-  static constexpr unsigned kSmem = kBytes + 128u;        // dynamic shared memory (alignment slack)
-};
+// A tile's span of the tile-major block (32 rows x kTileCells floats) staged in
+// shared memory by one bulk copy.
+constexpr unsigned kTmaTileBytes = kTileFloats * 4u;  // 32,512 bytes, a multiple of 16
+constexpr unsigned kTmaSmem = kTmaTileBytes + 128u;   // dynamic shared memory (alignment slack)
 
-// Loads a cell's inputs from the staged tile: column c of the stage holds cell
-// x0 + c. The face phase reads neighbours' hi parts from the stage as well, so
-// the next tile is prefetched (release) once the faces are computed.
+// Loads a cell's inputs from the staged tile (its owned cells; `first` its first
+// cell) or, for a halo cell in a neighbouring tile, from global memory; the halo
+// cells' hi parts are kept in shared memory for the face phase. The next tile is
+// copied in (release) once the faces have read the stage.
 template <int BLOCK>
 struct MixedStageLoader {
-  const float* stage;  // [kBoxes][32][kBoxW]
-  int64_t x0;          // first staged cell
+  const float* stage;   // [32][kTileCells]
+  const MixedArrays& a;
+  float2 (*halo)[7];    // [2][7]: the left / right halo cell's hi parts
+  int64_t first;
   uint64_t* bar;
-  const CUtensorMap* map;
-  int64_t next_x0;     // the block's next tile (< -4: none)
-  int row0;            // first row of the state's parity in the tensor
-  __device__ __forceinline__ const float* column(int64_t ic) const {
-    const int col = (int)(ic - x0);
-    const int b = min(col >> 7, TmaTile<BLOCK>::kBoxes - 1);
-    return stage + b * (kMixedRows * kBoxW) + (col - 128 * b);
-  }
+  const float* next;    // the next tile's span in global memory (null: none)
+  __device__ __forceinline__ bool staged(int64_t ic) const { return ic >= first && ic < first + kTileCells; }
   __device__ __forceinline__ void operator()(int, int64_t ic, MixedCellIn& c) const {
-    const float* s = column(ic);
+    const float* q = staged(ic) ? stage + (ic - first) : a.in + tile_cell_off(ic);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
-      c.qh[v] = s[v * kBoxW];
-      c.ql[v] = s[(14 + v) * kBoxW];
+      c.qh[v] = q[v * kTileCells];
+      c.ql[v] = q[(kRowLo + v) * kTileCells];
     }
-    c.li = s[28 * kBoxW];
-    c.I0.ir = s[29 * kBoxW];
-    c.I0.e_int = s[30 * kBoxW];
-    c.I0.sm1 = s[31 * kBoxW];
+    c.li = q[kRowLam * kTileCells];
+    c.I0.ir = q[kRowIsl * kTileCells];
+    c.I0.e_int = q[(kRowIsl + 1) * kTileCells];
+    c.I0.sm1 = q[(kRowIsl + 2) * kTileCells];
   }
-  __device__ __forceinline__ void keep(int, const MixedCellIn&) const {}
-  __device__ __forceinline__ float face_q(int v, int, int64_t ic) const { return column(ic)[v * kBoxW]; }
+  __device__ __forceinline__ void keep(int j, const MixedCellIn& c) const {
+    const int64_t i = first - 1 + j;
+    if ((j == 0 || j == BLOCK - 1) && !staged(i < 0 ? 0 : (i >= a.n ? a.n - 1 : i)))
+#pragma unroll
+      for (int k = 0; k < 7; ++k) halo[j == 0 ? 0 : 1][k] = pair_of(c.qh, k);
+  }
+  __device__ __forceinline__ float2 face_q2(int k, int j, int64_t ic) const {
+    if (!staged(ic)) return halo[j == 0 ? 0 : 1][k];
+    const float* s = stage + (ic - first);
+    return make_float2(s[2 * k * kTileCells], s[(2 * k + 1) * kTileCells]);
+  }
   // called after a barrier that follows the block's last read of the stage
   __device__ __forceinline__ void release() const {
-    if (threadIdx.x == 0 && next_x0 >= -4) {
+    if (threadIdx.x == 0 && next) {
       fence_proxy_async_smem();
-      mbar_arrive_expect_tx(bar, TmaTile<BLOCK>::kBytes);
-      for (int b = 0; b < TmaTile<BLOCK>::kBoxes; ++b)
-        tma_load_2d(const_cast<float*>(stage) + b * (kMixedRows * kBoxW), map, bar, (int)(next_x0 + 128 * b), row0);
+      mbar_arrive_expect_tx(bar, kTmaTileBytes);
+      bulk_load(const_cast<float*>(stage), next, kTmaTileBytes, bar);
     }
   }
 };
-
-// x of the first staged cell of a tile whose first owned cell is `first`: the
-// halo cell first - 1 rounded down to a multiple of 4 (the TMA x alignment).
-__device__ __forceinline__ int64_t stage_x0(int64_t first) { return (first - 1) & ~int64_t(3); }
 
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB)
-    step1_mixed_tma_kernel(const __grid_constant__ CUtensorMap map, MixedArrays a, EosMixed em, MixedSlots sl,
-                           DevState* S, double t_end, double cfl, double dx, int flux, int bc, int ntiles,
-                           int wait_tries) {
+    step1_mixed_tma_kernel(MixedArrays a, EosMixed em, MixedSlots sl, DevState* S, double t_end, double cfl, double dx,
+                           int flux, int bc, int ntiles, int wait_tries) {
+  static_assert(BLOCK == kTileCells + 2, "a block steps one tile of the tile-major block");
   extern __shared__ __align__(128) float stage_raw[];
   __shared__ __align__(8) uint64_t bar;
+  __shared__ float2 halo[2][7];
   float dtdx;
   if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
-  // TMA destinations must be 128-byte aligned in shared memory (the launch adds 128 bytes of slack)
+  // bulk-copy destinations are 16-byte aligned (128 here; the launch adds 128 bytes of slack)
   float* stage = stage_raw + ((128u - (smem_addr(stage_raw) & 127u)) & 127u) / 4u;
-  constexpr int64_t kT = BLOCK - 2;
-  const int row0 = kMixedRows * sl.p;
   int tile = blockIdx.x;
   if (threadIdx.x == 0) {
     mbar_init(&bar, 1);
     if (tile < ntiles) {
-      mbar_arrive_expect_tx(&bar, TmaTile<BLOCK>::kBytes);
-      const int64_t x0 = stage_x0(tile * kT);
-      for (int b = 0; b < TmaTile<BLOCK>::kBoxes; ++b)
-        tma_load_2d(stage + b * (kMixedRows * kBoxW), &map, &bar, (int)(x0 + 128 * b), row0);
+      mbar_arrive_expect_tx(&bar, kTmaTileBytes);
+      bulk_load(stage, a.in + (int64_t)tile * kTileFloats, kTmaTileBytes, &bar);
     }
   }
   __syncthreads();
@@ -303,17 +307,18 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   for (; tile < ntiles; tile += gridDim.x) {
     const bool ok = mbar_wait_bounded(&bar, phase, wait_tries);
     if (__syncthreads_or(!ok)) {
-      if (threadIdx.x == 0) mixed_record_err(S, HYP_CELL_TIMEOUT, tile * kT);
-      // the awaited box copy is the block's only one in flight: let it land (again a
+      if (threadIdx.x == 0) mixed_record_err(S, HYP_CELL_TIMEOUT, (long long)tile * kTileCells);
+      // the awaited copy is the block's only one in flight: let it land (again a
       // bounded wait) before the block's shared memory goes away
       mbar_wait_bounded(&bar, phase, kDrainTries);
       return;
     }
     phase ^= 1u;
-    const int64_t first = tile * kT;
+    const int64_t first = (int64_t)tile * kTileCells;
     const int next = tile + gridDim.x;
-    MixedStageLoader<BLOCK> ld{stage, stage_x0(first), &bar, &map, next < ntiles ? stage_x0(next * kT) : -8, row0};
-    m = fmaxf(m, mixed_tile<BLOCK>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld));
+    MixedStageLoader<BLOCK> ld{stage, a, halo, first, &bar,
+                               next < ntiles ? a.in + (int64_t)next * kTileFloats : nullptr};
+    m = fmaxf(m, mixed_tile<BLOCK, true>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld));
   }
   m = mixed_block_max<BLOCK>(m);
   if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
@@ -326,7 +331,7 @@ __global__ void __launch_bounds__(kBlock) lam1_mixed_kernel(MixedArrays a, EosMi
                                                             DevState* S) {
   const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
   float l = 0.0f;
-  if (i < a.n) l = mixed_cell_lambda(a, em, i, S, a.lam_out, a.isl_out);
+  if (i < a.n) l = mixed_cell_lambda<true>(a, em, i, S);
   const float m = mixed_block_max<kBlock>(l);
   if (threadIdx.x == 0) atomicMax(slot, (unsigned long long)__float_as_uint(m));
 }
@@ -336,22 +341,24 @@ __global__ void __launch_bounds__(kBlock) lam1_mixed_kernel(MixedArrays a, EosMi
 // memory that the device maps, so that the host link is the only transfer), splits
 // them into (hi, lo) pairs exactly as split_kernel does, and computes the cell's
 // wave speed and island outputs from those pairs exactly as lam1_mixed_kernel does
-// (max into `slot`). a: parity-0 arrays as outputs (Qh_out, Ql_out, lam_out, isl_out).
+// (max into `slot`). a.out: the parity-0 block.
 __global__ void __launch_bounds__(kBlock) install1_mixed_kernel(const double* __restrict__ q, MixedArrays a,
                                                                 EosMixed em, unsigned long long* slot, DevState* S) {
   const int64_t i = (int64_t)blockIdx.x * kBlock + threadIdx.x;
   float l = 0.0f;
   if (i < a.n) {
     float qh[14], ql[14];
+    float* o = a.out + tile_cell_off(i);
+    constexpr int64_t r = kTileCells;
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
       const double x = q[v * a.n + i];
       qh[v] = (float)x;
       ql[v] = (float)(x - (double)qh[v]);
-      a.Qh_out[v * a.stride + i] = qh[v];
-      a.Ql_out[v * a.stride + i] = ql[v];
+      o[v * r] = qh[v];
+      o[(kRowLo + v) * r] = ql[v];
     }
-    l = mixed_cell_lambda_of(em, qh, ql, i, a.stride, S, a.lam_out, a.isl_out);
+    l = mixed_cell_lambda_of(em, qh, ql, i, S, o, r);
   }
   const float m = mixed_block_max<kBlock>(l);
   if (threadIdx.x == 0) atomicMax(slot, (unsigned long long)__float_as_uint(m));
@@ -376,6 +383,17 @@ __global__ void join_kernel(const float* __restrict__ hi, const float* __restric
   }
 }
 
+// Tile-major single-phase block -> FP64 rows v0 .. v0 + rows - 1 of [14][n] (q points
+// at row v0): hi + lo of each variable.
+__global__ void join1_tiled_kernel(const float* __restrict__ base, double* __restrict__ q, int64_t n, int v0,
+                                   int64_t m) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
+    const int v = v0 + (int)(k / n);
+    const float* c = base + tile_cell_off(k % n) + (int64_t)v * kTileCells;
+    q[k] = (double)c[0] + (double)c[kRowLo * kTileCells];
+  }
+}
+
 unsigned elementwise_grid(int64_t m) {
   int64_t g = (m + kBlock - 1) / kBlock;
   return (unsigned)(g > 152 * 64 ? 152 * 64 : (g < 1 ? 1 : g));
@@ -394,21 +412,23 @@ cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, doub
 cudaError_t launch_split(hyp_ctx* c, const double* q, float* hi, float* lo) {
   return launch_split_n(c->stream, q, hi, lo, c->nvar, c->n, c->mpitch);
 }
-cudaError_t launch_join(hyp_ctx* c, const float* hi, const float* lo, double* q) {
-  return launch_join_n(c->stream, hi, lo, q, c->nvar, c->n, c->mpitch);
+// The FP64 state [nvar][n] of parity p: rows v0 .. v0 + rows - 1 into q (row v0 first).
+cudaError_t launch_join_rows(hyp_ctx* c, int p, double* q, int v0, int rows) {
+  if (c->cfg.model == HYP_MODEL_SINGLE) {
+    const int64_t m = (int64_t)rows * c->n;
+    join1_tiled_kernel<<<elementwise_grid(m), kBlock, 0, c->stream>>>(c->Qh[p], q, c->n, v0, m);
+    return cudaGetLastError();
+  }
+  return launch_join_n(c->stream, c->Qh[p] + (size_t)v0 * c->mpitch, c->Ql[p] + (size_t)v0 * c->mpitch, q, rows, c->n,
+                       c->mpitch);
 }
+cudaError_t launch_join(hyp_ctx* c, int p, double* q) { return launch_join_rows(c, p, q, 0, c->nvar); }
 
 static MixedArrays arrays_of(hyp_ctx* c, int p) {
   MixedArrays a;
-  a.Qh = c->Qh[p];
-  a.Ql = c->Ql[p];
-  a.lam = c->lamf[p];
-  a.isl = c->isl[p];
-  a.Qh_out = c->Qh[1 - p];
-  a.Ql_out = c->Ql[1 - p];
-  a.lam_out = c->lamf[1 - p];
-  a.isl_out = c->isl[1 - p];
-  a.stride = c->mpitch;
+  a.in = c->Qh[p];
+  a.out = c->Qh[1 - p];
+  a.rstride = kTileCells;
   a.n = c->n;
   a.own_lo = c->slab && c->slab_ghost[0] ? 1 : 0;
   a.own_hi = c->slab && c->slab_ghost[1] ? c->n - 1 : c->n;
@@ -424,29 +444,20 @@ cudaError_t launch_install1_mixed(hyp_ctx* c, const double* q, unsigned long lon
 
 cudaError_t launch_lam1_mixed(hyp_ctx* c, int p, unsigned long long* slot) {
   const unsigned grid = (unsigned)((c->n + kBlock - 1) / kBlock);
-  MixedArrays a = arrays_of(c, p);
-  a.lam_out = c->lamf[p];  // the uploaded state's own lambda and islands
-  a.isl_out = c->isl[p];
+  MixedArrays a = arrays_of(c, p);  // the uploaded state's own lambda and islands, into its own block
   lam1_mixed_kernel<<<grid, kBlock, 0, c->stream>>>(a, c->eos_mixed, slot, c->st);
   return cudaGetLastError();
 }
 
-// Prepares the TMA kernel for a context: tensor map over both parities, grid.
-// The one-block-per-tile kernel stays the default: on GB300 it measured faster
-// (0.89 vs 0.96 ms per step at 2^24 cells), the TMA body needing more registers
-// than 4 resident blocks per SM allow.
+// Prepares the TMA kernel for a context: its shared memory and persistent grid.
 int setup_mixed_tma(hyp_ctx* c) {
-  if (encode_tmap_2d_f32(&c->tmap, c->mixed_base, c->mpitch, 2 * kMixedRows, kBoxW, kMixedRows) != 0) return 1;
   auto kern = step1_mixed_tma_kernel<kTmaBlock, kTmaMinB>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)TmaTile<kTmaBlock>::kSmem) !=
-      cudaSuccess)
-    return 1;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTmaSmem) != cudaSuccess) return 1;
   int nb = 0, sms = 0;
-  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kTmaBlock, TmaTile<kTmaBlock>::kSmem) != cudaSuccess ||
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&nb, kern, kTmaBlock, kTmaSmem) != cudaSuccess ||
       cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, c->device) != cudaSuccess || nb < 1)
     return 1;
-  const int64_t ntiles = (c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2);
-  c->tma_grid = (int)std::min<int64_t>(ntiles, (int64_t)sms * nb);
+  c->tma_grid = (int)std::min<int64_t>(mixed_tiles(c->n), (int64_t)sms * nb);
   return 0;
 }
 
@@ -459,10 +470,9 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
   sl.clr = (int)((k + 2) % 3);
   const double dx = ctx_dx(c);
   if (c->mixed_kind == HYP_MIXED_TMA && !c->slab) {
-    const int ntiles = (int)((c->n + (kTmaBlock - 2) - 1) / (kTmaBlock - 2));
-    step1_mixed_tma_kernel<kTmaBlock, kTmaMinB><<<c->tma_grid, kTmaBlock, TmaTile<kTmaBlock>::kSmem, c->stream>>>(
-        c->tmap, arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc, ntiles,
-        c->wait_tries);
+    step1_mixed_tma_kernel<kTmaBlock, kTmaMinB><<<c->tma_grid, kTmaBlock, kTmaSmem, c->stream>>>(
+        arrays_of(c, p), c->eos_mixed, sl, c->st, t_end, c->cfg.cfl, dx, c->cfg.flux, c->cfg.bc,
+        (int)mixed_tiles(c->n), c->wait_tries);
   } else if (c->mixed_kind == HYP_MIXED_PAIR) {
     const int64_t ntiles = (c->n + (kPairBlock - 2) - 1) / (kPairBlock - 2);
     step1_mixed_pair_kernel<kPairBlock><<<(unsigned)((ntiles + 1) / 2), kPairBlock, 0, c->stream>>>(
@@ -476,25 +486,3 @@ cudaError_t launch_step1_mixed(hyp_ctx* c, long long k, double t_end) {
 }
 
 }  // namespace hyp
-
-// ---- host: tensor-map encoding through the driver entry point ------------------
-int hyp::encode_tmap_2d_f32(CUtensorMap* map, const float* base, int64_t pitch, int64_t rows, int box_w, int box_h) {
-  static PFN_cuTensorMapEncodeTiled_v12000 encode = nullptr;
-  if (!encode) {
-    void* fn = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
-        q != cudaDriverEntryPointSuccess || !fn)
-      return 1;
-    encode = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(fn);
-  }
-  if (pitch % 4 != 0 || box_w % 4 != 0 || box_w > 256 || box_h > 256) return 1;
-  cuuint64_t dims[2] = {(cuuint64_t)pitch, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)pitch * sizeof(float)};
-  cuuint32_t box[2] = {(cuuint32_t)box_w, (cuuint32_t)box_h};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = encode(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float*>(base), dims, strides, box, estr,
-                      CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
-                      CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  return r == CUDA_SUCCESS ? 0 : 1;
-}

@@ -1,16 +1,13 @@
-// hyp_tma.cuh -- tensor-memory-accelerator (TMA) tile loads with an mbarrier,
-// as inline PTX, and the host-side tensor-map encoding.
+// hyp_tma.cuh -- tensor-memory-accelerator (TMA) bulk copies into shared memory
+// with an mbarrier, as inline PTX.
 //
-// A tile load is one cp.async.bulk.tensor.2d per box, issued by one thread,
-// completing on an mbarrier whose transaction count the same thread set with
-// arrive.expect_tx. Every wait on the barrier is bounded: a waiter that gives
+// A tile load is one cp.async.bulk of the tile's contiguous span, issued by one
+// thread, completing on an mbarrier whose transaction count the same thread set
+// with arrive.expect_tx. Every wait on the barrier is bounded: a waiter that gives
 // up reports it, and the kernel records HYP_CELL_TIMEOUT and returns.
-// Rules kept by the callers: the x coordinate of a box is a multiple of 4
-// floats (16 bytes); the row pitch is a multiple of 16 bytes; boxes are at most
-// 256 elements wide; the shared-memory destination is 128-byte aligned.
+// Rules kept by the callers: source and destination 16-byte aligned, the size a
+// multiple of 16 bytes.
 #pragma once
-#include <cuda.h>
-#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <stdint.h>
 
@@ -56,17 +53,13 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity
   return false;
 }
 
-// One 2D box of the tensor `map` at element coordinates (x, y) into shared memory.
-__device__ __forceinline__ void tma_load_2d(void* dst, const CUtensorMap* map, uint64_t* bar, int x, int y) {
-  asm volatile(
-      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
-          smem_addr(dst)),
-      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(smem_addr(bar))
-      : "memory");
+// `bytes` contiguous bytes of global memory at src into shared memory at dst,
+// completing on `bar`.
+__device__ __forceinline__ void bulk_load(void* dst, const void* src, unsigned bytes, uint64_t* bar) {
+  asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                   smem_addr(dst)),
+               "l"(__cvta_generic_to_global(src)), "r"(bytes), "r"(smem_addr(bar))
+               : "memory");
 }
-
-// Host: a 2D FP32 tensor map over rows x cols floats (row pitch `pitch` floats)
-// with boxes of box_w x box_h; out-of-range elements read as zero.
-int encode_tmap_2d_f32(CUtensorMap* map, const float* base, int64_t pitch, int64_t rows, int box_w, int box_h);
 
 }  // namespace hyp
