@@ -82,10 +82,11 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     const TileCtl k = ctl[tix];
     const MixedGlobalLoader<BLOCK> ld{a};
     MixedCellIn c;
-    mixed_tile_load(d.first, d.lo, d.hi, ld, c);
+    mixed_tile_load<BLOCK>(d.first, d.lo, d.hi, ld, c);
     if (!k.active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
-      const int64_t i = d.first - 1 + threadIdx.x;
-      if (threadIdx.x > 0 && threadIdx.x < BLOCK - 1 && i < d.hi)
+      const int j = tile_local<BLOCK>();
+      const int64_t i = d.first - 1 + j;
+      if (j > 0 && j < BLOCK - 1 && i < d.hi)
         mixed_store_cell(a.out + i, a.rstride, c.qh, c.ql, c.li, c.I0);
       continue;
     }

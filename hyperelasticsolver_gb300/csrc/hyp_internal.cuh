@@ -122,15 +122,17 @@ struct SnapBuf;
 // parts, 14-27 lo parts, 28 the cell's wave speed, 29-31 its island outputs.
 // Row-major blocks (the batch solver, the two-phase step's 60 rows): row r of cell
 // i at r * pitch + i. Tile-major blocks (the single-phase step): cells in tiles of
-// kTileCells, each tile's 32 rows of kTileCells floats contiguous (32,512 bytes), so
-// that the block that steps a tile reads and writes one contiguous span.
+// kTileCells, each tile's 32 rows of kTileRow floats (its cells, then 2 unused)
+// contiguous (32 KB, 128-byte aligned rows), so that the block that steps a tile
+// reads and writes one contiguous span in whole 128-byte lines.
 constexpr int kMixedRows = 32;
 constexpr int kRowLo = 14, kRowLam = 28, kRowIsl = 29;
 constexpr int kTileCells = 254;  // owned cells of a 256-thread tile
-constexpr int kTileFloats = kMixedRows * kTileCells;
+constexpr int kTileRow = 256;    // floats from one row of a tile to the next
+constexpr int kTileFloats = kMixedRows * kTileRow;
 __host__ __device__ __forceinline__ int64_t mixed_pitch(int64_t n) { return (n + 3) & ~int64_t(3); }
 __host__ __device__ __forceinline__ int64_t mixed_tiles(int64_t n) { return (n + kTileCells - 1) / kTileCells; }
-// Offset of cell i's row 0 in a tile-major block (row r at + r * kTileCells).
+// Offset of cell i's row 0 in a tile-major block (row r at + r * kTileRow).
 __host__ __device__ __forceinline__ int64_t tile_cell_off(int64_t i) {
   const unsigned t = (unsigned)i / kTileCells;  // cells < 2^31: the state of 2^31 cells exceeds the device
   return (int64_t)t * kTileFloats + (int64_t)((unsigned)i - t * kTileCells);

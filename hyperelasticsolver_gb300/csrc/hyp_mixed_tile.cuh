@@ -23,7 +23,7 @@ namespace hyp {
 
 // A step's input and output state blocks (32 rows per cell: kRowLo, kRowLam,
 // kRowIsl), row-major (row r of cell i at r * rstride + i) or tile-major (at
-// tile_cell_off(i) + r * kTileCells).
+// tile_cell_off(i) + r * kTileRow).
 struct MixedArrays {
   const float* in;
   float* out;
@@ -35,7 +35,7 @@ struct MixedArrays {
 // cell's 32 rows are immediate offsets from one address; else row-major.
 template <bool kTiled>
 __device__ __forceinline__ int64_t rows_apart(const MixedArrays& a) {
-  return kTiled ? (int64_t)kTileCells : a.rstride;
+  return kTiled ? (int64_t)kTileRow : a.rstride;
 }
 template <bool kTiled>
 __device__ __forceinline__ int64_t cell_at(int64_t i) {
@@ -134,14 +134,24 @@ __device__ __forceinline__ float mixed_block_max(float v) {
 // read the step's control data (time, max lambda), so that the cell loads do not
 // wait behind those. mixed_tile_run then takes the step and returns this
 // thread's new wave speed (0 if it owns no cell).
-__device__ __forceinline__ int64_t tile_cell(int64_t first, int64_t lo, int64_t hi) {
-  const int64_t i = first - 1 + threadIdx.x;     // cell of this thread (halo at j = 0, BLOCK - 1)
+// Position in the tile (0 = left halo, 1 .. BLOCK-2 the owned cells, BLOCK-1 the
+// right halo) of this thread's cell: threads 0 .. BLOCK-3 take the owned cells, so
+// that warp w's 32 cells are the 128-byte line at 32 w of each tile-major row;
+// thread BLOCK-2 the right halo, thread BLOCK-1 the left.
+template <int BLOCK>
+__device__ __forceinline__ int tile_local() {
+  const int t = threadIdx.x;
+  return t == BLOCK - 1 ? 0 : t + 1;
+}
+__device__ __forceinline__ int64_t tile_cell(int64_t first, int64_t lo, int64_t hi, int j) {
+  const int64_t i = first - 1 + j;               // cell at position j
   return i < lo ? lo : (i >= hi ? hi - 1 : i);  // ghost cells copy the end cells
 }
-template <class Loader>
+template <int BLOCK, class Loader>
 __device__ __forceinline__ void mixed_tile_load(int64_t first, int64_t lo, int64_t hi, const Loader& load,
                                                 MixedCellIn& c) {
-  load((int)threadIdx.x, tile_cell(first, lo, hi), c);
+  const int j = tile_local<BLOCK>();
+  load(j, tile_cell(first, lo, hi, j), c);
 }
 // kOwnRegs: a face reads its left cell (this thread's) and an update its right face
 // (this thread's) from registers instead of shared memory -- 39 fewer shared loads
@@ -152,9 +162,9 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
                                                 const Loader& load, MixedCellIn& c) {
   __shared__ float2 sF[7][BLOCK];  // per variable pair: cell fluxes, then the face fluxes
   __shared__ float sL[BLOCK];
-  const int j = threadIdx.x;
+  const int j = tile_local<BLOCK>();  // position of this thread's cell in the tile
   const int64_t i = first - 1 + j;
-  const int64_t ic = tile_cell(first, lo, hi);
+  const int64_t ic = tile_cell(first, lo, hi, j);
   float2 fc[7];  // this cell's flux: its own face reads it from registers
   {
     PrimM P;
@@ -225,7 +235,7 @@ __device__ __forceinline__ float mixed_tile(const MixedArrays& a, const EosMixed
                                             int64_t hi, float dtdx, int flux, int bc, DevState* S,
                                             const Loader& load) {
   MixedCellIn c;
-  mixed_tile_load(first, lo, hi, load, c);
+  mixed_tile_load<BLOCK>(first, lo, hi, load, c);
   return mixed_tile_run<BLOCK, true, kTiled>(a, em, first, lo, hi, dtdx, flux, bc, S, load, c);
 }
 

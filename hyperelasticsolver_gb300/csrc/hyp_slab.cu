@@ -81,7 +81,7 @@ static int cells_copy(hyp_ctx* c, int64_t first, int64_t count, void* rec, bool 
     if (mixed) {  // the rest of cell i's tile
       run = std::min<int64_t>(first + count - i, kTileCells - i % kTileCells);
       dev = (char*)(c->Qh[c->cur] + tile_cell_off(i));
-      pitch = (size_t)kTileCells * sizeof(float);
+      pitch = (size_t)kTileRow * sizeof(float);
     } else {
       run = first + count - i;
       dev = (char*)(c->Q[c->cur] + i);

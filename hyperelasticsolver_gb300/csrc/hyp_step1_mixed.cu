@@ -71,11 +71,11 @@ __global__ void __launch_bounds__(kBlock, 4)
   const int64_t first = (int64_t)blockIdx.x * kTileM;
   const MixedGlobalLoader<kBlock, true> ld{a};
   MixedCellIn c;
-  mixed_tile_load(first, 0, a.n, ld, c);  // issued before the control reads below
+  mixed_tile_load<kBlock>(first, 0, a.n, ld, c);  // issued before the control reads below
   float dtdx;
   if (!mixed_step_prologue(sl, S, t_end, cfl, dx, dtdx)) return;
   float l = mixed_tile_run<kBlock, true, true>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld, c);
-  const int64_t i = first - 1 + threadIdx.x;
+  const int64_t i = first - 1 + tile_local<kBlock>();
   if (i < a.own_lo || i >= a.own_hi) l = 0.0f;  // a slab's ghost cells: their owner reports them
   const float m = mixed_block_max<kBlock>(l);
   if (threadIdx.x == 0) atomicMax(&S->lam_slots[sl.wr], (unsigned long long)__float_as_uint(m));
@@ -97,7 +97,7 @@ __global__ void __launch_bounds__(BLOCK, 4)
   __shared__ float2 sFF[14][BLOCK];  // cell fluxes (11 slots), then the face fluxes (14)
   __shared__ float2 sQ[14][BLOCK];
   __shared__ float2 sL[BLOCK];
-  constexpr int64_t r = kTileCells;
+  constexpr int64_t r = kTileRow;
   const int64_t hi = a.n;
   const int j = threadIdx.x;
   const int64_t firstA = (int64_t)blockIdx.x * (2 * M);
@@ -230,9 +230,9 @@ __global__ void __launch_bounds__(BLOCK, 4)
 
 // ---- TMA-prefetched persistent kernel ----------------------------------------
 
-// A tile's span of the tile-major block (32 rows x kTileCells floats) staged in
+// A tile's span of the tile-major block (32 rows x kTileRow floats) staged in
 // shared memory by one bulk copy.
-constexpr unsigned kTmaTileBytes = kTileFloats * 4u;  // 32,512 bytes, a multiple of 16
+constexpr unsigned kTmaTileBytes = kTileFloats * 4u;  // 32 KB, a multiple of 16
 constexpr unsigned kTmaSmem = kTmaTileBytes + 128u;   // dynamic shared memory (alignment slack)
 
 // Loads a cell's inputs from the staged tile (its owned cells; `first` its first
@@ -241,7 +241,7 @@ constexpr unsigned kTmaSmem = kTmaTileBytes + 128u;   // dynamic shared memory (
 // copied in (release) once the faces have read the stage.
 template <int BLOCK>
 struct MixedStageLoader {
-  const float* stage;   // [32][kTileCells]
+  const float* stage;   // [32][kTileRow]
   const MixedArrays& a;
   float2 (*halo)[7];    // [2][7]: the left / right halo cell's hi parts
   int64_t first;
@@ -252,13 +252,13 @@ struct MixedStageLoader {
     const float* q = staged(ic) ? stage + (ic - first) : a.in + tile_cell_off(ic);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
-      c.qh[v] = q[v * kTileCells];
-      c.ql[v] = q[(kRowLo + v) * kTileCells];
+      c.qh[v] = q[v * kTileRow];
+      c.ql[v] = q[(kRowLo + v) * kTileRow];
     }
-    c.li = q[kRowLam * kTileCells];
-    c.I0.ir = q[kRowIsl * kTileCells];
-    c.I0.e_int = q[(kRowIsl + 1) * kTileCells];
-    c.I0.sm1 = q[(kRowIsl + 2) * kTileCells];
+    c.li = q[kRowLam * kTileRow];
+    c.I0.ir = q[kRowIsl * kTileRow];
+    c.I0.e_int = q[(kRowIsl + 1) * kTileRow];
+    c.I0.sm1 = q[(kRowIsl + 2) * kTileRow];
   }
   __device__ __forceinline__ void keep(int j, const MixedCellIn& c) const {
     const int64_t i = first - 1 + j;
@@ -269,7 +269,7 @@ struct MixedStageLoader {
   __device__ __forceinline__ float2 face_q2(int k, int j, int64_t ic) const {
     if (!staged(ic)) return halo[j == 0 ? 0 : 1][k];
     const float* s = stage + (ic - first);
-    return make_float2(s[2 * k * kTileCells], s[(2 * k + 1) * kTileCells]);
+    return make_float2(s[2 * k * kTileRow], s[(2 * k + 1) * kTileRow]);
   }
   // called after a barrier that follows the block's last read of the stage
   __device__ __forceinline__ void release() const {
@@ -349,7 +349,7 @@ __global__ void __launch_bounds__(kBlock) install1_mixed_kernel(const double* __
   if (i < a.n) {
     float qh[14], ql[14];
     float* o = a.out + tile_cell_off(i);
-    constexpr int64_t r = kTileCells;
+    constexpr int64_t r = kTileRow;
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
       const double x = q[v * a.n + i];
@@ -389,8 +389,8 @@ __global__ void join1_tiled_kernel(const float* __restrict__ base, double* __res
                                    int64_t m) {
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < m; k += (int64_t)gridDim.x * blockDim.x) {
     const int v = v0 + (int)(k / n);
-    const float* c = base + tile_cell_off(k % n) + (int64_t)v * kTileCells;
-    q[k] = (double)c[0] + (double)c[kRowLo * kTileCells];
+    const float* c = base + tile_cell_off(k % n) + (int64_t)v * kTileRow;
+    q[k] = (double)c[0] + (double)c[kRowLo * kTileRow];
   }
 }
 
@@ -428,7 +428,7 @@ static MixedArrays arrays_of(hyp_ctx* c, int p) {
   MixedArrays a;
   a.in = c->Qh[p];
   a.out = c->Qh[1 - p];
-  a.rstride = kTileCells;
+  a.rstride = kTileRow;
   a.n = c->n;
   a.own_lo = c->slab && c->slab_ghost[0] ? 1 : 0;
   a.own_hi = c->slab && c->slab_ghost[1] ? c->n - 1 : c->n;
