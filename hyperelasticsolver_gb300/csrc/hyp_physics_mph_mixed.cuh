@@ -167,6 +167,7 @@ __device__ __forceinline__ int cons_to_prim_f2(const EosMixed& em, const float* 
 template <int kDef = -1>
 __device__ __forceinline__ int speeds2_m(const Eos2M& E, const float* Q, float& smin, float& smax) {
   int st = 0;
+#pragma unroll  // static phase indices: the EOS pair stays in the parameter bank, not a local copy
   for (int p = 0; p < 2; ++p) {
     PrimM2 P;
     st |= cons_to_prim_f2<kDef>(E.m[p], Q + 15 * p, P);
