@@ -167,7 +167,9 @@ __device__ __forceinline__ int cons_to_prim_f2(const EosMixed& em, const float* 
 template <int kDef = -1>
 __device__ __forceinline__ int speeds2_m(const Eos2M& E, const float* Q, float& smin, float& smax) {
   int st = 0;
-#pragma unroll  // static phase indices: the EOS pair stays in the parameter bank, not a local copy
+  // phase loop kept rolled: unrolled, the face kernels' code grows and the HLL step
+  // measured 3.08 against 2.72 ms at 2^22 cells (the local copy of the EOS pair it
+  // avoids costs less)
   for (int p = 0; p < 2; ++p) {
     PrimM2 P;
     st |= cons_to_prim_f2<kDef>(E.m[p], Q + 15 * p, P);
