@@ -369,17 +369,26 @@ def workload_summaries(args):
     return out
 
 
-def measure_rates(reps=3, nbytes=1 << 30):
+def measure_rates(reps=3, nbytes=1 << 30, layout_cells=1 << 24):
     """FP64 / FP32 / packed-f32x2 FMA throughput and the host link's copy rates of this GPU
-    (hyp_measure_peaks): the denominators the driver's copy and GEMM peaks do not give."""
+    (hyp_measure_peaks): the denominators the driver's copy and GEMM peaks do not give;
+    and the step's memory traffic without the physics in the row-major and the
+    tile-major state layout (hyp_measure_layouts)."""
     import ctypes
     import hyperelasticsolver_gb300 as h
+    L = h._lib.load()
     out = np.zeros(6)
-    h._lib.check(h._lib.load().hyp_measure_peaks(int(reps), int(nbytes), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+    h._lib.check(L.hyp_measure_peaks(int(reps), int(nbytes), out.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
                  what="hyp_measure_peaks")
+    lay = np.zeros(2)
+    h._lib.check(L.hyp_measure_layouts(int(reps), int(layout_cells), lay.ctypes.data_as(ctypes.POINTER(ctypes.c_double))),
+                 what="hyp_measure_layouts")
     return {"fp64_fma_tflops": out[0], "fp32_fma_tflops": out[1], "fp32x2_fma_tflops": out[2],
             "h2d_gbs": out[3], "d2h_gbs": out[4], "bidirectional_gbs_each_way": out[5],
-            "copy_bytes": nbytes, "note": "best of %d; FMA: 8 independent chains per thread, 8 x 256-thread blocks per SM" % reps}
+            "copy_bytes": nbytes, "step_traffic_rowmajor_gbs": lay[0], "step_traffic_tilemajor_gbs": lay[1],
+            "layout_cells": layout_cells,
+            "note": "best of %d; FMA: 8 independent chains per thread, 8 x 256-thread blocks per SM; "
+                    "step traffic: 256 B per cell, 32 FP32 rows read and written, no physics" % reps}
 
 
 def run_peaks(args):

@@ -129,6 +129,7 @@ _SIGS = {
     "hyp_init_riemann": ([ctypes.c_void_p, _dp, _dp], ctypes.c_int),
     "hyp_init_tanh": ([ctypes.c_void_p, _dp, _dp, ctypes.c_double], ctypes.c_int),
     "hyp_measure_peaks": ([ctypes.c_int, _i64, _dp], ctypes.c_int),
+    "hyp_measure_layouts": ([ctypes.c_int, _i64, _dp], ctypes.c_int),
     "hyp_host_alloc": ([ctypes.c_int64, ctypes.POINTER(ctypes.c_void_p)], ctypes.c_int),
     "hyp_host_free": ([ctypes.c_void_p], ctypes.c_int),
     "hyp_eval_finger": ([_dp, _dp, _i64], ctypes.c_int),

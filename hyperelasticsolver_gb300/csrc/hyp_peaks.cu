@@ -5,6 +5,13 @@
 //
 // FMA: every thread runs 8 independent chains of 4096 fused multiply-adds (no memory
 // traffic), 8 blocks of 256 threads per SM; FLOP/s = 2 x FMAs / kernel time.
+//
+// Layouts (hyp_measure_layouts): the single-phase mixed step's memory traffic -- 32
+// FP32 rows per cell read, the owned cells' 32 rows written -- without the physics,
+// in the two block layouts the step could use: row-major (row r of cell i at
+// r * pitch + i; a 256-thread block reads its 254 cells plus a halo cell each side
+// from every row) and tile-major (the layout the step uses: a tile's 32 rows of 256
+// floats contiguous, warp w reading the 128-byte line at 32 w of each row).
 #include <cuda_runtime.h>
 #include <vector>
 #include "../../include/hyperelastic.h"
@@ -47,6 +54,37 @@ __global__ void __launch_bounds__(256) fma_chains_f32x2(float* out, int iters, f
     s += x + y;
   }
   if (s == 12345.678f) out[0] = s;
+}
+
+__global__ void __launch_bounds__(256, 4) copy_rows_rowmajor(const float* __restrict__ in, float* __restrict__ out,
+                                                              int64_t n, int64_t pitch) {
+  const int64_t first = (int64_t)blockIdx.x * 254;
+  const int64_t i = first - 1 + threadIdx.x;
+  const int64_t ic = i < 0 ? 0 : (i >= n ? n - 1 : i);
+  float v[32];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) v[r] = in[r * pitch + ic];
+  float s = 0.f;
+#pragma unroll
+  for (int r = 0; r < 32; ++r) s += v[r];
+  if (threadIdx.x > 0 && threadIdx.x < 255 && i < n) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) out[r * pitch + i] = v[r] + s * 1e-30f;  // s keeps every load live
+  }
+}
+
+__global__ void __launch_bounds__(256, 4) copy_rows_tilemajor(const float* __restrict__ in, float* __restrict__ out) {
+  const int64_t base = (int64_t)blockIdx.x * (32 * 256) + threadIdx.x;
+  float v[32];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) v[r] = in[base + r * 256];
+  float s = 0.f;
+#pragma unroll
+  for (int r = 0; r < 32; ++r) s += v[r];
+  if (threadIdx.x < 254) {
+#pragma unroll
+    for (int r = 0; r < 32; ++r) out[base + r * 256] = v[r] + s * 1e-30f;
+  }
 }
 
 struct Timer {
@@ -154,5 +192,44 @@ extern "C" int hyp_measure_peaks(int reps, int64_t bytes, double* out) {
   if (d1) cudaFree(d1);
   if (h0) cudaFreeHost(h0);
   if (h1) cudaFreeHost(h1);
+  return rc;
+}
+
+// out[0..1]: GB/s (256 B per cell: 32 FP32 rows read and written) of the single-phase
+// mixed step's memory traffic for n_cells cells in a row-major and in a tile-major
+// block, without the physics; each the best of `reps`.
+extern "C" int hyp_measure_layouts(int reps, int64_t n_cells, double* out) {
+  if (!out || reps < 1 || n_cells < 256) return HYP_ERR_INVALID;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return HYP_ERR_NO_DEVICE;
+  out[0] = out[1] = 0.0;
+  const int64_t tiles = (n_cells + 253) / 254;
+  const int64_t pitch = (n_cells + 3) & ~int64_t(3);
+  const size_t floats = (size_t)32 * (size_t)(tiles * 256 > pitch ? tiles * 256 : pitch);
+  float *a = nullptr, *b = nullptr;
+  int rc = HYP_OK;
+  if (cudaMalloc(&a, floats * sizeof(float)) != cudaSuccess || cudaMalloc(&b, floats * sizeof(float)) != cudaSuccess ||
+      cudaMemset(a, 0, floats * sizeof(float)) != cudaSuccess)
+    rc = HYP_ERR_CUDA;
+  Timer t;
+  const double gb = 256.0 * (double)n_cells / 1e9;
+  float ms = 0.f;
+  for (int r = 0; r < reps + 1 && rc == HYP_OK; ++r) {  // the first round warms up
+    cudaEventRecord(t.a);
+    copy_rows_rowmajor<<<(unsigned)tiles, 256>>>(a, b, n_cells, pitch);
+    cudaEventRecord(t.b);
+    if (cudaEventSynchronize(t.b) != cudaSuccess) rc = HYP_ERR_CUDA;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    if (r > 0) out[0] = fmax(out[0], gb / (ms * 1e-3));
+    cudaEventRecord(t.a);
+    copy_rows_tilemajor<<<(unsigned)tiles, 256>>>(a, b);
+    cudaEventRecord(t.b);
+    if (cudaEventSynchronize(t.b) != cudaSuccess) rc = HYP_ERR_CUDA;
+    cudaEventElapsedTime(&ms, t.a, t.b);
+    if (r > 0) out[1] = fmax(out[1], gb / (ms * 1e-3));
+    if (cudaGetLastError() != cudaSuccess) rc = HYP_ERR_CUDA;
+  }
+  if (a) cudaFree(a);
+  if (b) cudaFree(b);
   return rc;
 }

@@ -384,6 +384,12 @@ function measure_peaks(; reps::Integer=3, bytes::Integer=1 << 30)
   check(ccall((:hyp_measure_peaks, libhyp), Cint, (Cint, Int64, Ptr{Float64}), reps, bytes, out), "hyp_measure_peaks")
   Tuple(out)
 end
+"measure_layouts(; reps, cells): GB/s of the single-phase mixed step's memory traffic without the physics, (row-major, tile-major)"
+function measure_layouts(; reps::Integer=3, cells::Integer=1 << 24)
+  out = zeros(2)
+  check(ccall((:hyp_measure_layouts, libhyp), Cint, (Cint, Int64, Ptr{Float64}), reps, cells, out), "hyp_measure_layouts")
+  Tuple(out)
+end
 "pinned_matrix(n, k): a Matrix{Float64} in page-locked host memory (hyp_host_alloc) for fast copies"
 function pinned_matrix(n::Integer, k::Integer)
   p = Ref{Ptr{Cvoid}}(C_NULL)

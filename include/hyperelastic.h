@@ -314,6 +314,12 @@ int hyp_init_tanh(hyp_ctx* ctx, const double* Ql, const double* Qr, double eps);
    buffers of `bytes`); each the best of `reps`. */
 int hyp_measure_peaks(int reps, int64_t bytes, double* out);
 
+/* The single-phase mixed step's memory traffic (32 FP32 rows per cell read, the
+   owned cells' rows written: 256 B per cell) for n_cells cells without the physics,
+   in a row-major block (out[0], GB/s) and in the tile-major block the step uses
+   (out[1], GB/s); each the best of `reps`. */
+int hyp_measure_layouts(int reps, int64_t n_cells, double* out);
+
 /* Page-locked host memory for staging states (fast, asynchronous-capable copies). */
 int hyp_host_alloc(int64_t bytes, void** out);
 int hyp_host_free(void* p);
