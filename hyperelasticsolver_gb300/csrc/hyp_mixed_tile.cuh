@@ -226,6 +226,12 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
       if (st) mixed_record_err(S, st, i);
     }
     mixed_store_cell(a.out + cell_at<kTiled>(i), rows_apart<kTiled>(a), c.qh, c.ql, lnew, I);
+  } else if (kTiled && BLOCK == kTileCells + 2 && (j == 0 || j == BLOCK - 1)) {
+    // the halo threads fill the two unused floats of each row of the output tile, so
+    // that the last warp writes whole 128-byte lines (no partial sectors for L2 to merge)
+    float* q = a.out + tile_cell_off(first) + (j == 0 ? kTileRow - 1 : kTileRow - 2);
+#pragma unroll
+    for (int r = 0; r < kMixedRows; ++r) q[r * kTileRow] = 0.0f;
   }
   __syncthreads();  // the shared arrays are reused by the block's next tile
   return lnew;
