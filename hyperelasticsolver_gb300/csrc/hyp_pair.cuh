@@ -24,6 +24,21 @@ __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return _
 __device__ __forceinline__ float2 f2rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 __device__ __forceinline__ float2 f2sqrt(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
 __device__ __forceinline__ float2 f2abs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
+// The hardware's approximate reciprocal and square root (PTX rcp.approx.f32 and
+// sqrt.approx.f32: one special-function instruction each, about one ulp from the
+// rounded results) for FP32 states whose own rounding already exceeds that.
+__device__ __forceinline__ float rcp_approx(float a) {
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ float sqrt_approx(float a) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ float2 f2rcp_approx(float2 a) { return make_float2(rcp_approx(a.x), rcp_approx(a.y)); }
+__device__ __forceinline__ float2 f2sqrt_approx(float2 a) { return make_float2(sqrt_approx(a.x), sqrt_approx(a.y)); }
 __device__ __forceinline__ float2 f2max(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
 
 struct ff2 {

@@ -60,7 +60,7 @@ struct PhaseBPair {
 template <int kDef = -1>
 __device__ __forceinline__ int phase_b_pair(const EosPair& e, const float2* q, PhaseBPair& b) {
   const float2* m = q + 6;
-  const float2 ia = f2rcp(q[0]);
+  const float2 ia = f2rcp_approx(q[0]);
   // det3 (cofactor expansion, SimpleLA.jl:84-89) / alpha^3
   const float2 c0 = f2fma(m[4], m[8], f2neg(f2mul(m[5], m[7])));
   const float2 c1 = f2fma(m[1], m[8], f2neg(f2mul(m[7], m[2])));
@@ -68,9 +68,9 @@ __device__ __forceinline__ int phase_b_pair(const EosPair& e, const float2* q, P
   const float2 det = f2fma(m[6], c2, f2fma(f2neg(m[3]), c1, f2mul(m[0], c0)));
   const float2 d = f2mul(det, f2mul(f2mul(ia, ia), ia));
   int st = (d.x > 0.0f && d.y > 0.0f) ? HYP_CELL_OK : HYP_CELL_NEG_DET;
-  const float2 rho = f2sqrt(f2mul(d, e.inv_rho0));
+  const float2 rho = f2sqrt_approx(f2mul(d, e.inv_rho0));
   const float2 den = f2mul(q[0], rho);
-  const float2 idn = f2rcp(den);
+  const float2 idn = f2rcp_approx(den);
   float2 u[3];
   for (int c = 0; c < 3; ++c) u[c] = f2mul(q[2 + c], idn);
   const float2 E = f2mul(q[5], idn);
@@ -80,7 +80,7 @@ __device__ __forceinline__ int phase_b_pair(const EosPair& e, const float2* q, P
   for (int c = 0; c < 9; ++c) A[c] = f2mul(m[c], idn);
   const float2 sf = f2mul(rho, e.inv_rho0);  // 1/det A
   const float2 sm1 = f2add(sf, f2s(-1.0f));
-  const float2 isf = f2rcp(sf);
+  const float2 isf = f2rcp_approx(sf);
   // Finger tensor G = adj(A A^T) p, p = s^2 (Strains.jl:26-32), and row 1 of H = G^2
   const float2 m00 = f2fma(A[6], A[6], f2fma(A[3], A[3], f2mul(A[0], A[0])));
   const float2 m11 = f2fma(A[7], A[7], f2fma(A[4], A[4], f2mul(A[1], A[1])));
@@ -163,7 +163,7 @@ __device__ __forceinline__ int noncons_bcol_pair(const EosPair& e, const float2*
   // interface velocity and stress (HyperelasticityMPh.jl:213-217, k = (1/2, 1/2))
   float uI[3], sI[3];
   for (int a = 0; a < 3; ++a) uI[a] = 0.5f * b.u[a].x + 0.5f * b.u[a].y;
-  const float iden = __frcp_rn(0.5f * b.T.x + 0.5f * b.T.y);
+  const float iden = rcp_approx(0.5f * b.T.x + 0.5f * b.T.y);
   for (int a = 0; a < 3; ++a) sI[a] = ((0.5f * b.T.y) * b.K0[a].x + (0.5f * b.T.x) * b.K0[a].y) * iden;
   bc[0] = f2s(uI[0]);
   bc[1] = f2s(0.0f);
