@@ -11,8 +11,11 @@
 // cons2prim. Everything else -- the Finger tensor, stress,
 // temperature, the non-conservative columns of B (HyperelasticityMPh.jl:178-250),
 // wave speeds, fluxes and the path-conservative HLL / LxF faces
-// (NumFluxes.jl:25-132) -- is FP32, statement for statement as in the FP64 forms.
+// (NumFluxes.jl:25-132) -- is FP32, statement for statement as in the FP64 forms,
+// with the hardware's approximate reciprocal and square root (about one ulp) where
+// the FP64 forms divide or take a root.
 #pragma once
+#include "hyp_pair.cuh"
 #include "hyp_physics_mixed.cuh"
 #include "hyp_physics_mph.cuh"
 
@@ -108,10 +111,10 @@ __device__ __forceinline__ void phase_flux_m2(const EosT<float>& e, float alpha,
 __device__ __forceinline__ float phase_cmax_m2(const EosT<float>& e, const PrimM2& P, const StressCT<float>& c) {
   float s0[3], s0r[3], om[9];
   stress_row0<float>(P.rho_s, P.k, c, s0);
-  const float irs = __frcp_rn(P.rho_s);
+  const float irs = rcp_approx(P.rho_s);
   for (int i = 0; i < 3; ++i) s0r[i] = s0[i] * irs;
   acoustic_omega<float>(e, P.k, P.w, c, P.xm1, s0r, om);
-  return sqrtf(spectral_radius_fast(om));
+  return sqrt_approx(spectral_radius_fast(om));
 }
 
 // Both phases' flux (30) and wave-speed bounds of a cell from its compensated state.
@@ -142,20 +145,20 @@ template <int kDef = -1>
 __device__ __forceinline__ int cons_to_prim_f2(const EosMixed& em, const float* q, PrimM2& P) {
   const EosT<float>& e = em.f;
   const float* m = q + 6;
-  const float ia = __frcp_rn(q[0]);
+  const float ia = rcp_approx(q[0]);
   const float d = det3(m) * (ia * ia * ia);  // det(alpha rho A / alpha)
   int st = d > 0.0f ? HYP_CELL_OK : HYP_CELL_NEG_DET;
-  const float rho = sqrtf(d * e.inv_rho0);
+  const float rho = sqrt_approx(d * e.inv_rho0);
   P.true_den = rho;
   P.den = q[0] * rho;
-  const float idn = __frcp_rn(P.den);
+  const float idn = rcp_approx(P.den);
   for (int c = 0; c < 3; ++c) P.u[c] = q[2 + c] * idn;
   P.E = q[5] * idn;
   P.e_int = P.E - 0.5f * (P.u[0] * P.u[0] + P.u[1] * P.u[1] + P.u[2] * P.u[2]);
   for (int c = 0; c < 9; ++c) P.A[c] = m[c] * idn;
   const float sf = rho * e.inv_rho0;
   P.sm1 = sf - 1.0f;
-  P.k = kinematics_s<float>(P.A, sf, __frcp_rn(sf));
+  P.k = kinematics_s<float>(P.A, sf, rcp_approx(sf));
   P.w = powers<float, kDef>(e, P.k);
   P.w.Pam1 = default_exponents<kDef>(e) ? P.sm1 : expm1f(e.alpha * log1pf(P.sm1));
   P.xm1 = entropy_xm1<float>(e, P.e_int, P.k, P.w);
@@ -207,7 +210,7 @@ __device__ __forceinline__ int noncons_bcol_m(const Eos2M& E, const float* Q, fl
   const int st = phase_b_m<kDef>(E.m[0], Q, b[0]) | phase_b_m<kDef>(E.m[1], Q + 15, b[1]);
   float uI[3], sI[3];
   for (int a = 0; a < 3; ++a) uI[a] = 0.5f * b[0].u[a] + 0.5f * b[1].u[a];
-  const float iden = __frcp_rn(0.5f * b[0].T + 0.5f * b[1].T);
+  const float iden = rcp_approx(0.5f * b[0].T + 0.5f * b[1].T);
   for (int a = 0; a < 3; ++a) sI[a] = ((0.5f * b[1].T) * b[0].K0[a] + (0.5f * b[0].T) * b[1].K0[a]) * iden;
   for (int p = 0; p < 2; ++p) {
     float* r = bcol + 15 * p;
