@@ -6,11 +6,26 @@
 // (Dekker 1971); products, quotients and square roots after Joldes, Muller and
 // Popescu, "Tight and rigorous error bounds for basic building blocks of
 // double-word arithmetic" (ACM TOMS 2017). The _rn intrinsics keep the compiler
-// from contracting or reassociating the error terms.
+// from contracting or reassociating the error terms. A quotient's and a square
+// root's first FP32 approximation comes from the hardware's approximate reciprocal
+// and square root (about one ulp): the correction step that follows takes its error
+// to the square of it (~2^-46 relative), as it does for a rounded first value.
 #pragma once
 #include <cuda_runtime.h>
 
 namespace hyp {
+
+// PTX rcp.approx.f32 / sqrt.approx.f32: one special-function instruction each.
+__device__ __forceinline__ float rcp_approx(float a) {
+  float r;
+  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
+__device__ __forceinline__ float sqrt_approx(float a) {
+  float r;
+  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
+  return r;
+}
 
 struct ff {
   float hi, lo;
@@ -66,7 +81,7 @@ __device__ __forceinline__ ff ff_mul_f(ff a, float b) {
 // remainder in float-float, and one correction (the remainder step removes the
 // first quotient's error, so IEEE division is not needed).
 __device__ __forceinline__ ff ff_div(ff a, ff b) {
-  const float rb = __frcp_rn(b.hi);
+  const float rb = rcp_approx(b.hi);
   float q1 = __fmul_rn(a.hi, rb);
   ff r = ff_sub(a, ff_mul(b, ff{q1, 0.0f}));
   float q2 = __fmul_rn(r.hi, rb);
@@ -75,10 +90,10 @@ __device__ __forceinline__ ff ff_div(ff a, ff b) {
 __device__ __forceinline__ ff ff_recip(ff b) { return ff_div(ff{1.0f, 0.0f}, b); }
 // sqrt(a), a > 0: one Newton correction of the FP32 root in float-float
 __device__ __forceinline__ ff ff_sqrt(ff a) {
-  float s = __fsqrt_rn(a.hi);
+  float s = sqrt_approx(a.hi);
   ff p = two_prod(s, s);
   float r = __fadd_rn(__fsub_rn(__fsub_rn(a.hi, p.hi), p.lo), a.lo);
-  float c = __fmul_rn(r, __fmul_rn(0.5f, __frcp_rn(s)));
+  float c = __fmul_rn(r, __fmul_rn(0.5f, rcp_approx(s)));
   return fast_two_sum(s, c);
 }
 // a*b - c*d with one rounding of the final sum (cofactors of the determinant)

@@ -162,7 +162,7 @@ __device__ __forceinline__ int prim_from_islands_pair(const EosMixed& em, const 
   for (int c = 0; c < 3; ++c) P.u[c] = f2mul(qh[1 + c], ir);
   P.E = f2mul(qh[4], ir);
   for (int c = 0; c < 9; ++c) P.A[c] = f2mul(qh[5 + c], ir);
-  kinematics_pair(P.A, sf, f2rcp(sf), P.k);
+  kinematics_pair(P.A, sf, f2rcp_approx(sf), P.k);
   powers_pair(e, P.k, I.sm1, P.w);
   // entropy argument minus one, clamped at 1e-6 (EquationsOfState.jl:150-154)
   const float2 w_sh = f2mul(f2mul(f2s(0.5f * e.b0sq), P.w.Pb), P.k.psi);
@@ -262,7 +262,7 @@ __device__ __forceinline__ void acoustic_pair(const EosT<float>& e, const PrimP&
 __device__ __forceinline__ void seed_lane(float c0, float c2, float t, float p, float q, float disc, float& seed,
                                           float& other) {
   if (disc < 0.0f && p < 0.0f) {
-    const float m = 2.0f * sqrtf(-p * (1.0f / 3.0f));
+    const float m = 2.0f * sqrt_approx(-p * (1.0f / 3.0f));
     const float cc = fminf(1.0f, fmaxf(-1.0f, __fdividef(3.0f * q, p * m)));
     const float th = acos_seed(cc) * (1.0f / 3.0f);
     const float y0 = m * __cosf(th) + t, y1 = m * __cosf(th - 2.0943951f) + t, y2 = m * __cosf(th - 4.1887902f) + t;
@@ -278,9 +278,9 @@ __device__ __forceinline__ void seed_lane(float c0, float c2, float t, float p, 
       other = fmaxf(a0, a1);
     }
   } else {
-    const float sd = sqrtf(fmaxf(disc, 0.0f));
+    const float sd = sqrt_approx(fmaxf(disc, 0.0f));
     seed = cbrt_seed(-0.5f * q + sd) + cbrt_seed(-0.5f * q - sd) + t;
-    other = seed != 0.0f ? sqrtf(fabsf(__fdividef(c0, seed))) : fabsf(c2);
+    other = seed != 0.0f ? sqrt_approx(fabsf(__fdividef(c0, seed))) : fabsf(c2);
   }
 }
 
@@ -295,7 +295,7 @@ __device__ __forceinline__ float deflate_lane(float c0, float c1, float c2, floa
     qq = c1;
   }
   const float dsc = s * s - 4.0f * qq;
-  return dsc < 0.0f ? sqrtf(fabsf(qq)) : 0.5f * (fabsf(s) + sqrtf(dsc));
+  return dsc < 0.0f ? sqrt_approx(fabsf(qq)) : 0.5f * (fabsf(s) + sqrt_approx(dsc));
 }
 
 // spectral_radius_fast for two 3x3 matrices: the characteristic polynomial and the
@@ -336,7 +336,7 @@ __device__ __forceinline__ float2 lambda_pair(const EosMixed& em, const PrimP& P
   stress_row0_pair(P, c, s0);
   for (int i = 0; i < 3; ++i) s0r[i] = f2mul(s0[i], P.inv_rho_s);
   acoustic_pair(em.f, P, c, s0r, om);
-  return f2add(f2abs(P.u[0]), f2sqrt(spectral_radius_pair(om)));
+  return f2add(f2abs(P.u[0]), f2sqrt_approx(spectral_radius_pair(om)));
 }
 
 }  // namespace hyp

@@ -12,6 +12,7 @@
 // Muller and Popescu, ACM TOMS 2017), lane by lane.
 #pragma once
 #include <cuda_runtime.h>
+#include "hyp_ff.cuh"
 
 namespace hyp {
 
@@ -24,19 +25,8 @@ __device__ __forceinline__ float2 f2fma(float2 a, float2 b, float2 c) { return _
 __device__ __forceinline__ float2 f2rcp(float2 a) { return make_float2(__frcp_rn(a.x), __frcp_rn(a.y)); }
 __device__ __forceinline__ float2 f2sqrt(float2 a) { return make_float2(sqrtf(a.x), sqrtf(a.y)); }
 __device__ __forceinline__ float2 f2abs(float2 a) { return make_float2(fabsf(a.x), fabsf(a.y)); }
-// The hardware's approximate reciprocal and square root (PTX rcp.approx.f32 and
-// sqrt.approx.f32: one special-function instruction each, about one ulp from the
-// rounded results) for FP32 states whose own rounding already exceeds that.
-__device__ __forceinline__ float rcp_approx(float a) {
-  float r;
-  asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
-  return r;
-}
-__device__ __forceinline__ float sqrt_approx(float a) {
-  float r;
-  asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(a));
-  return r;
-}
+// The hardware's approximate reciprocal and square root (hyp_ff.cuh; about one ulp
+// from the rounded results) for FP32 states whose own rounding already exceeds that.
 __device__ __forceinline__ float2 f2rcp_approx(float2 a) { return make_float2(rcp_approx(a.x), rcp_approx(a.y)); }
 __device__ __forceinline__ float2 f2sqrt_approx(float2 a) { return make_float2(sqrt_approx(a.x), sqrt_approx(a.y)); }
 __device__ __forceinline__ float2 f2max(float2 a, float2 b) { return make_float2(fmaxf(a.x, b.x), fmaxf(a.y, b.y)); }
@@ -80,17 +70,17 @@ __device__ __forceinline__ ff2 ff2_mul_f(ff2 a, float2 b) {
   return fast_two_sum2(p.hi, f2fma(a.lo, b, p.lo));
 }
 __device__ __forceinline__ ff2 ff2_div(ff2 a, ff2 b) {
-  const float2 rb = f2rcp(b.hi);
+  const float2 rb = f2rcp_approx(b.hi);
   const float2 q1 = f2mul(a.hi, rb);
   const ff2 r = ff2_sub(a, ff2_mul(b, ff2{q1, f2s(0.0f)}));
   return fast_two_sum2(q1, f2mul(r.hi, rb));
 }
 __device__ __forceinline__ ff2 ff2_recip(ff2 b) { return ff2_div(ff2{f2s(1.0f), f2s(0.0f)}, b); }
 __device__ __forceinline__ ff2 ff2_sqrt(ff2 a) {
-  const float2 s = make_float2(__fsqrt_rn(a.hi.x), __fsqrt_rn(a.hi.y));
+  const float2 s = f2sqrt_approx(a.hi);
   const ff2 p = two_prod2(s, s);
   const float2 r = f2add(f2sub(f2sub(a.hi, p.hi), p.lo), a.lo);
-  const float2 c = f2mul(r, f2mul(f2s(0.5f), f2rcp(s)));
+  const float2 c = f2mul(r, f2mul(f2s(0.5f), f2rcp_approx(s)));
   return fast_two_sum2(s, c);
 }
 __device__ __forceinline__ ff2 ff2_diff_prod(float2 a, float2 b, float2 c, float2 d) {

@@ -91,7 +91,7 @@ __device__ __forceinline__ int prim_from_islands(const EosMixed& em, const float
   for (int c = 0; c < 3; ++c) P.u[c] = qh[1 + c] * ir;
   P.E = qh[4] * ir;
   for (int c = 0; c < 9; ++c) P.A[c] = qh[5 + c] * ir;
-  P.k = kinematics_s<float>(P.A, sf, __frcp_rn(sf));
+  P.k = kinematics_s<float>(P.A, sf, rcp_approx(sf));
   P.w = powers<float>(e, P.k);
   P.w.Pam1 = e.default_exp ? sm1 : expm1f(e.alpha * log1pf(sm1));
   P.xm1 = entropy_xm1<float>(e, P.e_int, P.k, P.w);
@@ -127,7 +127,7 @@ __device__ __forceinline__ void flux_mixed(const EosMixed& em, const float* qh, 
 // acos on [-1, 1] to ~7e-5 (Abramowitz & Stegun 4.4.45): enough for a Newton seed.
 __device__ __forceinline__ float acos_seed(float x) {
   const float ax = fabsf(x);
-  const float r = sqrtf(1.0f - ax) * (1.5707288f + ax * (-0.2121144f + ax * (0.0742610f - 0.0187293f * ax)));
+  const float r = sqrt_approx(1.0f - ax) * (1.5707288f + ax * (-0.2121144f + ax * (0.0742610f - 0.0187293f * ax)));
   return x >= 0.0f ? r : 3.14159265f - r;
 }
 __device__ __forceinline__ float cbrt_seed(float x) {
@@ -149,7 +149,7 @@ __device__ __forceinline__ float spectral_radius_fast(const float* a) {
   const float disc = 0.25f * q * q + p * p * p * (1.0f / 27.0f);
   float seed, other;  // seed: root of largest modulus; other: largest modulus of the rest
   if (disc < 0.0f && p < 0.0f) {
-    const float m = 2.0f * sqrtf(-p * (1.0f / 3.0f));
+    const float m = 2.0f * sqrt_approx(-p * (1.0f / 3.0f));
     const float cc = fminf(1.0f, fmaxf(-1.0f, __fdividef(3.0f * q, p * m)));
     const float th = acos_seed(cc) * (1.0f / 3.0f);
     const float y0 = m * __cosf(th) + t, y1 = m * __cosf(th - 2.0943951f) + t, y2 = m * __cosf(th - 4.1887902f) + t;
@@ -158,9 +158,9 @@ __device__ __forceinline__ float spectral_radius_fast(const float* a) {
     else if (a1 >= a2) { seed = y1; other = fmaxf(a0, a2); }
     else { seed = y2; other = fmaxf(a0, a1); }
   } else {
-    const float sd = sqrtf(fmaxf(disc, 0.0f));
+    const float sd = sqrt_approx(fmaxf(disc, 0.0f));
     seed = cbrt_seed(-0.5f * q + sd) + cbrt_seed(-0.5f * q - sd) + t;
-    other = seed != 0.0f ? sqrtf(fabsf(__fdividef(c0, seed))) : fabsf(c2);  // |complex pair| = sqrt(c0 / r)
+    other = seed != 0.0f ? sqrt_approx(fabsf(__fdividef(c0, seed))) : fabsf(c2);  // |complex pair| = sqrt(c0 / r)
   }
   float r = seed;
   for (int it = 0; it < 2; ++it) {
@@ -173,7 +173,7 @@ __device__ __forceinline__ float spectral_radius_fast(const float* a) {
     float s, qq;
     if (r != 0.0f) { s = c2 - r; qq = c0 / r; } else { s = c2; qq = c1; }
     const float dsc = s * s - 4.0f * qq;
-    const float m2 = dsc < 0.0f ? sqrtf(fabsf(qq)) : 0.5f * (fabsf(s) + sqrtf(dsc));
+    const float m2 = dsc < 0.0f ? sqrt_approx(fabsf(qq)) : 0.5f * (fabsf(s) + sqrt_approx(dsc));
     rad = fmaxf(rad, m2);
   }
   return rad;
@@ -185,7 +185,7 @@ __device__ __forceinline__ float lambda_mixed(const EosMixed& em, const PrimM& P
   stress_row0<float>(P.rho_s, P.k, c, s0);
   for (int i = 0; i < 3; ++i) s0r[i] = s0[i] * P.inv_rho_s;
   acoustic_omega<float>(em.f, P.k, P.w, c, P.xm1, s0r, om);
-  return fabsf(P.u[0]) + sqrtf(spectral_radius_fast(om));
+  return fabsf(P.u[0]) + sqrt_approx(spectral_radius_fast(om));
 }
 
 }  // namespace hyp
