@@ -155,9 +155,9 @@ int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel
    single-phase, FP64, Rusanov or LxF, with cfg->n_cells == n_cells. The step's
    scratch is one fixed static device array sized for at most 65,536 cells
    (13,631,552 bytes = 13.0 MiB per GPU that loads the library, held until exit);
-   larger n_cells is rejected with HYP_ERR_INVALID. The first call on a device
-   looks up that array (cudaGetSymbolAddress) and should come before any stream
-   capture. Calls share the array, so calls that overlap on the GPU race. Runs
+   larger n_cells is rejected with HYP_ERR_INVALID. The call synchronises `stream`
+   (it reads the step's status back), so it cannot be made inside a stream capture
+   or a CUDA graph. Calls share the array, so calls that overlap on the GPU race. Runs
    n_steps CFL steps from time t0 on `stream` (a cudaStream_t, NULL = the legacy
    default stream: pass the stream that produced d_Q_in, or synchronise first),
    waits for that stream to finish, and reports the new time; on HYP_ERR_NEG_DET /
