@@ -450,8 +450,7 @@ def run_batch(args):
                                    f"[256, 65536] (total {total}), per-problem CFL dt, {K} steps in one CUDA graph",
                        "l2": "inputs larger than L2"},
             "precision": PRECISION_NOTE["mixed"], "clocks": clocks,
-            "autotune": {"chosen_variant": chosen, "variants": ["128x8 persistent", "256x4 persistent", "256x3 persistent", "512x2 persistent",
-                                      "128x8 block per tile", "256x4 block per tile"],
+            "autotune": {"chosen_variant": chosen, "variants": ["256x4 persistent", "256x3 persistent", "256x4 block per tile"],
                          "ms_per_step": [float(x) for x in tune_ms]},
             "roofline": {"bound": "hbm", "achieved": BYTES_PER_CELL_UPDATE["single"] * total / (ms / K / 1e3) / 1e9,
                          "peak": peak, "unit": "GB/s", "peak_source": peak_kind,

@@ -24,7 +24,7 @@ HYP_FLUX_RUSANOV, HYP_FLUX_LXF, HYP_FLUX_HLL = 0, 1, 2
 HYP_BC_FROZEN, HYP_BC_TRANSMISSIVE = 0, 1
 HYP_PREC_FP64, HYP_PREC_MIXED = 0, 1
 HYP_RELAX_NONE, HYP_RELAX_PRESSURE, HYP_RELAX_MECHANICAL = 0, 1, 2
-HYP_BATCH_NUM_VARIANTS = 6
+HYP_BATCH_NUM_VARIANTS = 3
 
 
 class HypError(RuntimeError):

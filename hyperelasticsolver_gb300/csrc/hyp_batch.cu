@@ -9,9 +9,14 @@
 // persistent (grid = SMs x resident blocks, a loop over tiles), one launch per
 // step, and a whole run of steps is captured as one CUDA graph.
 //
-// Mixed precision: the tile body of hyp_mixed_tile.cuh, templated on the block
-// size; the autotuner times each (block, blocks-per-SM) variant on the batch
-// itself and keeps the fastest. FP64: per-cell flux / wave speed then update.
+// Mixed precision: the tile body of hyp_mixed_tile.cuh on a tile-major state block
+// (hyp_internal.cuh): every problem is cut into tiles of kTileCells cells, and tile
+// t of the tile table (problems in order) owns span t of the block, so that a
+// problem's tiles are consecutive spans and a tile's halo cells are the edge cells
+// of its neighbouring spans (at a problem's ends the clamped ghost is in the tile
+// itself). The autotuner times the grid variants (persistent at 4 or 3 resident
+// blocks per SM, or one block per tile) on the batch itself and keeps the fastest.
+// FP64: per-cell flux / wave speed then update, on row-major [var][cell] states.
 #include <algorithm>
 #include <cmath>
 #include <cstring>
@@ -80,36 +85,69 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   for (int tix = blockIdx.x; tix < ntiles; tix += gridDim.x) {
     const TileDesc d = tiles[tix];
     const TileCtl k = ctl[tix];
-    const MixedGlobalLoader<BLOCK> ld{a};
+    const TileOrigin org{(int64_t)tix * kTileFloats, d.first};
+    const MixedGlobalLoader<BLOCK, true> ld{a, org};
     MixedCellIn c;
     mixed_tile_load<BLOCK>(d.first, d.lo, d.hi, ld, c);
     if (!k.active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
       const int j = tile_local<BLOCK>();
       const int64_t i = d.first - 1 + j;
       if (j > 0 && j < BLOCK - 1 && i < d.hi)
-        mixed_store_cell(a.out + i, a.rstride, c.qh, c.ql, c.li, c.I0);
+        mixed_store_cell(a.out + org.base + (j - 1), kTileRow, c.qh, c.ql, c.li, c.I0);
       continue;
     }
     // faces from shared memory: the batch variants at 64 registers spill more otherwise
-    const float l = mixed_tile_run<BLOCK, false>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
+    const float l = mixed_tile_run<BLOCK, false, true>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
     const float m = mixed_block_max<BLOCK>(l);
     if (threadIdx.x == 0) atomicMax(&slots_wr[d.problem], (unsigned long long)__float_as_uint(m));
     __syncthreads();  // the block-max scratch is reused by the next tile
   }
 }
 
-// lambda and islands of every cell of an uploaded batch; max per problem into slot 0
-__global__ void __launch_bounds__(kBlock) batch_mixed_lam_kernel(MixedArrays a, EosMixed em,
-                                                                 const TileDesc* __restrict__ tiles, int ntiles,
-                                                                 int tile_cells, BatchDev b, DevState* S) {
+// An uploaded batch installed in one pass, one block per tile: thread j reads cell
+// first + j's 14 FP64 values from the staged [14][total] array, splits them into
+// (hi, lo) pairs into slot j of the tile's span, and computes the cell's wave speed
+// and island outputs there (mixed_cell_lambda_of); the problem's max lambda into its
+// slot 0.
+__global__ void __launch_bounds__(kBlock) batch_install_kernel(const double* __restrict__ q, int64_t total,
+                                                               float* __restrict__ out, EosMixed em,
+                                                               const TileDesc* __restrict__ tiles, int ntiles,
+                                                               BatchDev b, DevState* S) {
   for (int tix = blockIdx.x; tix < ntiles; tix += gridDim.x) {
     const TileDesc d = tiles[tix];
-    float m = 0.0f;
-    for (int64_t i = d.first + threadIdx.x; i < d.first + tile_cells && i < d.hi; i += kBlock)
-      m = fmaxf(m, mixed_cell_lambda<false>(a, em, i, S));
-    m = mixed_block_max<kBlock>(m);
-    if (threadIdx.x == 0) atomicMax(&b.slots[d.problem], (unsigned long long)__float_as_uint(m));
+    const int64_t i = d.first + threadIdx.x;
+    float l = 0.0f;
+    if (threadIdx.x < kTileCells && i < d.hi) {
+      float qh[14], ql[14];
+      float* o = out + (int64_t)tix * kTileFloats + threadIdx.x;
+#pragma unroll
+      for (int v = 0; v < 14; ++v) {
+        const double x = q[v * total + i];
+        qh[v] = (float)x;
+        ql[v] = (float)(x - (double)qh[v]);
+        o[v * kTileRow] = qh[v];
+        o[(kRowLo + v) * kTileRow] = ql[v];
+      }
+      l = mixed_cell_lambda_of(em, qh, ql, i, S, o, kTileRow);
+    }
+    l = mixed_block_max<kBlock>(l);
+    if (threadIdx.x == 0) atomicMax(&b.slots[d.problem], (unsigned long long)__float_as_uint(l));
     __syncthreads();
+  }
+}
+
+// The batch's FP64 state [14][total] from a tile-major block, one block per tile.
+__global__ void __launch_bounds__(kBlock) batch_join_kernel(const float* __restrict__ in, int64_t total,
+                                                            double* __restrict__ q, const TileDesc* __restrict__ tiles,
+                                                            int ntiles) {
+  for (int tix = blockIdx.x; tix < ntiles; tix += gridDim.x) {
+    const TileDesc d = tiles[tix];
+    const int64_t i = d.first + threadIdx.x;
+    if (threadIdx.x < kTileCells && i < d.hi) {
+      const float* c = in + (int64_t)tix * kTileFloats + threadIdx.x;
+#pragma unroll
+      for (int v = 0; v < 14; ++v) q[v * total + i] = (double)c[v * kTileRow] + (double)c[(kRowLo + v) * kTileRow];
+    }
   }
 }
 
@@ -214,7 +252,7 @@ __global__ void __launch_bounds__(kBlock) batch_f64_update_kernel(const double* 
 struct Variant {
   int block, minb, persist;
 };
-constexpr Variant kVariants[] = {{128, 8, 1}, {256, 4, 1}, {256, 3, 1}, {512, 2, 1}, {128, 8, 0}, {256, 4, 0}};
+constexpr Variant kVariants[] = {{256, 4, 1}, {256, 3, 1}, {256, 4, 0}};
 constexpr int kNumVariants = HYP_BATCH_NUM_VARIANTS;
 static_assert(sizeof(kVariants) / sizeof(kVariants[0]) == kNumVariants, "variant table");
 
@@ -247,12 +285,10 @@ struct hyp_batch {
   cudaStream_t stream = nullptr;
   EosC eos;
   EosMixed eos_mixed;
-  // mixed state: one block [2][32][mpitch] floats (hyp_mixed_tile.cuh layout); a parity's
+  // mixed state: per parity one tile-major block of the tile table's spans; a parity's
   // block also stages FP64 uploads and downloads
   float* mixed_base = nullptr;
-  int64_t mpitch = 0;
   float* Qh[2] = {nullptr, nullptr};
-  float* Ql[2] = {nullptr, nullptr};
   // FP64 state
   double* Q[2] = {nullptr, nullptr};
   double* F = nullptr;
@@ -265,7 +301,7 @@ struct hyp_batch {
   TileCtl* ctl = nullptr;  // mixed: per-tile step control
   int ntiles = 0;
   int tile_cells = 0;
-  int variant = 1;
+  int variant = 2;
   int grid = 0;
   std::vector<int64_t> offsets;
   long long k = 0;  // steps taken by every problem since the upload (the batch steps in lockstep)
@@ -314,19 +350,13 @@ static int select_variant(hyp_batch* b, int v) {
     return rc;
   }
   if (v < 0 || v >= kNumVariants) return berr(b, HYP_ERR_INVALID, "no such kernel variant");
-  int res = 0;
-  switch (v) {
-    case 0: case 4: res = resident_blocks<128, 8>(); break;
-    case 1: case 5: res = resident_blocks<256, 4>(); break;
-    case 2: res = resident_blocks<256, 3>(); break;
-    default: res = resident_blocks<512, 2>(); break;
-  }
+  const int res = kVariants[v].minb == 4 ? resident_blocks<256, 4>() : resident_blocks<256, 3>();
   b->variant = v;
   if (b->graph) {
     cudaGraphExecDestroy(b->graph);
     b->graph = nullptr;
   }
-  const int rc = build_tiles(b, kVariants[v].block - 2);
+  const int rc = b->tiles ? HYP_OK : build_tiles(b, kTileCells);  // the block's spans follow this table
   b->grid = kVariants[v].persist ? b->sms * (res > 0 ? res : 1) : b->ntiles;
   return rc;
 }
@@ -335,7 +365,7 @@ static MixedArrays batch_arrays(hyp_batch* b, int p) {
   MixedArrays a;
   a.in = b->Qh[p];
   a.out = b->Qh[1 - p];
-  a.rstride = b->mpitch;
+  a.rstride = kTileRow;
   a.n = b->total;
   a.own_lo = 0;
   a.own_hi = b->total;
@@ -353,12 +383,10 @@ static int enqueue_batch_step(hyp_batch* b, long long k, double t_end) {
     unsigned long long* sw = b->b.slots + (size_t)wr * b->P;
     const int fl = b->cfg.flux, bc = b->cfg.bc;
     cudaError_t e;
-    switch (b->variant) {
-      case 0: case 4: e = launch_batch_mixed_t<128, 8>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
-      case 1: case 5: e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
-      case 2: e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
-      default: e = launch_batch_mixed_t<512, 2>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st); break;
-    }
+    if (kVariants[b->variant].minb == 4)
+      e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st);
+    else
+      e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st);
     BCK(e);
   } else {
     batch_f64_cell_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->Q[par], b->total, b->eos, b->F, b->lam, b->tiles,
@@ -428,12 +456,13 @@ extern "C" int hyp_batch_create(const hyp_config* cfg, const int64_t* offsets, i
   ck(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
   const size_t nq = (size_t)14 * b->total;
   if (b->mixed) {
-    b->mpitch = mixed_pitch(b->total);
-    ck(cudaMalloc(&b->mixed_base, (size_t)2 * kMixedRows * b->mpitch * sizeof(float)));
-    for (int p = 0; p < 2 && rc == HYP_OK; ++p) {
-      b->Qh[p] = b->mixed_base + (size_t)p * kMixedRows * b->mpitch;
-      b->Ql[p] = b->Qh[p] + (size_t)14 * b->mpitch;
-    }
+    // one span per tile of kTileCells cells of each problem (the tile table's order);
+    // 32,768 bytes per 254 cells also hold the 14 FP64 values per cell of a staged upload
+    int64_t nt = 0;
+    for (int p = 0; p < n_problems; ++p) nt += mixed_tiles(offsets[p + 1] - offsets[p]);
+    const size_t block = (size_t)nt * kTileFloats;
+    ck(cudaMalloc(&b->mixed_base, 2 * block * sizeof(float)));
+    for (int p = 0; p < 2 && rc == HYP_OK; ++p) b->Qh[p] = b->mixed_base + (size_t)p * block;
   } else {
     for (int p = 0; p < 2 && rc == HYP_OK; ++p) ck(cudaMalloc(&b->Q[p], nq * sizeof(double)));
   }
@@ -451,7 +480,7 @@ extern "C" int hyp_batch_create(const hyp_config* cfg, const int64_t* offsets, i
     std::vector<double> dx(n_problems);
     for (int p = 0; p < n_problems; ++p) dx[p] = cfg->x_length / (double)(offsets[p + 1] - offsets[p]);
     ck(cudaMemcpy(b->b.dx, dx.data(), dx.size() * sizeof(double), cudaMemcpyHostToDevice));
-    if (rc == HYP_OK) rc = select_variant(b, b->mixed ? 1 : 0);
+    if (rc == HYP_OK) rc = select_variant(b, b->mixed ? 2 : 0);
   }
   if (rc != HYP_OK) {
     free_batch(b);
@@ -493,10 +522,8 @@ extern "C" int hyp_batch_upload(hyp_batch* b, const double* Q, double t0) {
   if (b->mixed) {
     double* stage = (double*)b->Qh[1];
     BCK(cudaMemcpyAsync(stage, Q, bytes, cudaMemcpyHostToDevice, b->stream));
-    BCK(launch_split_n(b->stream, stage, b->Qh[0], b->Ql[0], 14, b->total, b->mpitch));
-    const MixedArrays a = batch_arrays(b, 0);  // lambda and islands into the uploaded block itself
-    batch_mixed_lam_kernel<<<b->sms * 8, kBlock, 0, b->stream>>>(a, b->eos_mixed, b->tiles, b->ntiles, b->tile_cells,
-                                                                  b->b, b->st);
+    batch_install_kernel<<<b->sms * 8, kBlock, 0, b->stream>>>(stage, b->total, b->Qh[0], b->eos_mixed, b->tiles,
+                                                                b->ntiles, b->b, b->st);
     BCK(cudaGetLastError());
   } else {
     BCK(cudaMemcpyAsync(b->Q[0], Q, bytes, cudaMemcpyHostToDevice, b->stream));
@@ -512,7 +539,8 @@ extern "C" int hyp_batch_download(hyp_batch* b, double* Q) {
   const size_t bytes = (size_t)14 * b->total * sizeof(double);
   if (b->mixed) {
     double* stage = (double*)b->Qh[1 - b->cur];
-    BCK(launch_join_n(b->stream, b->Qh[b->cur], b->Ql[b->cur], stage, 14, b->total, b->mpitch));
+    batch_join_kernel<<<b->sms * 8, kBlock, 0, b->stream>>>(b->Qh[b->cur], b->total, stage, b->tiles, b->ntiles);
+    BCK(cudaGetLastError());
     BCK(cudaMemcpyAsync(Q, stage, bytes, cudaMemcpyDeviceToHost, b->stream));
   } else {
     BCK(cudaMemcpyAsync(Q, b->Q[b->cur], bytes, cudaMemcpyDeviceToHost, b->stream));
@@ -598,7 +626,7 @@ extern "C" int hyp_batch_autotune(hyp_batch* b, int trial_steps, int* chosen, do
   const int p0 = b->cur;
   const long long k0 = b->k;
   // the parity block holds hi, lo, lambda and islands
-  const size_t bq = (size_t)kMixedRows * b->mpitch * sizeof(float), bt = (size_t)2 * b->P * sizeof(double),
+  const size_t bq = (size_t)b->ntiles * kTileFloats * sizeof(float), bt = (size_t)2 * b->P * sizeof(double),
                bs = (size_t)3 * b->P * sizeof(unsigned long long), bk = (size_t)b->P * sizeof(long long);
   char* save = nullptr;
   BCK(cudaMalloc(&save, bq + bt + bs + bk));

@@ -31,6 +31,18 @@ struct MixedArrays {
   int64_t n;        // cells
   int64_t own_lo, own_hi;  // cells whose new wave speed enters the step's max (a slab's ghosts do not)
 };
+// A tile of a tile-major block: where its span starts and its first cell. Its halo
+// cells are the last cell of the span before and the first of the span after (a
+// problem's tiles are consecutive spans).
+struct TileOrigin {
+  int64_t base;   // offset of the tile's span in the block (a multiple of kTileFloats)
+  int64_t first;  // the tile's first cell
+};
+// Offset of cell ic (first - 1 <= ic <= first + kTileCells) relative to a tile.
+__device__ __forceinline__ int64_t tile_rel_off(const TileOrigin& o, int64_t ic) {
+  const int64_t rel = ic - o.first;
+  return o.base + (rel < 0 ? (int64_t)(kTileCells - 1) - kTileFloats : (rel >= kTileCells ? (int64_t)kTileFloats : rel));
+}
 // kTiled: tile-major blocks, whose row stride is known at compile time, so that a
 // cell's 32 rows are immediate offsets from one address; else row-major.
 template <bool kTiled>
@@ -60,13 +72,14 @@ __device__ __forceinline__ float2 pair_of(const float* v, int k) { return make_f
 template <int BLOCK, bool kTiled = false>
 struct MixedGlobalLoader {
   const MixedArrays& a;
+  TileOrigin o;  // tile-major: the tile being stepped
   __device__ __forceinline__ static float2 (&sQ())[7][BLOCK] {
     __shared__ float2 q[7][BLOCK];
     return q;
   }
   __device__ __forceinline__ void operator()(int, int64_t ic, MixedCellIn& c) const {
     const int64_t r = rows_apart<kTiled>(a);
-    const float* q = a.in + cell_at<kTiled>(ic);
+    const float* q = a.in + (kTiled ? tile_rel_off(o, ic) : ic);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
       c.qh[v] = q[v * r];
@@ -83,6 +96,7 @@ struct MixedGlobalLoader {
   }
   __device__ __forceinline__ float2 face_q2(int k, int j, int64_t) const { return sQ()[k][j]; }
   __device__ __forceinline__ void release() const {}
+  __device__ __forceinline__ const TileOrigin& origin() const { return o; }
 };
 
 // A cell's 11 flux components (flux_slot1 order) as 7 pairs of variables, zero
@@ -225,13 +239,17 @@ __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosM
       if (!(lnew <= 3.0e38f)) st |= HYP_CELL_NONFINITE;
       if (st) mixed_record_err(S, st, i);
     }
-    mixed_store_cell(a.out + cell_at<kTiled>(i), rows_apart<kTiled>(a), c.qh, c.ql, lnew, I);
-  } else if (kTiled && BLOCK == kTileCells + 2 && (j == 0 || j == BLOCK - 1)) {
-    // the halo threads fill the two unused floats of each row of the output tile, so
-    // that the last warp writes whole 128-byte lines (no partial sectors for L2 to merge)
-    float* q = a.out + tile_cell_off(first) + (j == 0 ? kTileRow - 1 : kTileRow - 2);
+    int64_t off = i;
+    if constexpr (kTiled) off = load.origin().base + (i - first);  // an owned cell: in the tile's span
+    mixed_store_cell(a.out + off, rows_apart<kTiled>(a), c.qh, c.ql, lnew, I);
+  } else if constexpr (kTiled && BLOCK == kTileCells + 2) {
+    if (j == 0 || j == BLOCK - 1) {
+      // the halo threads fill the two unused floats of each row of the output tile, so
+      // that the last warp writes whole 128-byte lines (no partial sectors for L2 to merge)
+      float* q = a.out + load.origin().base + (j == 0 ? kTileRow - 1 : kTileRow - 2);
 #pragma unroll
-    for (int r = 0; r < kMixedRows; ++r) q[r * kTileRow] = 0.0f;
+      for (int r = 0; r < kMixedRows; ++r) q[r * kTileRow] = 0.0f;
+    }
   }
   __syncthreads();  // the shared arrays are reused by the block's next tile
   return lnew;

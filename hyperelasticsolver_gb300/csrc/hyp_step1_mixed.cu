@@ -69,7 +69,7 @@ __global__ void __launch_bounds__(kBlock, 4)
     step1_mixed_kernel(MixedArrays a, EosMixed em, MixedSlots sl, DevState* S, double t_end, double cfl, double dx,
                        int flux, int bc) {
   const int64_t first = (int64_t)blockIdx.x * kTileM;
-  const MixedGlobalLoader<kBlock, true> ld{a};
+  const MixedGlobalLoader<kBlock, true> ld{a, {(int64_t)blockIdx.x * kTileFloats, first}};
   MixedCellIn c;
   mixed_tile_load<kBlock>(first, 0, a.n, ld, c);  // issued before the control reads below
   float dtdx;
@@ -235,8 +235,8 @@ __global__ void __launch_bounds__(BLOCK, 4)
 constexpr unsigned kTmaTileBytes = kTileFloats * 4u;  // 32 KB, a multiple of 16
 constexpr unsigned kTmaSmem = kTmaTileBytes + 128u;   // dynamic shared memory (alignment slack)
 
-// Loads a cell's inputs from the staged tile (its owned cells; `first` its first
-// cell) or, for a halo cell in a neighbouring tile, from global memory; the halo
+// Loads a cell's inputs from the staged tile (its owned cells; o its origin) or,
+// for a halo cell in a neighbouring tile, from global memory; the halo
 // cells' hi parts are kept in shared memory for the face phase. The next tile is
 // copied in (release) once the faces have read the stage.
 template <int BLOCK>
@@ -244,12 +244,13 @@ struct MixedStageLoader {
   const float* stage;   // [32][kTileRow]
   const MixedArrays& a;
   float2 (*halo)[7];    // [2][7]: the left / right halo cell's hi parts
-  int64_t first;
+  TileOrigin o;
   uint64_t* bar;
   const float* next;    // the next tile's span in global memory (null: none)
-  __device__ __forceinline__ bool staged(int64_t ic) const { return ic >= first && ic < first + kTileCells; }
+  __device__ __forceinline__ bool staged(int64_t ic) const { return ic >= o.first && ic < o.first + kTileCells; }
+  __device__ __forceinline__ const TileOrigin& origin() const { return o; }
   __device__ __forceinline__ void operator()(int, int64_t ic, MixedCellIn& c) const {
-    const float* q = staged(ic) ? stage + (ic - first) : a.in + tile_cell_off(ic);
+    const float* q = staged(ic) ? stage + (ic - o.first) : a.in + tile_rel_off(o, ic);
 #pragma unroll
     for (int v = 0; v < 14; ++v) {
       c.qh[v] = q[v * kTileRow];
@@ -261,14 +262,14 @@ struct MixedStageLoader {
     c.I0.sm1 = q[(kRowIsl + 2) * kTileRow];
   }
   __device__ __forceinline__ void keep(int j, const MixedCellIn& c) const {
-    const int64_t i = first - 1 + j;
+    const int64_t i = o.first - 1 + j;
     if ((j == 0 || j == BLOCK - 1) && !staged(i < 0 ? 0 : (i >= a.n ? a.n - 1 : i)))
 #pragma unroll
       for (int k = 0; k < 7; ++k) halo[j == 0 ? 0 : 1][k] = pair_of(c.qh, k);
   }
   __device__ __forceinline__ float2 face_q2(int k, int j, int64_t ic) const {
     if (!staged(ic)) return halo[j == 0 ? 0 : 1][k];
-    const float* s = stage + (ic - first);
+    const float* s = stage + (ic - o.first);
     return make_float2(s[2 * k * kTileRow], s[(2 * k + 1) * kTileRow]);
   }
   // called after a barrier that follows the block's last read of the stage
@@ -316,7 +317,7 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     phase ^= 1u;
     const int64_t first = (int64_t)tile * kTileCells;
     const int next = tile + gridDim.x;
-    MixedStageLoader<BLOCK> ld{stage, a, halo, first, &bar,
+    MixedStageLoader<BLOCK> ld{stage, a, halo, {(int64_t)tile * kTileFloats, first}, &bar,
                                next < ntiles ? a.in + (int64_t)next * kTileFloats : nullptr};
     m = fmaxf(m, mixed_tile<BLOCK, true>(a, em, first, 0, a.n, dtdx, flux, bc, S, ld));
   }

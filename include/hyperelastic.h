@@ -241,11 +241,10 @@ int hyp_batch_status(hyp_batch* b, double* t, int64_t* steps);
 int hyp_batch_last_ms(const hyp_batch* b, double* ms);
 /* Mixed precision: time each tile-kernel variant for trial_steps steps on the
    batch's own state (restored afterwards) and keep the fastest; ms_per_step
-   receives HYP_BATCH_NUM_VARIANTS timings. Variants 0-3: a persistent grid (one
-   wave striding over the tiles) of 128/256/256/512-thread blocks at 8/4/3/2
-   resident blocks per SM; 4, 5: one block per tile, 128 threads at 8 per SM and
-   256 at 4. */
-#define HYP_BATCH_NUM_VARIANTS 6
+   receives HYP_BATCH_NUM_VARIANTS timings. Every variant steps 254-cell tiles with
+   256-thread blocks: 0, 1: a persistent grid (one wave striding over the tiles) at
+   4 / 3 resident blocks per SM; 2 (the default): one block per tile. */
+#define HYP_BATCH_NUM_VARIANTS 3
 int hyp_batch_autotune(hyp_batch* b, int trial_steps, int* chosen, double* ms_per_step);
 int hyp_batch_set_variant(hyp_batch* b, int variant);
 
