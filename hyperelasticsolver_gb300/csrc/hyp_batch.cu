@@ -77,6 +77,30 @@ __global__ void batch_mixed_ctl_kernel(const TileDesc* __restrict__ tiles, int n
   }
 }
 
+// One tile of the batch: its problem's step (or, for a finished problem, its cells
+// carried to the other buffer), the block max of the new wave speeds into the
+// problem's slot.
+template <int BLOCK, bool kOwnRegs>
+__device__ __forceinline__ void batch_tile(const MixedArrays& a, const EosMixed& em, const TileDesc& d,
+                                           const TileCtl& k, int tix, unsigned long long* slots_wr, int flux, int bc,
+                                           DevState* S) {
+  const TileOrigin org{(int64_t)tix * kTileFloats, d.first};
+  const MixedGlobalLoader<BLOCK, true> ld{a, org};
+  MixedCellIn c;
+  mixed_tile_load<BLOCK>(d.first, d.lo, d.hi, ld, c);
+  if (!k.active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
+    const int j = tile_local<BLOCK>();
+    const int64_t i = d.first - 1 + j;
+    if (j > 0 && j < BLOCK - 1 && i < d.hi) mixed_store_cell(a.out + org.base + (j - 1), kTileRow, c.qh, c.ql, c.li, c.I0);
+    return;
+  }
+  const float l = mixed_tile_run<BLOCK, kOwnRegs, true>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
+  const float m = mixed_block_max<BLOCK>(l);
+  if (threadIdx.x == 0) atomicMax(&slots_wr[d.problem], (unsigned long long)__float_as_uint(m));
+}
+
+// Persistent grid: each block strides over the tile table. Faces from shared memory:
+// at 64 registers the loop's state leaves no room for the own-register faces.
 template <int BLOCK, int MINB>
 __global__ void __launch_bounds__(BLOCK, MINB)
     batch_mixed_kernel(MixedArrays a, EosMixed em, const TileDesc* __restrict__ tiles,
@@ -85,23 +109,20 @@ __global__ void __launch_bounds__(BLOCK, MINB)
   for (int tix = blockIdx.x; tix < ntiles; tix += gridDim.x) {
     const TileDesc d = tiles[tix];
     const TileCtl k = ctl[tix];
-    const TileOrigin org{(int64_t)tix * kTileFloats, d.first};
-    const MixedGlobalLoader<BLOCK, true> ld{a, org};
-    MixedCellIn c;
-    mixed_tile_load<BLOCK>(d.first, d.lo, d.hi, ld, c);
-    if (!k.active) {  // uniform over the block: carry the problem's cells to the other buffer unchanged
-      const int j = tile_local<BLOCK>();
-      const int64_t i = d.first - 1 + j;
-      if (j > 0 && j < BLOCK - 1 && i < d.hi)
-        mixed_store_cell(a.out + org.base + (j - 1), kTileRow, c.qh, c.ql, c.li, c.I0);
-      continue;
-    }
-    // faces from shared memory: the batch variants at 64 registers spill more otherwise
-    const float l = mixed_tile_run<BLOCK, false, true>(a, em, d.first, d.lo, d.hi, k.dtdx, flux, bc, S, ld, c);
-    const float m = mixed_block_max<BLOCK>(l);
-    if (threadIdx.x == 0) atomicMax(&slots_wr[d.problem], (unsigned long long)__float_as_uint(m));
-    __syncthreads();  // the block-max scratch is reused by the next tile
+    batch_tile<BLOCK, false>(a, em, d, k, tix, slots_wr, flux, bc, S);
+    __syncthreads();  // the shared scratch is reused by the next tile
   }
+}
+
+// One block per tile.
+template <int BLOCK, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
+    batch_tile_kernel(MixedArrays a, EosMixed em, const TileDesc* __restrict__ tiles, const TileCtl* __restrict__ ctl,
+                      unsigned long long* __restrict__ slots_wr, int flux, int bc, DevState* S) {
+  const int tix = blockIdx.x;
+  const TileDesc d = tiles[tix];
+  const TileCtl k = ctl[tix];
+  batch_tile<BLOCK, true>(a, em, d, k, tix, slots_wr, flux, bc, S);
 }
 
 // An uploaded batch installed in one pass, one block per tile: thread j reads cell
@@ -257,10 +278,13 @@ constexpr int kNumVariants = HYP_BATCH_NUM_VARIANTS;
 static_assert(sizeof(kVariants) / sizeof(kVariants[0]) == kNumVariants, "variant table");
 
 template <int BLOCK, int MINB>
-cudaError_t launch_batch_mixed_t(cudaStream_t s, int grid, const MixedArrays& a, const EosMixed& em,
+cudaError_t launch_batch_mixed_t(cudaStream_t s, int grid, bool persist, const MixedArrays& a, const EosMixed& em,
                                  const TileDesc* tiles, const TileCtl* ctl, int ntiles, unsigned long long* slots_wr,
                                  int flux, int bc, DevState* S) {
-  batch_mixed_kernel<BLOCK, MINB><<<grid, BLOCK, 0, s>>>(a, em, tiles, ctl, ntiles, slots_wr, flux, bc, S);
+  if (persist)
+    batch_mixed_kernel<BLOCK, MINB><<<grid, BLOCK, 0, s>>>(a, em, tiles, ctl, ntiles, slots_wr, flux, bc, S);
+  else
+    batch_tile_kernel<BLOCK, MINB><<<ntiles, BLOCK, 0, s>>>(a, em, tiles, ctl, slots_wr, flux, bc, S);
   return cudaGetLastError();
 }
 
@@ -383,10 +407,13 @@ static int enqueue_batch_step(hyp_batch* b, long long k, double t_end) {
     unsigned long long* sw = b->b.slots + (size_t)wr * b->P;
     const int fl = b->cfg.flux, bc = b->cfg.bc;
     cudaError_t e;
+    const bool persist = kVariants[b->variant].persist != 0;
     if (kVariants[b->variant].minb == 4)
-      e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st);
+      e = launch_batch_mixed_t<256, 4>(b->stream, b->grid, persist, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw,
+                                       fl, bc, b->st);
     else
-      e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw, fl, bc, b->st);
+      e = launch_batch_mixed_t<256, 3>(b->stream, b->grid, persist, a, b->eos_mixed, b->tiles, b->ctl, b->ntiles, sw,
+                                       fl, bc, b->st);
     BCK(e);
   } else {
     batch_f64_cell_kernel<<<b->grid, kBlock, 0, b->stream>>>(b->Q[par], b->total, b->eos, b->F, b->lam, b->tiles,
