@@ -14,6 +14,7 @@
 // through the templates of hyp_physics.cuh.
 #pragma once
 #include "hyp_ff.cuh"
+#include "hyp_pair.cuh"
 #include "hyp_physics.cuh"
 
 namespace hyp {
@@ -179,12 +180,65 @@ __device__ __forceinline__ float spectral_radius_fast(const float* a) {
   return rad;
 }
 
+// acoustic_omega<float> with columns 1 and 2 (the same formulas, dcGG = 0 and no
+// density or p term) as the two lanes of packed FP32 pairs; column 0 scalar.
+__device__ __forceinline__ void acoustic_omega_f32(const EosT<float>& e, const KinT<float>& k, const PowsT<float>& w,
+                                                   const StressCT<float>& c, float xm1, const float* s0r, float* om) {
+  const SymT<float>& G = k.G;
+  const SymT<float>& H = k.H;
+  const float G0[3] = {G.a00, G.a01, G.a02}, H0[3] = {H.a00, H.a01, H.a02};
+  float o0[3];
+  {  // column 0 (acoustic_omega's j = 0 statements)
+    const float di1 = -2.0f * G.a00;
+    const float dpsi = (2.0f / 3.0f) * k.i1 * G.a00 - 2.0f * H.a00;
+    const float dp = -2.0f * k.p;
+    const float dPb = 0.5f * e.beta * w.Pb1 * dp;
+    const float dPa = 0.5f * e.alpha * w.Pa1 * dp;
+    const float dPa1 = (0.5f * e.alpha - 1.0f) * w.Pa2 * dp;
+    const float dPg1 = (0.5f * e.gamma - 1.0f) * w.Pg2 * dp;
+    const float dPb1 = (0.5f * e.beta - 1.0f) * w.Pb2 * dp;
+    const float dcG = -e.b0sq_6 * (dPb * k.i1 + w.Pb * di1);
+    const float dcGG = 0.5f * e.b0sq * dPb;
+    const float dE3 = e.kE3a * (dPa * w.Pa1 + w.Pam1 * dPa1) + e.kE3g * dPg1 * xm1 + e.kE3b * (dPb1 * k.psi + w.Pb1 * dpsi);
+    const float dcI = dE3 * k.p + c.E3 * dp;
+#pragma unroll
+    for (int i = 0; i < 3; ++i) {
+      const float dG0i = -((i == 0 ? G.a00 : 0.0f) + G0[i]);
+      const float dH0i = -(G.a00 * G0[i] + H0[i] + (i == 0 ? H.a00 : 0.0f) + G.a00 * G0[i]);
+      const float v = dcG * G0[i] + c.cG * dG0i + dcGG * H0[i] + c.cGG * dH0i + (i == 0 ? dcI : 0.0f);
+      o0[i] = -2.0f * v - s0r[i];
+    }
+  }
+  const float2 G0j = make_float2(G.a01, G.a02), H0j = make_float2(H.a01, H.a02);
+  const float2 di1 = f2mul(f2s(-2.0f), G0j);
+  const float2 dpsi = f2fma(f2s((2.0f / 3.0f) * k.i1), G0j, f2mul(f2s(-2.0f), H0j));
+  const float2 dcG = f2mul(f2s(-e.b0sq_6 * w.Pb), di1);
+  const float2 dcI = f2mul(f2mul(f2s(e.kE3b * w.Pb1), dpsi), f2s(k.p));
+  const float2 cG = f2s(c.cG), cGG = f2s(c.cGG);
+  // rows i of columns 1, 2: G(i,1), G(i,2) and H(i,1), H(i,2)
+  const float2 Gi[3] = {make_float2(G.a01, G.a02), make_float2(G.a11, G.a12), make_float2(G.a12, G.a22)};
+  const float2 Hi[3] = {make_float2(H.a01, H.a02), make_float2(H.a11, H.a12), make_float2(H.a12, H.a22)};
+#pragma unroll
+  for (int i = 0; i < 3; ++i) {
+    const float2 dG0i = f2neg(i == 0 ? f2add(G0j, Gi[i]) : Gi[i]);
+    float2 t = f2fma(G0j, f2s(G0[i]), Hi[i]);
+    if (i == 0) t = f2add(t, H0j);
+    const float2 dH0i = f2neg(f2fma(f2s(G.a00), Gi[i], t));
+    float2 v = f2fma(cGG, dH0i, f2fma(cG, dG0i, f2mul(dcG, f2s(G0[i]))));
+    if (i == 0) v = f2add(v, dcI);
+    const float2 o = f2mul(f2s(-2.0f), v);
+    om[i] = o0[i];
+    om[i + 3] = o.x;
+    om[i + 6] = o.y;
+  }
+}
+
 // max |u1 +- c_k| = |u1| + sqrt(spectral radius of the acoustic tensor)
 __device__ __forceinline__ float lambda_mixed(const EosMixed& em, const PrimM& P, const StressCT<float>& c) {
   float s0[3], s0r[3], om[9];
   stress_row0<float>(P.rho_s, P.k, c, s0);
   for (int i = 0; i < 3; ++i) s0r[i] = s0[i] * P.inv_rho_s;
-  acoustic_omega<float>(em.f, P.k, P.w, c, P.xm1, s0r, om);
+  acoustic_omega_f32(em.f, P.k, P.w, c, P.xm1, s0r, om);
   return fabsf(P.u[0]) + sqrt_approx(spectral_radius_fast(om));
 }
 
