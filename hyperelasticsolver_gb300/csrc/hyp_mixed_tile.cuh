@@ -4,7 +4,9 @@
 //
 // A block of BLOCK threads owns BLOCK - 2 consecutive cells of one problem and
 // loads them plus one halo cell on each side (clamped to the problem's cells
-// [lo, hi): a ghost cell copies the end cell, i.e. a zero-gradient boundary):
+// [lo, hi): a ghost cell copies the end cell, i.e. a zero-gradient boundary);
+// threads 0 .. BLOCK - 3 take the owned cells and the last two the halos
+// (tile_local), and the state blocks are row-major or tile-major (MixedArrays):
 //   1. flux of every loaded cell from its (hi, lo) state and the float-float
 //      island outputs cached by the step that produced it -> shared memory;
 //   2. Rusanov face fluxes 0.5 (f_L + f_R) - 0.5 lambda_face (Q_R - Q_L)
@@ -168,8 +170,9 @@ __device__ __forceinline__ void mixed_tile_load(int64_t first, int64_t lo, int64
   load(j, tile_cell(first, lo, hi, j), c);
 }
 // kOwnRegs: a face reads its left cell (this thread's) and an update its right face
-// (this thread's) from registers instead of shared memory -- 39 fewer shared loads
-// per cell, at 11 more registers live across a barrier (the same values either way).
+// (this thread's) from registers instead of shared memory -- 21 fewer shared loads
+// per cell (the 7 pairs of flux, state and face), at 11 more registers live across a
+// barrier (the same values either way).
 template <int BLOCK, bool kOwnRegs = true, bool kTiled = false, class Loader>
 __device__ __forceinline__ float mixed_tile_run(const MixedArrays& a, const EosMixed& em, int64_t first, int64_t lo,
                                                 int64_t hi, float dtdx, int flux, int bc, DevState* S,
