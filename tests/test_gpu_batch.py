@@ -29,10 +29,19 @@ def density(Q, rho0=8.93):
     return np.sqrt(det / rho0)
 
 
+# problems whose ends fall on, just before and just after the 254-cell tiles of the
+# mixed batch's tile-major state (a tile's halo cells are its neighbours' edge cells)
+TILE_EDGE_SIZES = [3, 253, 254, 255, 508, 509, 762, 763, 1017]
+
+
 @pytest.mark.parametrize("precision", ["fp64", "mixed"])
-def test_batch_matches_individual_runs(hyp, orc, precision):
+@pytest.mark.parametrize("sizes_kind", ["random", "tile_edges"])
+def test_batch_matches_individual_runs(hyp, orc, precision, sizes_kind):
     rng = np.random.default_rng(3)
-    sizes = np.floor(np.exp(rng.uniform(np.log(16), np.log(700), 20))).astype(np.int64)
+    if sizes_kind == "random":
+        sizes = np.floor(np.exp(rng.uniform(np.log(16), np.log(700), 20))).astype(np.int64)
+    else:
+        sizes = np.array(TILE_EDGE_SIZES, dtype=np.int64)
     Q0 = make_batch_state(orc, sizes)
     steps = 37
     with hyp.Batch(hyp.Barton2009(), sizes, precision=precision) as b:
