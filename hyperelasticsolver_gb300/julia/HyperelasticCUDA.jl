@@ -463,7 +463,7 @@ function last_ms(b::Batch)
   bcheck(ccall((:hyp_batch_last_ms, libhyp), Cint, (Ptr{Cvoid}, Ref{Float64}), b.h, ms), b, "hyp_batch_last_ms")
   ms[]
 end
-"set_variant!(b, v): the tile kernel variant (0-5, as autotune! numbers them)"
+"set_variant!(b, v): the tile kernel variant (0-2, as autotune! numbers them)"
 set_variant!(b::Batch, v::Integer) =
   bcheck(ccall((:hyp_batch_set_variant, libhyp), Cint, (Ptr{Cvoid}, Cint), b.h, v), b, "hyp_batch_set_variant")
 
