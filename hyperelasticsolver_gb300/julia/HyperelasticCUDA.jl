@@ -444,7 +444,7 @@ end
 step!(b::Batch, n_steps::Integer; T::Float64=Inf) =
   bcheck(ccall((:hyp_batch_step, libhyp), Cint, (Ptr{Cvoid}, Cint, Float64), b.h, n_steps, T), b, "hyp_batch_step")
 function autotune!(b::Batch; trial_steps::Integer=10)
-  chosen, ms = Ref{Cint}(-1), zeros(6)
+  chosen, ms = Ref{Cint}(-1), zeros(3)  # HYP_BATCH_NUM_VARIANTS
   bcheck(ccall((:hyp_batch_autotune, libhyp), Cint, (Ptr{Cvoid}, Cint, Ref{Cint}, Ptr{Float64}), b.h, trial_steps,
                chosen, ms), b, "hyp_batch_autotune")
   (chosen[], ms)
