@@ -566,7 +566,7 @@ HYP_HD double rsqrt_d(double x) {
 #ifdef __CUDA_ARCH__
   return rsqrt(x);
 #else
-  return 1.0 / std::sqrt(x);
+  return 1.0 / sqrt(x);
 #endif
 }
 
