@@ -36,6 +36,9 @@ import numpy as np  # noqa: E402
 
 METRIC = "cell-updates/s"
 BYTES_PER_CELL_UPDATE = {"single": 224, "multi": 480}  # state read + write per cell-update (14 or 30 values x 8 B x 2)
+# floating-point operations of the formulation per cell-update (tests/flop_count.cpp: the product's
+# FP64 physics run with an operation-counting scalar type; Rusanov single phase, HLL two-phase)
+FLOPS_PER_CELL_UPDATE = {"single": 674, "multi": 15087}
 
 
 def measured_peaks():
@@ -301,6 +304,8 @@ def run_ours(args):
         return 0
     rf = roofline(tm, prec, n, peak, peak_kind)
     rf["step_hbm_frac"] = (BYTES_PER_CELL_UPDATE["single"] * n / (ms_total / K / 1e3) / 1e9) / peak
+    rf["formulation_flops_per_cell_update"] = FLOPS_PER_CELL_UPDATE["single"]
+    rf["formulation_tflops"] = FLOPS_PER_CELL_UPDATE["single"] * n / (ms_total / K / 1e3) / 1e12
     line = {
         "metric": METRIC, "value": value, "unit": METRIC, "n_gpus": WORLD, "steps": K, "warmup": W,
         "ms_per_step": ms_total / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
@@ -518,6 +523,8 @@ def run_mph(args):
                                     "update": tm["ms_update"] / max(1, tm["n_update"])},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
                          "frac": ach / peak,
+                         "formulation_flops_per_cell_update": FLOPS_PER_CELL_UPDATE["multi"],
+                         "formulation_tflops": FLOPS_PER_CELL_UPDATE["multi"] * n / (ms / 1e3) / 1e12,
                          "note": "the face kernel (18 evaluations of B per face) is bound by FP32 issue, not HBM"},
             "fp64": {"value": n * K / (tm64["ms_total"] / 1e3), "ms_per_step": tm64["ms_total"] / K,
                      "kernels_ms_per_step": {"cell+face": tm64["ms_cell"] / max(1, tm64["n_cell"]),
