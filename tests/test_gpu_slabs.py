@@ -67,3 +67,24 @@ def test_slab_records_round_trip_and_refusals(hyp):
                 sl.get_cells(sl.n - 1, 2)  # beyond the slab
     with hyp.Solver((hyp.Barton2009(), hyp.Barton2009()), 64, model="multi", flux="hll") as s:
         assert hyp._lib.load().hyp_set_slab(s._h, 1.0 / 64, 1, 1) == hyp._lib.HYP_ERR_UNSUPPORTED
+
+
+@pytest.mark.parametrize("first,count", [(250, 10), (0, 300), (505, 260), (N - 7, 7)])
+def test_mixed_records_across_tiles(hyp, first, count):
+    """Mixed records of cells on both sides of the 254-cell tiles of the tile-major
+    state: one 2D copy per tile the range touches. The records' hi + lo rows are the
+    downloaded state's values; writing a range back at the same cells changes nothing,
+    and written at other cells it reads back unchanged."""
+    from hyperelasticsolver_gb300.domain import GpuSlab
+    eos, Q0 = _state(hyp)
+    with GpuSlab(eos, N, 1, 0, precision="mixed") as sl:
+        sl.upload(Q0)
+        rec = sl.get_cells(first, count)
+        assert rec.shape == (32, count) and rec.dtype == np.float32
+        Q = sl.solver.download()
+        assert np.array_equal(rec[:14].astype(np.float64) + rec[14:28].astype(np.float64), Q[:, first:first + count])
+        sl.set_cells(first, rec)
+        assert np.array_equal(sl.solver.download(), Q)
+        other = (first + 127) % (N - count)
+        sl.set_cells(other, rec)
+        assert np.array_equal(sl.get_cells(other, count), rec)
