@@ -173,3 +173,46 @@ def step_all(steppers):
     for r, s in enumerate(steppers):
         halo_in(s, outs[r - 1]["right"] if r > 0 else None, outs[r + 1]["left"] if r + 1 < len(steppers) else None)
     return ts
+
+
+# ---- a batch's problems over ranks --------------------------------------------------
+# The problems of a batch are independent (each its own dx, CFL dt and time:
+# main.jl:202-227 per problem), so ranks step disjoint sets of them as separate
+# batches with no exchange between steps; only the final states are gathered.
+
+def shard_problems(sizes, world):
+    """The problems of a batch (cell counts `sizes`) dealt to `world` ranks so that
+    their cell counts balance: largest problem first onto the rank with the fewest cells
+    so far (ties to the lower rank, then the lower problem index). Returns one array of
+    problem indices per rank, in batch order. No rank's cells exceed the mean by more
+    than the largest problem."""
+    import heapq
+    sizes = np.asarray(sizes, dtype=np.int64)
+    if world < 1 or len(sizes) < world or np.any(sizes < 1):
+        raise ValueError(f"cannot deal {len(sizes)} problems to {world} ranks")
+    order = sorted(range(len(sizes)), key=lambda p: (-int(sizes[p]), p))
+    heap = [(0, r) for r in range(world)]
+    shards = [[] for _ in range(world)]
+    for p in order:
+        load, r = heapq.heappop(heap)
+        shards[r].append(p)
+        heapq.heappush(heap, (load + int(sizes[p]), r))
+    return [np.array(sorted(s), dtype=np.int64) for s in shards]
+
+
+def shard_columns(sizes, problems):
+    """Columns of the listed problems in the batch's SoA state (problem p in columns
+    offsets[p]:offsets[p + 1]), in the order listed: a shard's own state."""
+    offsets = np.concatenate([[0], np.cumsum(np.asarray(sizes, dtype=np.int64))])
+    parts = [np.arange(offsets[p], offsets[p + 1]) for p in problems]
+    return np.concatenate(parts) if parts else np.zeros(0, dtype=np.int64)
+
+
+def gather_shards(sizes, shards, states):
+    """The batch's SoA state from the ranks' shard states (states[r] over the columns
+    shard_columns(sizes, shards[r]))."""
+    total = int(np.sum(sizes))
+    Q = np.empty((states[0].shape[0], total), dtype=states[0].dtype)
+    for problems, Qr in zip(shards, states):
+        Q[:, shard_columns(sizes, problems)] = Qr
+    return Q
