@@ -229,13 +229,13 @@ __device__ __forceinline__ int hll_face2_pair(const Eos2M& E, const EosPair& e, 
   const float2 s_r = f2s(sr), s_l = f2s(sl), id = f2s(idsr);
   for (int k = 0; k < 15; ++k) {
     Qh[k] = f2mul(f2sub(f2fma(QR[k], s_r, f2neg(f2mul(QL[k], s_l))), f2add(acc[k], dF[k])), id);
-    acc[k] = f2s(0.0f);
+    acc[k] = dF[k];  // the two integrals through Q_hll add onto f_R - f_L: dF is not live across them
   }
   st |= path_integral_add_pair<kDef>(e, qd, QL, Qh, acc);
   st |= path_integral_add_pair<kDef>(e, qd, Qh, QR, acc);
   const float2 cm = f2s((-sl) * idsr), cp = f2s(sr * idsr), cq = f2s((sl * sr) * idsr);
   for (int k = 0; k < 15; ++k) {
-    const float2 inner = f2add(dF[k], acc[k]);
+    const float2 inner = acc[k];
     const float2 jump = f2sub(QR[k], QL[k]);
     dm[k] = f2fma(cm, inner, f2mul(cq, jump));
     dp[k] = f2fma(cp, inner, f2neg(f2mul(cq, jump)));

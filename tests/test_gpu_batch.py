@@ -150,3 +150,27 @@ def test_batch_t_end_stops_each_problem(hyp, orc):
             assert k == sb[p] and abs(t - tb[p]) <= MIXED_AGREE * t and tb[p] >= t_end
             assert_close_soa(Qb[:, o:o + n], s.download(), MIXED_AGREE, f"problem {p}")
         o += n
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_batch_shards_equal_the_whole_batch(hyp, orc, precision):
+    """A batch dealt into three shards (domain.shard_problems), each stepped as its own
+    batch (as three GPUs would), gathers back to the whole batch's result bit for bit:
+    the same kernel on the same problem's cells, whatever else shares the batch."""
+    from hyperelasticsolver_gb300.domain import gather_shards, shard_columns, shard_problems
+    sizes = np.array(TILE_EDGE_SIZES + [40, 17, 600, 1300], dtype=np.int64)
+    Q0 = make_batch_state(orc, sizes, seed=13)
+    with hyp.Batch(hyp.Barton2009(), sizes, precision=precision) as b:
+        b.upload(Q0)
+        b.step(31)
+        Qb = b.download()
+        tb, _ = b.status()
+    shards = shard_problems(sizes, 3)
+    parts = []
+    for problems in shards:
+        with hyp.Batch(hyp.Barton2009(), sizes[problems], precision=precision) as b:
+            b.upload(np.ascontiguousarray(Q0[:, shard_columns(sizes, problems)]))
+            b.step(31)
+            parts.append(b.download())
+            assert np.array_equal(b.status()[0], tb[problems])
+    assert np.array_equal(gather_shards(sizes, shards, parts), Qb)
