@@ -164,6 +164,80 @@ __global__ void __launch_bounds__(kFaceBlockM) face2_hll_pair_kernel(
   store_face_pairs(DP, nf, f, dp);
 }
 
+// The HLL pair face kernel with the update fused in. Block b computes faces
+// 63 b .. 63 b + 63 (one per thread; the last is computed again by block b + 1 as its
+// first) and updates cells 63 b .. 63 b + 62: cell i from the D+ of its left face i
+// (this thread's) and the D- of its right face i + 1 (the next thread's, through shared
+// memory), with update2_mixed_kernel's dt/dx, FP32 expression and two-sum. D+- never
+// go to memory; the face work is bound by FP32 issue, and the update's loads and
+// stores of the (hi, lo) state run under it instead of in a kernel of their own.
+constexpr int kFusedCells = kFaceBlockM - 1;
+
+template <int kDef>
+__global__ void __launch_bounds__(kFaceBlockM) face_update2_hll_pair_kernel(
+    const float* __restrict__ Qh, const float* __restrict__ Ql, float* __restrict__ Qh_out,
+    float* __restrict__ Ql_out, int64_t pitch, int64_t n, Eos2M E, EosPair ep, Quad6F qd,
+    const float* __restrict__ F, int64_t fpitch, const float* __restrict__ smin, const float* __restrict__ smax,
+    const unsigned long long* lam_in, unsigned long long* lam_next, const double* t_in, double* t_out,
+    long long* steps, double t_end, double cfl, float cfl_f, double dx, int bc, DevState* S) {
+  __shared__ float2 sDM[15][kFaceBlockM];  // D- of face 63 b + t, column t
+  double tn = 0.0, lmax = 0.0;
+  int act = 0;
+  float dtdx_0 = 0.0f;
+  if ((threadIdx.x & 31) == 0) {
+    tn = *t_in;
+    act = tn < t_end;
+    lmax = __longlong_as_double((long long)*lam_in);
+    dtdx_0 = cfl_f / (float)lmax;
+  }
+  const bool active = __shfl_sync(0xffffffffu, act, 0) != 0;  // the same in every warp
+  const float dtdx = __shfl_sync(0xffffffffu, dtdx_0, 0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double dt = (cfl * dx) / lmax;
+    *t_out = active ? tn + dt : tn;
+    *lam_next = 0ull;
+    if (active) *steps += 1;
+  }
+  if (!active) return;  // the whole grid
+  const int64_t f = (int64_t)blockIdx.x * kFusedCells + threadIdx.x;  // face between cells f-1 and f
+  float2 dm[15], dp[15];
+  if (f <= n) {
+    const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+    if (L == R) {  // boundary face with a zero-gradient ghost: no jump, no fluctuation
+      for (int k = 0; k < 15; ++k) dm[k] = dp[k] = f2s(0.0f);
+    } else {
+      float2 QL[15], QR[15], fl[15], fr[15];
+      load_face_pairs(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
+      for (int k = 0; k < 15; ++k) fr[k] = f2sub(fr[k], fl[k]);  // f(Q_r) - f(Q_l)
+      const int st = hll_face2_pair<kDef>(E, ep, qd, QL, QR, fr, smin[L], smax[R], dm, dp);
+      if (st) record_err2m(S, st, R);
+    }
+    for (int k = 0; k < 15; ++k) sDM[k][threadIdx.x] = dm[k];
+  }
+  __syncthreads();
+  const int64_t i = f;  // the cell right of this thread's face
+  if (threadIdx.x >= kFusedCells || i >= n) return;
+  const bool frozen = bc == HYP_BC_FROZEN && (i == 0 || i == n - 1);
+#pragma unroll
+  for (int k = 0; k < 15; ++k) {  // variables k and 15 + k: the pair's lanes
+    const float2 m2 = sDM[k][threadIdx.x + 1];
+#pragma unroll
+    for (int ph = 0; ph < 2; ++ph) {
+      const int64_t o = (int64_t)(15 * ph + k) * pitch + i;
+      float h = Qh[o], l = Ql[o];
+      if (!frozen) {
+        const float dmv = ph ? m2.y : m2.x, dpv = ph ? dp[k].y : dp[k].x;
+        const float delta = -dtdx * (0.0f + (dmv + dpv));  // update2_mixed_kernel's form, F_r - F_l = 0
+        const ff q = ff_add_f(ff{h, l}, delta);
+        h = q.hi;
+        l = q.lo;
+      }
+      Qh_out[o] = h;
+      Ql_out[o] = l;
+    }
+  }
+}
+
 // 168 registers (6 blocks of 64 per SM, 48 B of spills): 1.36 against 1.43 ms per LxF
 // step at 2^22 cells with 128 registers and 208 B of spills
 template <int kDef>
@@ -292,6 +366,21 @@ cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
     kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n,
                                               c->smin32, c->smax32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
   }
+  return cudaGetLastError();
+}
+
+bool fused_face_update2_mixed(const hyp_ctx* c) {
+  return c->cfg.flux != HYP_FLUX_LXF && c->mixed_kind == HYP_MIXED_PAIR;
+}
+
+cudaError_t launch_face_update2_mixed(hyp_ctx* c, int p, double t_end) {
+  const double dx = c->cfg.x_length / (double)c->n;
+  auto kern = default_exps(c) ? face_update2_hll_pair_kernel<1> : face_update2_hll_pair_kernel<-1>;
+  const Eos2M E = eos2m(c);
+  kern<<<grid_m(c->n, kFusedCells), kFaceBlockM, 0, c->stream>>>(
+      c->Qh[p], c->Ql[p], c->Qh[1 - p], c->Ql[1 - p], c->mpitch, c->n, E, make_eos_pair(E), to_f(c->quad), c->F32,
+      c->n, c->smin32, c->smax32, &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p], &c->st->t[1 - p],
+      &c->st->steps, t_end, c->cfg.cfl, (float)c->cfg.cfl, dx, c->cfg.bc, c->st);
   return cudaGetLastError();
 }
 

@@ -142,7 +142,9 @@ int hyp_max_wavespeed(hyp_ctx* ctx, double* out);
 int hyp_get_time(const hyp_ctx* ctx, double* t, int64_t* steps);
 
 /* Device timing of the last hyp_step: total elapsed ms, and when profiling is
-   on, the summed ms and launch count of the per-cell flux/wave-speed kernel. */
+   on, each step split in two, summed over the steps with their counts: first the
+   per-cell flux/wave-speed kernel (two phases: with the face kernel, except in the
+   mixed HLL step, whose faces run in one kernel with the update), then the rest. */
 int hyp_set_profiling(hyp_ctx* ctx, int on);
 int hyp_last_timing(const hyp_ctx* ctx, double* ms_total, double* ms_cell_kernel, int* cell_launches,
                     double* ms_update_kernel, int* update_launches);
