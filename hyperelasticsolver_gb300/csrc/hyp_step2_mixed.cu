@@ -140,31 +140,8 @@ __device__ __forceinline__ void store_face_pairs(float* D, int64_t nf, int64_t f
   }
 }
 
-template <int kDef>
-__global__ void __launch_bounds__(kFaceBlockM) face2_hll_pair_kernel(
-    const float* __restrict__ Qh, int64_t pitch, int64_t n, Eos2M E, EosPair ep, Quad6F qd,
-    const float* __restrict__ F, int64_t fpitch, const float* __restrict__ smin, const float* __restrict__ smax,
-    float* __restrict__ DM, float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
-  if (!(*t_now < t_end)) return;
-  const int64_t f = (int64_t)blockIdx.x * kFaceBlockM + threadIdx.x;  // face between cells f-1 and f
-  if (f > n) return;
-  const int64_t nf = n + 1;
-  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
-  float2 dm[15], dp[15];
-  if (L == R) {  // boundary face with a zero-gradient ghost: no jump, no fluctuation
-    for (int k = 0; k < 15; ++k) dm[k] = dp[k] = f2s(0.0f);
-  } else {
-    float2 QL[15], QR[15], fl[15], fr[15];
-    load_face_pairs(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
-    for (int k = 0; k < 15; ++k) fr[k] = f2sub(fr[k], fl[k]);  // f(Q_r) - f(Q_l)
-    const int st = hll_face2_pair<kDef>(E, ep, qd, QL, QR, fr, smin[L], smax[R], dm, dp);
-    if (st) record_err2m(S, st, R);
-  }
-  store_face_pairs(DM, nf, f, dm);
-  store_face_pairs(DP, nf, f, dp);
-}
-
-// The HLL pair face kernel with the update fused in. Block b computes faces
+// The HLL faces on packed pairs (hll_face2_pair) with the update fused in: the
+// default two-phase mixed HLL step (HYP_MIXED_PAIR). Block b computes faces
 // 63 b .. 63 b + 63 (one per thread; the last is computed again by block b + 1 as its
 // first) and updates cells 63 b .. 63 b + 62: cell i from the D+ of its left face i
 // (this thread's) and the D- of its right face i + 1 (the next thread's, through shared
@@ -355,12 +332,8 @@ cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
                                                 c->n, &c->st->lam_bits[p], c->cfg.cfl, c->FF32, c->DM32, c->DP32,
                                                 &c->st->t[p], t_end, c->st);
     }
-  } else if (pair) {
-    auto kern = def ? face2_hll_pair_kernel<1> : face2_hll_pair_kernel<-1>;
-    const Eos2M E = eos2m(c);
-    kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, E, make_eos_pair(E), to_f(c->quad),
-                                              c->F32, c->n, c->smin32, c->smax32, c->DM32, c->DP32, &c->st->t[p],
-                                              t_end, c->st);
+  } else if (pair) {  // runs in face_update2_hll_pair_kernel (launch_face_update2_mixed)
+    return cudaErrorInvalidValue;
   } else {
     auto kern = def ? face2_hll_mixed_kernel<1> : face2_hll_mixed_kernel<-1>;
     kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n,
