@@ -1,5 +1,5 @@
 // hyp_peaks.cu -- the rates this GB300 reaches on the operations the step uses, for
-// the roofline denominators the driver does not measure: FP64 and FP32 fused
+// the roofline denominators beyond the HBM copy and bf16 GEMM rates: FP64 and FP32 fused
 // multiply-add throughput (scalar FP32 and packed f32x2), and the host link
 // (page-locked copies each way and both ways at once).
 //

@@ -86,7 +86,7 @@ const char* hyp_last_error(const hyp_ctx* ctx);
 int64_t hyp_error_cell(const hyp_ctx* ctx);
 
 /* Copy a conservative state in (host SoA [n_vars][n_cells]); resets t to t0.
-   Replaces the driver's Q0 = initial_condition(...) (main.jl:99-106, 178-179). */
+   Replaces main.jl's Q0 = initial_condition(...) (main.jl:99-106, 178-179). */
 int hyp_upload(hyp_ctx* ctx, const double* Q, int64_t n_cells, int n_vars, double t0);
 /* Copy the current conservative state out (host SoA). */
 int hyp_download(hyp_ctx* ctx, double* Q, int64_t n_cells, int n_vars);

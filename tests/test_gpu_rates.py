@@ -1,5 +1,5 @@
-"""The rate micro-benchmarks behind the roofline denominators the driver does not
-measure (hyp_measure_peaks: FMA throughput and host-link copies; hyp_measure_layouts:
+"""The rate micro-benchmarks behind the roofline denominators beyond the HBM copy
+and bf16 GEMM rates (hyp_measure_peaks: FMA throughput and host-link copies; hyp_measure_layouts:
 the mixed step's traffic in the two state layouts): they run, return finite positive
 rates in a plausible order, and reject bad arguments."""
 import ctypes
