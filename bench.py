@@ -519,16 +519,15 @@ def run_mph(args):
                                    "8 cells, phase 2 shear modulus x0.1", "l2": "inputs larger than L2"},
             "precision": "FP32 two-phase physics and fluxes, compensated hi/lo FP32 state, float-float cons2prim "
                          "islands per phase", "clocks": clocks,
-            # the mixed HLL step runs its faces and update in one kernel, after the cell kernel
-            "kernels_ms_per_step": {("cell" if args.flux == "hll" else "cell+face"): tm["ms_cell"] / max(1, tm["n_cell"]),
-                                    ("face+update" if args.flux == "hll" else "update"):
-                                        tm["ms_update"] / max(1, tm["n_update"])},
+            # the mixed step runs its faces and update in one kernel, after the cell kernel
+            "kernels_ms_per_step": {"cell": tm["ms_cell"] / max(1, tm["n_cell"]),
+                                    "face+update": tm["ms_update"] / max(1, tm["n_update"])},
             "roofline": {"bound": "hbm", "achieved": ach, "peak": peak, "unit": "GB/s", "peak_source": peak_kind,
                          "frac": ach / peak,
                          "formulation_flops_per_cell_update": FLOPS_PER_CELL_UPDATE["multi"],
                          "formulation_tflops": FLOPS_PER_CELL_UPDATE["multi"] * n / (ms / 1e3) / 1e12,
-                         "note": "the face kernel (18 evaluations of B per face; with HLL, the update fused "
-                                 "in) is bound by FP32 issue, not HBM"},
+                         "note": "the face kernel (HLL: 18 evaluations of B per face, LxF: 6; the update "
+                                 "fused in) is bound by FP32 issue, not HBM"},
             "fp64": {"value": n * K / (tm64["ms_total"] / 1e3), "ms_per_step": tm64["ms_total"] / K,
                      "kernels_ms_per_step": {"cell+face": tm64["ms_cell"] / max(1, tm64["n_cell"]),
                                              "update": tm64["ms_update"] / max(1, tm64["n_update"])},

@@ -327,7 +327,7 @@ static int enqueue_step(hyp_ctx* c, long long k, double t_end, bool prof) {
   if (c->cfg.model == HYP_MODEL_MULTI && mixed(c)) {
     const int p = (int)(k & 1);
     CK(launch_cell2_mixed(c, p, &c->st->lam_bits[p], &c->st->t[p], t_end));
-    if (fused_face_update2_mixed(c)) {  // profiled as cell, then faces + update
+    if (fused_face_update2_mixed(c)) {  // pair faces; profiled as cell, then faces + update
       if (prof) CK(cudaEventRecord(e1, c->stream));
       CK(launch_face_update2_mixed(c, p, t_end));
     } else {

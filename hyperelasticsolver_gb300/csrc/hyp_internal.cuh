@@ -258,7 +258,7 @@ cudaError_t launch_join_n(cudaStream_t s, const float* hi, const float* lo, doub
 cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, const double* t_now, double t_end);
 cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end);
 cudaError_t launch_update2_mixed(hyp_ctx* c, int p, double t_end);
-// the HLL step's faces and update in one kernel (pair faces): replaces the two launches above
+// the step's pair faces (HLL or LxF) and update in one kernel: replaces the two launches above
 bool fused_face_update2_mixed(const hyp_ctx* c);
 cudaError_t launch_face_update2_mixed(hyp_ctx* c, int p, double t_end);
 int setup_mixed_tma(hyp_ctx* c);

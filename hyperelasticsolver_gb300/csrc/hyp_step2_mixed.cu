@@ -215,27 +215,74 @@ __global__ void __launch_bounds__(kFaceBlockM) face_update2_hll_pair_kernel(
   }
 }
 
-// 168 registers (6 blocks of 64 per SM, 48 B of spills): 1.36 against 1.43 ms per LxF
-// step at 2^22 cells with 128 registers and 208 B of spills
+// The LxF pair faces (lxf_face2_pair) with the update fused in, as
+// face_update2_hll_pair_kernel: cell i from F_{i+1/2} - F_{i-1/2} and D-_{i+1/2} +
+// D+_{i-1/2}, the right face's F and D (D- = D+ for LxF) through shared memory; at most
+// 168 registers (6 blocks of 64 per SM): 1.00 against 1.36 ms per LxF step at 2^22
+// cells with the face and update kernels apart.
 template <int kDef>
-__global__ void __launch_bounds__(kFaceBlockM, 6) face2_lxf_pair_kernel(
-    const float* __restrict__ Qh, int64_t pitch, int64_t n, EosPair ep, Quad6F lobatto, const float* __restrict__ F,
-    int64_t fpitch, const unsigned long long* lam_now, double cfl, float* __restrict__ FF,
-    float* __restrict__ DM, float* __restrict__ DP, const double* t_now, double t_end, DevState* S) {
-  if (!(*t_now < t_end)) return;
-  const int64_t f = (int64_t)blockIdx.x * kFaceBlockM + threadIdx.x;
-  if (f > n) return;
-  const int64_t nf = n + 1;
-  const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
-  const double lmax = __longlong_as_double((long long)*lam_now);
-  const float lam = (float)lmax / (float)cfl;  // lambda = dx/dt = lmax/cfl (main.jl:223), in FP32
-  float2 QL[15], QR[15], fl[15], fr[15], ff_[15], dm[15], dp[15];
-  load_face_pairs(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
-  const int st = lxf_face2_pair<kDef>(ep, lobatto, QL, QR, fl, fr, lam, ff_, dm, dp);
-  if (st) record_err2m(S, st, R);
-  store_face_pairs(FF, nf, f, ff_);
-  store_face_pairs(DM, nf, f, dm);
-  store_face_pairs(DP, nf, f, dp);
+__global__ void __launch_bounds__(kFaceBlockM, 6) face_update2_lxf_pair_kernel(
+    const float* __restrict__ Qh, const float* __restrict__ Ql, float* __restrict__ Qh_out,
+    float* __restrict__ Ql_out, int64_t pitch, int64_t n, EosPair ep, Quad6F lobatto, const float* __restrict__ F,
+    int64_t fpitch, const unsigned long long* lam_in, unsigned long long* lam_next, const double* t_in,
+    double* t_out, long long* steps, double t_end, double cfl, float cfl_f, double dx, int bc, DevState* S) {
+  __shared__ float2 sFF[15][kFaceBlockM], sD[15][kFaceBlockM];
+  double tn = 0.0, lmax = 0.0;
+  int act = 0;
+  float dtdx_0 = 0.0f;
+  if ((threadIdx.x & 31) == 0) {
+    tn = *t_in;
+    act = tn < t_end;
+    lmax = __longlong_as_double((long long)*lam_in);
+    dtdx_0 = cfl_f / (float)lmax;
+  }
+  const bool active = __shfl_sync(0xffffffffu, act, 0) != 0;
+  const float dtdx = __shfl_sync(0xffffffffu, dtdx_0, 0);
+  lmax = __shfl_sync(0xffffffffu, lmax, 0);
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const double dt = (cfl * dx) / lmax;
+    *t_out = active ? tn + dt : tn;
+    *lam_next = 0ull;
+    if (active) *steps += 1;
+  }
+  if (!active) return;
+  const int64_t f = (int64_t)blockIdx.x * kFusedCells + threadIdx.x;
+  float2 ff_[15], dm[15], dp[15];
+  if (f <= n) {
+    const int64_t L = f > 0 ? f - 1 : 0, R = f < n ? f : n - 1;
+    const float lam = (float)lmax / (float)cfl;  // lambda = dx/dt = lmax/cfl (main.jl:223), in FP32
+    float2 QL[15], QR[15], fl[15], fr[15];
+    load_face_pairs(Qh, pitch, F, fpitch, L, R, QL, QR, fl, fr);
+    const int st = lxf_face2_pair<kDef>(ep, lobatto, QL, QR, fl, fr, lam, ff_, dm, dp);
+    if (st) record_err2m(S, st, R);
+    for (int k = 0; k < 15; ++k) {
+      sFF[k][threadIdx.x] = ff_[k];
+      sD[k][threadIdx.x] = dm[k];
+    }
+  }
+  __syncthreads();
+  const int64_t i = f;
+  if (threadIdx.x >= kFusedCells || i >= n) return;
+  const bool frozen = bc == HYP_BC_FROZEN && (i == 0 || i == n - 1);
+#pragma unroll
+  for (int k = 0; k < 15; ++k) {
+    const float2 fr2 = sFF[k][threadIdx.x + 1], dm2 = sD[k][threadIdx.x + 1];
+#pragma unroll
+    for (int ph = 0; ph < 2; ++ph) {
+      const int64_t o = (int64_t)(15 * ph + k) * pitch + i;
+      float h = Qh[o], l = Ql[o];
+      if (!frozen) {
+        const float frv = ph ? fr2.y : fr2.x, flv = ph ? ff_[k].y : ff_[k].x;
+        const float dmv = ph ? dm2.y : dm2.x, dpv = ph ? dp[k].y : dp[k].x;
+        const float delta = -dtdx * ((frv - flv) + (dmv + dpv));  // update2_mixed_kernel's form
+        const ff q = ff_add_f(ff{h, l}, delta);
+        h = q.hi;
+        l = q.lo;
+      }
+      Qh_out[o] = h;
+      Ql_out[o] = l;
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kBlock) update2_mixed_kernel(
@@ -320,20 +367,12 @@ cudaError_t launch_cell2_mixed(hyp_ctx* c, int p, unsigned long long* lam_slot, 
 cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
   const bool def = default_exps(c), pair = c->mixed_kind == HYP_MIXED_PAIR;
   const unsigned grid = grid_m(c->n + 1, kFaceBlockM);
+  if (pair) return cudaErrorInvalidValue;  // the pair faces run with the update (launch_face_update2_mixed)
   if (c->cfg.flux == HYP_FLUX_LXF) {
-    if (pair) {
-      auto kern = def ? face2_lxf_pair_kernel<1> : face2_lxf_pair_kernel<-1>;
-      kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, make_eos_pair(eos2m(c)),
-                                                to_f(c->lobatto), c->F32, c->n, &c->st->lam_bits[p], c->cfg.cfl,
-                                                c->FF32, c->DM32, c->DP32, &c->st->t[p], t_end, c->st);
-    } else {
-      auto kern = def ? face2_lxf_mixed_kernel<1> : face2_lxf_mixed_kernel<-1>;
-      kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->lobatto), c->F32,
-                                                c->n, &c->st->lam_bits[p], c->cfg.cfl, c->FF32, c->DM32, c->DP32,
-                                                &c->st->t[p], t_end, c->st);
-    }
-  } else if (pair) {  // runs in face_update2_hll_pair_kernel (launch_face_update2_mixed)
-    return cudaErrorInvalidValue;
+    auto kern = def ? face2_lxf_mixed_kernel<1> : face2_lxf_mixed_kernel<-1>;
+    kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->lobatto), c->F32, c->n,
+                                              &c->st->lam_bits[p], c->cfg.cfl, c->FF32, c->DM32, c->DP32,
+                                              &c->st->t[p], t_end, c->st);
   } else {
     auto kern = def ? face2_hll_mixed_kernel<1> : face2_hll_mixed_kernel<-1>;
     kern<<<grid, kFaceBlockM, 0, c->stream>>>(c->Qh[p], c->mpitch, c->n, eos2m(c), to_f(c->quad), c->F32, c->n,
@@ -342,12 +381,19 @@ cudaError_t launch_face2_mixed(hyp_ctx* c, int p, double t_end) {
   return cudaGetLastError();
 }
 
-bool fused_face_update2_mixed(const hyp_ctx* c) {
-  return c->cfg.flux != HYP_FLUX_LXF && c->mixed_kind == HYP_MIXED_PAIR;
-}
+// Both fluxes' pair faces run with the update; the scalar faces (HYP_MIXED_TILE) apart.
+bool fused_face_update2_mixed(const hyp_ctx* c) { return c->mixed_kind == HYP_MIXED_PAIR; }
 
 cudaError_t launch_face_update2_mixed(hyp_ctx* c, int p, double t_end) {
   const double dx = c->cfg.x_length / (double)c->n;
+  if (c->cfg.flux == HYP_FLUX_LXF) {
+    auto kern = default_exps(c) ? face_update2_lxf_pair_kernel<1> : face_update2_lxf_pair_kernel<-1>;
+    kern<<<grid_m(c->n, kFusedCells), kFaceBlockM, 0, c->stream>>>(
+        c->Qh[p], c->Ql[p], c->Qh[1 - p], c->Ql[1 - p], c->mpitch, c->n, make_eos_pair(eos2m(c)), to_f(c->lobatto),
+        c->F32, c->n, &c->st->lam_bits[p], &c->st->lam_bits[1 - p], &c->st->t[p], &c->st->t[1 - p], &c->st->steps,
+        t_end, c->cfg.cfl, (float)c->cfg.cfl, dx, c->cfg.bc, c->st);
+    return cudaGetLastError();
+  }
   auto kern = default_exps(c) ? face_update2_hll_pair_kernel<1> : face_update2_hll_pair_kernel<-1>;
   const Eos2M E = eos2m(c);
   kern<<<grid_m(c->n, kFusedCells), kFaceBlockM, 0, c->stream>>>(

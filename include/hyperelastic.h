@@ -179,8 +179,8 @@ int hyp_step_noalloc_f64(const hyp_config* cfg, const double* d_Q_in, double* d_
    error).
    Two-phase: HYP_MIXED_TILE, the face kernels with both phases in scalar FP32 and
    a separate update kernel; HYP_MIXED_PAIR (the default), the face kernels with the
-   two phases as the lanes of packed FP32 pairs, with HLL faces computing the update
-   in the same kernel. HYP_MIXED_TMA is single-phase only.
+   two phases as the lanes of packed FP32 pairs, computing the update in the same
+   kernel. HYP_MIXED_TMA is single-phase only.
    Returns HYP_ERR_UNSUPPORTED for FP64 contexts, an unknown kind, or TMA where it
    is not available; the CUDA graphs of the previous kernel are dropped. */
 enum { HYP_MIXED_TILE = 0, HYP_MIXED_TMA = 1, HYP_MIXED_PAIR = 2 };

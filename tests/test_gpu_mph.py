@@ -271,24 +271,25 @@ def test_nondefault_exponents_twophase(hyp, orc, flux, kernel):
     assert max(e[0] for e in errs) <= 1e-6
 
 
+@pytest.mark.parametrize("flux", ["hll", "lxf"])
 @pytest.mark.parametrize("bc", ["frozen", "transmissive"])
 @pytest.mark.parametrize("nx", [5, 63, 64, 126, 127, 400])
-def test_fused_hll_face_update_blocks(hyp, orc, nx, bc):
-    """The mixed HLL step with paired faces runs its faces and update in one kernel
-    (63 cells per block, each block computing its right neighbour's first face again);
-    the scalar faces run them as two kernels. Across block edges (nx around multiples
+def test_fused_face_update_blocks(hyp, orc, nx, bc, flux):
+    """The mixed step with paired faces runs its faces and update in one kernel (63
+    cells per block, each block computing its right neighbour's first face again); the
+    scalar faces run them as two kernels. Across block edges (nx around multiples
     of 63) and with both end rules the two agree to FP32 rounding after 40 steps (the
     paired and scalar faces round alike, not identically): each variable within 1e-4 of
-    its scale (measured up to 1.7e-6 on 5 cells, where every cell moves), each phase's
-    density within 1e-6 in L1 (measured 1.2e-8). A fluctuation taken from the wrong
-    face, or a cell updated twice or not at all, is an O(1) error."""
+    its scale (HLL: measured up to 1.7e-6 on 5 cells, where every cell moves), each
+    phase's density within 1e-6 in L1 (HLL: measured 1.2e-8). A fluctuation taken
+    from the wrong face, or a cell updated twice or not at all, is an O(1) error."""
     from hyperelasticsolver_gb300._cases import mph_case, initial_condition
     pb = oracle_pb(orc, nx=nx, cfl=0.6)
     Pl, Pr = mph_case(6)
     Q0 = initial_condition(orc.prim2cons(pb, Pl), orc.prim2cons(pb, Pr), nx)
     out = {}
     for kernel in KERNELS:
-        with hyp.Solver(eos_pair(hyp), nx, model="multi", flux="hll", precision="mixed", bc=bc, cfl=0.6) as s:
+        with hyp.Solver(eos_pair(hyp), nx, model="multi", flux=flux, precision="mixed", bc=bc, cfl=0.6) as s:
             s.set_mixed_kernel(kernel)
             s.upload(Q0)
             n, t = s.step(max_steps=40)
